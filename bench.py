@@ -1,0 +1,409 @@
+"""Benchmark: Heston Monte Carlo path-steps/s on one GB300 (or N ranks).
+
+Workload (one "step"): full-truncation Euler Heston in FP32, kappa=2.0,
+theta=0.04, xi=0.3, rho=-0.7, v0=0.04, S0=100, r=0.02, 2^22 paths, 252 steps
+to T=1, Philox4x32-10 draws generated in-kernel, a batch of 64 European call
+strikes uniform in [70, 130] (fixed seed), FP64 cross-path accumulation of
+payoff sums and sums of squares — one fused kernel pass plus the fixed-order
+partial-sum reduction.  `value` = paths x steps x ranks / max-over-ranks
+device time per step.
+
+`--impl reference` times the reference algorithm on the host cores: the
+oracle's NumPy restatement of euler_sampling.sample with the same Heston
+full-truncation coefficients (TensorFlow itself cannot be installed on
+these machines), run on every host core over a bounded path sample.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "tf-quant-finance_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Heston path-steps/s"
+UNIT = "path-steps/s"
+N_PATHS = 1 << 22
+N_STEPS = 252
+N_STRIKES = 64
+PARAMS = dict(spot=100.0, variance=0.04, mean_reversion=2.0, theta=0.04, volvol=0.3, rho=-0.7,
+              discount_rate=0.02, expiry=1.0)
+# Algorithmic 32-bit lane operations per path-step of the fused kernel (see
+# DESIGN.md, "Roofline accounting"): Philox4x32-10 half block (40: per round
+# 4 multiplies, 2 three-input XORs, 2 key adds; 10 rounds per 2 steps), one
+# Box–Muller pair (14: two uniform conversions, lg2, scale, sqrt, angle,
+# sin, cos, two products) and the full-truncation step (14: max, sqrt, two
+# dW products, 3 ops log-spot, 7 ops variance).
+ALU_OPS_PER_PATH_STEP = 40 + 14 + 14
+# DRAM bytes per launch measured by ncu on this kernel (2^22 paths x 252 steps):
+# see profiles/heston_ft_f32_2p22x252.md.  None until captured.
+NCU_TRAFFIC_BYTES = None
+
+
+def strikes():
+    return np.sort(np.random.default_rng(2024).uniform(70.0, 130.0, N_STRIKES))
+
+
+def workload_config(n_paths, n_steps, world):
+    return {"workload": f"Heston full-truncation Euler FP32, {n_paths} paths x {n_steps} steps to T=1, "
+                        f"Philox4x32-10 in-kernel, 64 European strikes in [70,130], FP64 accumulation",
+            "paths_per_rank": n_paths, "time_steps": n_steps, "strikes": N_STRIKES,
+            "params": PARAMS, "parallelism": f"path-sharded x{world}" if world > 1 else "single GPU",
+            "l2": "L2 flushed (256 MiB write) between timed steps"}
+
+
+# ---------------------------------------------------------------- CPU side
+def _cpu_worker(args):
+    n_paths, n_steps, seed = args
+    from oracle import euler as oeuler
+    p = PARAMS
+    dtype = np.float32
+    rng = np.random.default_rng(seed)
+    drift, vol = oeuler.heston_ft_coefficients(p["discount_rate"], p["mean_reversion"], p["theta"], p["volvol"],
+                                               p["rho"], dtype)
+    t0 = time.perf_counter()
+    all_t = np.linspace(0, p["expiry"], n_steps + 1).astype(dtype)
+    keep = np.zeros(n_steps + 1, bool)
+    keep[-1] = True
+    draws = rng.standard_normal((n_steps, n_paths, 2), dtype=np.float32)
+    x0 = np.tile(np.array([np.log(p["spot"]), p["variance"]], dtype), (n_paths, 1))
+    out = oeuler.sample_with_draws(drift, vol, all_t, keep, 1, x0, draws, dtype)
+    S = np.exp(out[:, 0, 0].astype(np.float64))
+    k = strikes()
+    pay = np.maximum(S[:, None] - k[None, :], 0.0)
+    _ = pay.sum(0), (pay * pay).sum(0)
+    return time.perf_counter() - t0, n_paths * n_steps
+
+
+def cpu_reference_step(pool, cores, paths_per_core, n_steps, seed):
+    t0 = time.perf_counter()
+    res = pool.map(_cpu_worker, [(paths_per_core, n_steps, seed * 1000 + i) for i in range(cores)])
+    wall = time.perf_counter() - t0
+    units = sum(r[1] for r in res)
+    return units, wall
+
+
+def run_cpu_baseline(steps, warmup, budget_s=12.0):
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    paths_per_core = 4096
+    with ctx.Pool(cores) as pool:
+        # calibrate the sample so that one step takes about budget_s / steps
+        units, wall = cpu_reference_step(pool, cores, 512, N_STEPS, 0)
+        rate = units / wall
+        target = max(budget_s / max(steps + warmup, 1), 0.5)
+        paths_per_core = int(max(256, min(1 << 16, rate * target / (cores * N_STEPS))))
+        for w in range(warmup):
+            cpu_reference_step(pool, cores, paths_per_core, N_STEPS, 1 + w)
+        tot_units, tot_wall = 0, 0.0
+        for s in range(steps):
+            u, t = cpu_reference_step(pool, cores, paths_per_core, N_STEPS, 100 + s)
+            tot_units += u
+            tot_wall += t
+    return tot_units / tot_wall, cores, paths_per_core, tot_wall / steps
+
+
+# ---------------------------------------------------------------- GPU side
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append((time.time(), [c.strip() for c in line.split(",")]))
+
+    def mark(self, start=True):
+        if start:
+            self.t0 = time.time()
+        else:
+            self.t1 = time.time()
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread is not None:
+                self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        t0, t1 = getattr(self, "t0", 0.0), getattr(self, "t1", float("inf"))
+        for ts, r in self.rows:
+            if ts < t0 or ts > t1 + 0.25:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def fma_peak(torch, L):
+    """FP32 FMA lane-ops/s of this GPU (probe kernel, best of 5)."""
+    import ctypes
+    dev = torch.device("cuda", torch.cuda.current_device())
+    out = torch.zeros(1, dtype=torch.float32, device=dev)
+    lane_ops = ctypes.c_double(0)
+    s = torch.cuda.current_stream()
+    best = 0.0
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        L.call("tqf_fma_peak_probe", 4096, 8, out.data_ptr(), ctypes.byref(lane_ops), s.cuda_stream)
+        e1.record(s)
+        e1.synchronize()
+        best = max(best, lane_ops.value / (e0.elapsed_time(e1) * 1e-3))
+    return best
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+    import tqf._lib as L
+    from tqf.math.random import RandomType
+    from tqf.pricing import heston_european_mc
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    n_paths, n_steps = args.paths, args.time_steps
+    k = strikes()
+    kw = dict(strikes=k, num_samples=n_paths, num_time_steps=n_steps, scheme="full_truncation",
+              random_type=RandomType.STATELESS, seed=[20240, 7], path_offset=rank * n_paths, **PARAMS)
+
+    # Device-resident pieces for the kernel-only timing: everything a step needs
+    # is built once; a timed step is the fused kernel + partial-sum reduction.
+    import ctypes
+    from tqf.models import heston_model
+    from tqf.models.coefficients import HestonFullTruncation
+    from tqf.models import utils
+    from tqf.math.random import multivariate_normal as mvn
+    from tqf.pricing.european import make_payoff, stats_from_sums
+    p = PARAMS
+    all_t = np.linspace(0.0, p["expiry"], n_steps + 1).astype(np.float32)
+    dt = (all_t[1:] - all_t[:-1]).astype(np.float32)
+    h = HestonFullTruncation(p["discount_rate"], p["mean_reversion"], p["theta"], p["volvol"], p["rho"])
+    rows = heston_model.full_truncation_table(h, all_t, dt, np.sqrt(dt).astype(np.float32),
+                                              np.full(n_steps, -1, np.int32), n_steps)
+    table = utils.step_table(rows, torch.float32, dev)
+    pay, out, keep = make_payoff(k, None, torch.float32, dev, n_paths,
+                                 lambda ns: L.load().tqf_heston_workspace_bytes(0, 0, n_paths, ns), "bench")
+    hargs = L.HestonArgs()
+    hargs.dtype = L.TQF_F32
+    hargs.num_steps = n_steps
+    hargs.num_paths = n_paths
+    hargs.step_table = table.data_ptr()
+    hargs.x0, hargs.v0 = math.log(p["spot"]), p["variance"]
+    hargs.draws = mvn.philox_draws(RandomType.STATELESS, [20240, 7], n_paths, rank * n_paths)
+    hargs.payoff = pay
+    hargs.dev_status = L.status_buffer(dev).data_ptr()
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def kernel_step():
+        L.call("tqf_heston_euler", hargs, stream.cuda_stream)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        kernel_step()
+        flush.fill_(1)
+    barrier()
+    launches0 = L.launch_count()
+    times_ms = []
+    with ClockSampler(local_rank) as clocks:
+        time.sleep(1.0)  # let the sampler start before the timed region
+        clocks.mark(True)
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            kernel_step()
+            e1.record(stream)
+            flush.fill_(1)  # evict L2 between timed steps (outside the events)
+            times_ms.append((e0, e1))
+        barrier()
+        wall = time.perf_counter() - t_wall0
+        clocks.mark(False)
+    launches = L.launch_count() - launches0
+    per_step = [a.elapsed_time(b) for a, b in times_ms]
+    ms = sum(per_step) / len(per_step)
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    L.check_device_status(dev)
+    res = stats_from_sums(out, n_paths, math.exp(-p["discount_rate"] * p["expiry"]))
+    value = n_paths * n_steps * world / (ms * 1e-3)
+
+    # The dominant kernel's own duration: the fused path kernel alone
+    # (payoff.out = NULL leaves the partial sums in the workspace and skips
+    # the reduction launch), timed by events on the launching stream.
+    kargs = L.HestonArgs()
+    ctypes.memmove(ctypes.byref(kargs), ctypes.byref(hargs), ctypes.sizeof(L.HestonArgs))
+    kargs.payoff.out = None
+    hk = []
+    for _ in range(max(3, min(args.steps, 10))):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.call("tqf_heston_euler", kargs, stream.cuda_stream)
+        e1.record(stream)
+        flush.fill_(1)
+        hk.append((e0, e1))
+    torch.cuda.synchronize()
+    step_ms = sum(a.elapsed_time(b) for a, b in hk) / len(hk)
+
+    # End to end through the public API with host buffers: strikes from pinned
+    # host memory, results read back each step.
+    k_host = torch.from_numpy(k.astype(np.float32)).pin_memory()
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = heston_european_mc(**{**kw, "strikes": k_host})
+        price = r.price.cpu()
+        se = r.standard_error.cpu()
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_times.append(t1 - t0)
+    e2e_s = sum(e2e_times) / len(e2e_times)
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+        dist.all_reduce(out, op=dist.ReduceOp.SUM)
+
+    peaks, peak_kind = measured_peaks()
+    fp32_peak = fma_peak(torch, L)
+    alg_ops = ALU_OPS_PER_PATH_STEP * n_paths * n_steps
+    achieved = alg_ops / (step_ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox draws, fixed strikes)",
+        "config": workload_config(n_paths, n_steps, world),
+        "e2e": {"value": n_paths * n_steps * world / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": int(k.size * 4), "d2h_bytes_per_step": int(2 * k.size * 8),
+                "api": "tqf.pricing.heston_european_mc (host strikes -> device prices)"},
+        "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": fp32_peak / 1e12,
+                     "unit": "T lane-op/s", "frac": achieved / fp32_peak, "traffic": NCU_TRAFFIC_BYTES,
+                     "kernel": "heston_kernel<float, FT, PHILOX, store=0, price=1>",
+                     "kernel_ms": step_ms, "alg_ops_per_path_step": ALU_OPS_PER_PATH_STEP,
+                     "peak_source": "tqf_fma_peak_probe measured live (FP32 FMA lane-ops/s)",
+                     "hbm_peak_gbs": peaks.get("hbm_gbs"), "hbm_peak_kind": peak_kind},
+        "gpu_launches": int(launches),
+        "wall_s_timed_region": wall,
+        "clocks": clocks.summary(),
+        "result_check": {"atm_call_price": float(res.price[int(np.argmin(np.abs(k - 100)))]),
+                         "strike": float(k[int(np.argmin(np.abs(k - 100)))]),
+                         "se": float(res.standard_error[int(np.argmin(np.abs(k - 100)))])},
+    }
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["tqf", "reference"], default="tqf")
+    ap.add_argument("--paths", type=int, default=N_PATHS)
+    ap.add_argument("--time-steps", type=int, default=N_STEPS)
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "tqf" else args.warmup
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        rate, cores, ppc, step_s = run_cpu_baseline(args.steps, args.warmup, args.cpu_budget)
+        sample = f"oracle full-truncation Euler (numpy f32) {cores} procs x {ppc} paths x {N_STEPS} steps per step, incl. RNG + 64-strike payoff"
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(args.paths, args.time_steps, 1),
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }))
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # CPU sample first (spawned workers, before any CUDA context exists).
+        rate, cores, ppc, _ = run_cpu_baseline(2, 1, args.cpu_budget)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"oracle full-truncation Euler (numpy f32), {cores} procs x {ppc} paths x {N_STEPS} steps, 2 timed rounds, incl. RNG + 64-strike payoff"}
+    line = run_gpu(args, rank, world, local_rank)
+    if rank == 0:
+        line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,283 @@
+/*
+ * tqf.h — C ABI of the GB300 (sm_103a) Monte Carlo engine for the SDE
+ * path-simulation hot path of tf-quant-finance.
+ *
+ * Every entry point is asynchronous on the caller's CUDA stream (`stream`, a
+ * cudaStream_t passed as void*), allocates no device memory, never throws and
+ * returns an int status: TQF_OK (0) or a negative TQF_E_* code, with a
+ * message readable through tqf_last_error() on the calling thread.  All
+ * buffers are caller-owned device pointers unless a parameter says "host".
+ *
+ * Random draws follow one canonical layout, shared by every kernel: the draw
+ * for path n and draw dimension k (k = step * num_normal_draws + component,
+ * the dimension order of tff/models/utils.py:95-127) is a pure function of
+ * (key, n, k), so fused in-kernel generation and materialised draws agree and
+ * a path range can be resumed or sharded by `path_offset`.
+ */
+#ifndef TQF_H_
+#define TQF_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define TQF_API __attribute__((visibility("default")))
+#else
+#define TQF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define TQF_OK 0
+#define TQF_E_INVALID (-1)     /* bad argument (shape, size, null pointer) */
+#define TQF_E_CUDA (-2)        /* a CUDA runtime call failed */
+#define TQF_E_UNSUPPORTED (-3) /* valid request outside what is built */
+#define TQF_E_TIMEOUT (-4)     /* a bounded device-side wait ran out */
+#define TQF_E_IO (-5)          /* host file could not be read/parsed */
+
+/* ---- dtypes / enums ------------------------------------------------------ */
+#define TQF_F32 0
+#define TQF_F64 1
+
+#define TQF_DRAWS_MEMORY 0 /* read normals from `tqf_draws.ptr` with strides */
+#define TQF_DRAWS_PHILOX 1 /* generate them in-kernel (Philox4x32-10) */
+
+/* Sobol output kinds (tqf_sobol_sample / tqf_sobol_normal_draws). */
+#define TQF_SOBOL_U32 0        /* integer at the reference's nd-digit scaling */
+#define TQF_SOBOL_F32 1        /* float32(int) * 2^-nd (reference float) */
+#define TQF_SOBOL_F64 2        /* float64(int) * 2^-nd */
+#define TQF_SOBOL_NORMAL_F32 3 /* erfinv((u-0.5)*2)*sqrt(2) on the f32 value */
+#define TQF_SOBOL_NORMAL_F64 4 /* same on the f64 value */
+#define TQF_SOBOL_F32_CENTERED 5 /* (int + 0.5) * 2^-nd: strictly inside (0,1) */
+
+/* ---- shared argument blocks --------------------------------------------- */
+
+/* Source of the N(0,1) draws consumed by a path kernel.  Memory draws are
+ * addressed as ptr[step*stride_step + path*stride_path + comp*stride_comp]
+ * (elements of the kernel's dtype), so both the reference's [steps, N, d]
+ * layout and the caller-facing [N, steps, d] layout are read without a
+ * transpose copy.  Philox draws use key (key0, key1) and the canonical
+ * counter layout; `antithetic` makes paths [half, 2*half) the negation of
+ * paths [0, half) (tff/math/random_ops/multivariate_normal.py:276-311). */
+typedef struct tqf_draws {
+  int32_t source;
+  int32_t antithetic;
+  const void* ptr;
+  int64_t stride_step;
+  int64_t stride_path;
+  int64_t stride_comp;
+  uint32_t key0;
+  uint32_t key1;
+  int64_t path_offset;
+  int64_t antithetic_half;
+} tqf_draws;
+
+/* Recorded output: paths[N, num_slots, dim] in the kernel's dtype.  The
+ * state after step i is stored to the slot held (as an exact integer value,
+ * -1 = none) in the last column of row i of the kernel's step table, and the
+ * initial state to init_slot (-1 = none).  The host derives the slots from
+ * the reference's written_count/keep_mask recursion
+ * (tff/models/euler_sampling.py:424-455). */
+typedef struct tqf_path_output {
+  void* ptr;
+  int32_t num_slots;
+  int32_t init_slot;
+} tqf_path_output;
+
+/* Fused European payoff over the final state: for each strike j the kernel
+ * accumulates, in FP64 across paths, sum_p f_j(S_p) and sum_p f_j(S_p)^2 with
+ * f_j = max(S - K_j, 0) (call) or max(K_j - S, 0) (put) and
+ * S = spot_scale * exp(state[0]) (log-spot models) or state[0] (level models,
+ * see each entry point).  out[2*j] = sum, out[2*j+1] = sum of squares.
+ * `workspace` holds per-CTA partial sums; its size is given by the matching
+ * *_workspace_bytes query.  With out == NULL the path kernels leave the
+ * partial sums in the workspace and skip the reduction launch.  Results are deterministic (fixed summation order)
+ * for a given device and launch shape. */
+typedef struct tqf_payoff {
+  int32_t num_strikes; /* 0 disables the payoff */
+  int32_t pad0;
+  const void* strikes;    /* device, [num_strikes], kernel dtype */
+  const uint8_t* is_call; /* device, [num_strikes] or NULL (all calls) */
+  double spot_scale;
+  double* out;            /* device, [num_strikes * 2] */
+  void* workspace;
+  size_t workspace_bytes;
+} tqf_payoff;
+
+/* ---- library ------------------------------------------------------------- */
+
+/* ABI version (major*100 + minor). */
+TQF_API int tqf_abi_version(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+TQF_API const char* tqf_last_error(void);
+
+/* Number of kernels this library has launched in the process (all threads);
+ * used to count kernel launches inside a timed region. */
+TQF_API uint64_t tqf_launch_count(void);
+
+/* FP32-pipe peak probe (no reference counterpart; roofline denominator):
+ * launches SMs x blocks_per_sm CTAs of 256 threads running independent FMA
+ * chains and stores the number of FMA lane operations issued in *lane_ops
+ * (host).  Time it with events on `stream`. */
+TQF_API int tqf_fma_peak_probe(int32_t iters, int32_t blocks_per_sm, float* out, double* lane_ops,
+                               void* stream);
+
+/* ---- Sobol (tff/math/random_ops/sobol/sobol_impl.py) --------------------- */
+
+/* Host-only.  Parses the Joe–Kuo file (new-joe-kuo-6.21201) and writes the
+ * 32-bit direction numbers v[d*32 + j] = m_dj << (31 - j) for dimensions
+ * 0..dim-1 (dimension 0: all m = 1).  Replaces _compute_direction_numbers
+ * and load_data (sobol_impl.py:171-197, 237-261). */
+TQF_API int tqf_sobol_direction_numbers(const char* joe_kuo_path, int32_t dim,
+                                uint32_t* v_host);
+
+/* Number of binary digits the reference uses for a request:
+ * ceil(log(skip + num_results + 1) / log 2) (sobol_impl.py:118-123). */
+TQF_API int32_t tqf_sobol_num_digits(int64_t num_results, int64_t skip);
+
+/* out[n, d] for n in [0, num_results), d in [0, dim): Sobol point with
+ * sequence index skip + 1 + n (natural order), scaled to nd digits, written
+ * as `out_kind`.  v_dev is the device copy of tqf_sobol_direction_numbers.
+ * Replaces sobol.sample (sobol_impl.py:39-167). */
+TQF_API int tqf_sobol_sample(const uint32_t* v_dev, int32_t dim, int64_t num_results,
+                     int64_t skip, int32_t nd, int32_t out_kind, void* out,
+                     void* stream);
+
+/* Normal draws in the reference's path-simulation layout
+ * out[i, n, c] = normal(point skip+1+n, dimension i*num_normal_draws + c),
+ * shape [num_steps, num_paths, num_normal_draws]; out_kind is
+ * TQF_SOBOL_NORMAL_F32 or TQF_SOBOL_NORMAL_F64.  Replaces the SOBOL branch
+ * of generate_mc_normal_draws (tff/models/utils.py:20-128,
+ * multivariate_normal.py:356-424). */
+TQF_API int tqf_sobol_normal_draws(const uint32_t* v_dev, int32_t num_normal_draws,
+                           int32_t num_steps, int64_t num_paths, int64_t skip,
+                           int32_t nd, int32_t out_kind, void* out,
+                           void* stream);
+
+/* ---- Philox draws (PSEUDO / STATELESS / *_ANTITHETIC) -------------------- */
+
+/* Raw Philox4x32-10 blocks: out[4*b + l] = philox(ctr=(ctr0+b, c1, c2, c3),
+ * key)[l] for b in [0, num_blocks).  Known-answer testing of the generator. */
+TQF_API int tqf_philox4x32_10(uint32_t ctr0, uint32_t c1, uint32_t c2, uint32_t c3,
+                      uint32_t key0, uint32_t key1, int64_t num_blocks,
+                      uint32_t* out, void* stream);
+
+/* Materialised normal draws out[i, n, c] (shape [num_steps, num_paths,
+ * num_normal_draws], dtype TQF_F32/TQF_F64) from the canonical stream of
+ * `draws` (source must be TQF_DRAWS_PHILOX).  Replaces the PSEUDO/STATELESS
+ * branches of generate_mc_normal_draws (tff/models/utils.py:20-128,
+ * multivariate_normal.py:248-311). */
+TQF_API int tqf_philox_normal_draws(const tqf_draws* draws, int32_t num_normal_draws,
+                            int32_t num_steps, int64_t num_paths, int32_t dtype,
+                            void* out, void* stream);
+
+/* ---- Euler–Maruyama (tff/models/euler_sampling.py) ----------------------- */
+
+/* Structured coefficients of dX = a(X) dt + B(X) dW, dim <= 16:
+ *   a(x)   = drift_m + drift_M x                       ([dim], [dim, dim])
+ *   B(x)ij = (vol_s0_i + vol_s1_i x_i) vol_C_ij        ([dim], [dim], [dim, dim])
+ * (GBM, arithmetic BM, OU, correlated GBM in levels).  step_table is
+ * [num_steps][4] = (dt_i, sqrt(dt_i), slot_i, 0).  x0 is [dim] or [num_paths, dim]
+ * (x0_per_path = 1).  One kernel pass, state in registers; replaces the
+ * while-loop body _euler_step (euler_sampling.py:513-537). */
+typedef struct tqf_euler_affine_args {
+  int32_t dtype;
+  int32_t dim;
+  int64_t num_paths;
+  int32_t num_steps;
+  int32_t x0_per_path;
+  const void* step_table;
+  const void* x0;
+  const void* drift_m;
+  const void* drift_M;
+  const void* vol_s0;
+  const void* vol_s1;
+  const void* vol_C;
+  tqf_draws draws;
+  tqf_path_output output;
+  int32_t* dev_status; /* device int or NULL: set to TQF_E_TIMEOUT on a timed-out wait */
+} tqf_euler_affine_args;
+
+TQF_API int tqf_euler_affine(const tqf_euler_affine_args* args, void* stream);
+
+/* One Euler step for arbitrary coefficients evaluated by the caller:
+ * x_next = x + dt * a + B · (z * sqrt_dt), x/a [num_paths, dim], B
+ * [num_paths, dim, dim] row-major, z from `draws` at `step`.  If
+ * out_slot >= 0 the new state is also stored to output.ptr[:, out_slot, :].
+ * (euler_sampling.py:519-530). */
+typedef struct tqf_euler_update_args {
+  int32_t dtype;
+  int32_t dim;
+  int64_t num_paths;
+  int32_t step;
+  int32_t out_slot;
+  double dt;
+  double sqrt_dt;
+  const void* x;
+  const void* drift;
+  const void* vol;
+  void* x_next;
+  tqf_draws draws;
+  void* paths_out;
+  int32_t num_slots;
+  int32_t pad0;
+} tqf_euler_update_args;
+
+TQF_API int tqf_euler_update(const tqf_euler_update_args* args, void* stream);
+
+/* Full-truncation Euler for the Heston model in log-spot form, as the
+ * reference Euler sampler runs it with drift [r - v+/2, kappa (theta - v+)]
+ * and volatility [[sqrt v+, 0], [xi rho sqrt v+, xi sqrt(1-rho^2) sqrt v+]],
+ * v+ = max(v, 0), coefficients evaluated at t_{i+1}.  step_table is
+ * [num_steps][8] = (dt, sqrt_dt, r, kappa, theta, xi*rho,
+ * xi*sqrt(1-rho^2), slot).  Component 0 of the draws drives the log-spot.
+ * Optional path store and fused European payoff (S = spot_scale*exp(x_T)). */
+typedef struct tqf_heston_args {
+  int32_t dtype;
+  int32_t num_steps;
+  int64_t num_paths;
+  const void* step_table;
+  double x0;
+  double v0;
+  tqf_draws draws;
+  tqf_path_output output;
+  tqf_payoff payoff;
+  int32_t* dev_status;
+} tqf_heston_args;
+
+TQF_API int tqf_heston_euler(const tqf_heston_args* args, void* stream);
+
+/* Andersen QE scheme exactly as HestonModel.sample_paths runs it
+ * (tff/models/heston/heston_model.py:322-460, 522-572): step_table is
+ * [num_steps][12] = (skip, theta, E=exp(-kappa dt), A, B, k0, k1, k2, k3,
+ * k4, 0, slot) with s^2 = v A + B; skip != 0 marks dt <= tolerance steps that
+ * consume draws but leave the state unchanged.  Component 0 of the draws
+ * drives the variance, component 1 the log-spot; output slots hold
+ * (log-spot, variance). */
+TQF_API int tqf_heston_qe(const tqf_heston_args* args, void* stream);
+
+/* Workspace bytes that tqf_heston_euler / tqf_heston_qe need in
+ * payoff.workspace for a given dtype, path count and strike count. */
+TQF_API size_t tqf_heston_workspace_bytes(int32_t dtype, int32_t qe, int64_t num_paths,
+                                  int32_t num_strikes);
+
+/* ---- payoff reduction over stored values ----------------------------------- */
+
+/* FP64 sums of European payoffs over values[p * stride] for p < num_values
+ * (level model: S = spot_scale * values, or log model: S = spot_scale *
+ * exp(values) when log_values != 0).  Same output layout as tqf_payoff. */
+TQF_API int tqf_european_payoff_sums(int32_t dtype, const void* values, int64_t stride,
+                             int64_t num_values, int32_t log_values,
+                             const tqf_payoff* payoff, void* stream);
+
+TQF_API size_t tqf_european_workspace_bytes(int64_t num_values, int32_t num_strikes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TQF_H_ */

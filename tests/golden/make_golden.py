@@ -1,0 +1,75 @@
+"""Extracts the reference's known-answer vectors for the hot path into
+sobol_golden.json / heston_golden.json.
+
+Run in a checkout that has the reference sources (read as text; TensorFlow is
+not needed):  python tests/golden/make_golden.py /path/to/tf-quant-finance
+"""
+
+import ast
+import json
+import os
+import sys
+
+
+def _literal_assignments(path, func_name):
+    tree = ast.parse(open(path).read())
+    out = {}
+    for node in ast.walk(tree):
+        if isinstance(node, ast.FunctionDef) and node.name == func_name:
+            for stmt in ast.walk(node):
+                if isinstance(stmt, ast.Assign) and len(stmt.targets) == 1 and isinstance(stmt.targets[0], ast.Name):
+                    try:
+                        out[stmt.targets[0].id] = ast.literal_eval(stmt.value)
+                    except ValueError:
+                        pass
+    return out
+
+
+def main(ref_root):
+    tff = os.path.join(ref_root, "tf_quant_finance")
+    sob = os.path.join(tff, "math", "random_ops", "sobol", "sobol_test.py")
+    more = _literal_assignments(sob, "test_more_known_values")["expected"]
+    large = _literal_assignments(sob, "test_large_skip")
+    src = open(sob).read()
+    # test_known_values_small_dimension builds its array inline: np.array([...])
+    tree = ast.parse(src)
+    small = None
+    for node in ast.walk(tree):
+        if isinstance(node, ast.FunctionDef) and node.name == "test_known_values_small_dimension":
+            for call in ast.walk(node):
+                if isinstance(call, ast.Call) and getattr(call.func, "attr", "") == "array" and call.args:
+                    small = ast.literal_eval(call.args[0])
+    golden = {
+        "source": "tf_quant_finance/math/random_ops/sobol/sobol_test.py",
+        "dim2_first5": {"dim": 2, "num_results": 5, "skip": 0, "expected": small},
+        "dim5_first31_gray_order": {"dim": 5, "num_results": 31, "skip": 0, "expected": more},
+        "large_skip": {"dim": large["dim"], "num_results": large["num_results"],
+                       "skip_expr": "2**31 - 5", "skip": 2 ** 31 - 5,
+                       "expected": [[0.25], [0.75], [0.5]]},
+    }
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "sobol_golden.json"), "w") as f:
+        json.dump(golden, f, indent=1)
+    hest = {
+        "source": ["tf_quant_finance/models/heston/heston_model_test.py:179-219",
+                   "tf_quant_finance/models/heston/approximations/european_option_test.py:30-53"],
+        "piecewise_drift_vol": {
+            "mean_reversion": [[0.5], [1, 1.1]], "theta": [[0.5], [1, 0.9]],
+            "volvol": [[0.3], [0.1, 0.2]], "rho": [[0.5], [0.4, 0.6]],
+            "t": 0.1, "state": "log(100), 0.045",
+            "drift": [-0.0225, 0.955], "volatility": [[0.21213203, 0.0], [0.00848528, 0.01944222]]},
+        "european_docstring": {"variances": 0.11, "strikes": 102.0, "expiries": 1.2, "forwards": 100.0,
+                               "mean_reversion": 2.0, "theta": 0.5, "volvol": 0.15, "rho": 0.3,
+                               "discount_factors": 1.0, "price": 24.822196},
+    }
+    # Cross-check the numbers quoted above against the test sources.
+    hsrc = open(os.path.join(tff, "models", "heston", "heston_model_test.py")).read()
+    assert "0.21213203" in hsrc and "0.00848528, 0.01944222" in hsrc and "-0.0225, 0.955" in hsrc
+    esrc = open(os.path.join(tff, "models", "heston", "approximations", "european_option_test.py")).read()
+    assert "24.822196" in esrc
+    with open(os.path.join(here, "heston_golden.json"), "w") as f:
+        json.dump(hest, f, indent=1)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

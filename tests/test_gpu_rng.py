@@ -1,0 +1,159 @@
+"""Sobol and Philox kernels against the oracle (GPU)."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import philox as ophilox
+from oracle import sobol as osobol
+
+pytestmark = pytest.mark.gpu
+
+
+def _u32(t):
+    return t.cpu().numpy().view(np.uint32)
+
+
+@pytest.mark.parametrize("dim,n,skip", [(1, 1, 0), (2, 5, 0), (5, 31, 0), (7, 1000, 17), (16, 4099, 0),
+                                        (1024, 3000, 0), (13, 2 ** 16, 123), (1, 3, 2 ** 31 - 5),
+                                        (504, 4097, 0), (33, 777, 2 ** 20)])
+def test_sobol_integers_bit_exact(cuda, dim, n, skip):
+    from tqf.math.random import sobol
+    got = _u32(sobol.sample_uint32(dim, n, skip))
+    want = osobol.sample_int(dim, n, skip).astype(np.uint32)
+    np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_sobol_floats_match_reference_conversion(cuda, dtype):
+    from tqf.math.random import sobol
+    np_dt = np.float32 if dtype == torch.float32 else np.float64
+    for dim, n, skip in [(2, 5, 0), (10, 50, 17), (64, 5000, 3)]:
+        got = sobol.sample(dim, n, skip=skip, dtype=dtype).cpu().numpy()
+        want = osobol.sample(dim, n, skip=skip, dtype=np_dt)
+        np.testing.assert_array_equal(got, want)
+
+
+def test_sobol_golden_vectors_on_gpu(cuda):
+    import json, os
+    from tqf.math.random import sobol
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "sobol_golden.json")))
+    a = g["dim2_first5"]
+    np.testing.assert_allclose(sobol.sample(a["dim"], a["num_results"]).cpu().numpy(), a["expected"], rtol=1e-6)
+    b = g["dim5_first31_gray_order"]
+    got = sobol.sample(b["dim"], b["num_results"], dtype=torch.float64).cpu().numpy()
+    assert sorted(map(tuple, got)) == sorted(map(tuple, b["expected"]))
+    c = g["large_skip"]
+    np.testing.assert_allclose(sobol.sample(c["dim"], c["num_results"], skip=c["skip"]).cpu().numpy(), c["expected"])
+
+
+def test_sobol_skip_consistency(cuda):
+    from tqf.math.random import sobol
+    full = sobol.sample(10, 67).cpu().numpy()
+    part = sobol.sample(10, 50, skip=17).cpu().numpy()
+    np.testing.assert_array_equal(full[17:], part)
+
+
+def test_sobol_normals_close_to_erfinv(cuda):
+    from tqf.math.random import sobol
+    got = sobol.sample_normal(12, 5000, skip=5).cpu().numpy()
+    u = osobol.sample(12, 5000, skip=5, dtype=np.float32)
+    want = osobol.normal_from_uniform(u)
+    np.testing.assert_allclose(got, want, rtol=2e-6, atol=2e-6)
+    got64 = sobol.sample_normal(12, 5000, skip=5, dtype=torch.float64).cpu().numpy()
+    want64 = osobol.normal_from_uniform(osobol.sample(12, 5000, skip=5, dtype=np.float64))
+    np.testing.assert_allclose(got64, want64, rtol=1e-13, atol=1e-13)
+
+
+def test_sobol_draw_layout(cuda):
+    # [steps, N, d] with Sobol dimension step*d + c and point index skip+1+n.
+    from tqf.math.random import sobol
+    steps, N, d, skip = 7, 1500, 3, 11
+    got = sobol.normal_draws(d, steps, N, skip=skip).cpu().numpy()
+    u = osobol.sample(steps * d, N, skip=skip, dtype=np.float32)
+    want = osobol.normal_from_uniform(u).reshape(N, steps, d).transpose(1, 0, 2)
+    np.testing.assert_allclose(got, want, rtol=2e-6, atol=2e-6)
+
+
+def test_sobol_full_scale_permutation_property(cuda):
+    # n = 2^k - 1 points from index 1: each dimension is a permutation of
+    # 1 .. 2^k - 1 (at nd = k digits) — checked by sums (and sums of squares
+    # where int64 holds them).
+    from tqf.math.random import sobol
+    n = 2 ** 24 - 1
+    assert sobol.num_digits(n, 0) == 24
+    x = sobol.sample_uint32(16, n).to(torch.int64)
+    assert torch.all(x.sum(dim=0) == n * (n + 1) // 2)
+    n = 2 ** 20 - 1
+    x = sobol.sample_uint32(64, n).to(torch.int64)
+    assert torch.all(x.sum(dim=0) == n * (n + 1) // 2)
+    assert torch.all((x * x).sum(dim=0) == n * (n + 1) * (2 * n + 1) // 6)
+
+
+def test_sobol_2pow26_reference_rounding(cuda):
+    # At 2^26 points the reference's float32 output reaches exactly 1.0.
+    from tqf.math.random import sobol
+    x = sobol.sample(1, 4, skip=2 ** 26 - 4)
+    nd = sobol.num_digits(4, 2 ** 26 - 4)
+    assert nd == 27
+    assert float(x.max()) == 1.0
+    c = sobol.sample_centered(1, 4, skip=2 ** 26 - 4)
+    assert float(c.max()) < 1.0
+
+
+PHILOX_KAT = [
+    ((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+    ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+    ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+     (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)),
+]
+
+
+@pytest.mark.parametrize("ctr,key,expected", PHILOX_KAT)
+def test_philox_kernel_known_answers(cuda, ctr, key, expected):
+    import tqf._lib as L
+    out = torch.zeros(4, dtype=torch.int32, device=cuda)
+    L.call("tqf_philox4x32_10", *ctr, *key, 1, out.data_ptr(), L.stream_ptr())
+    assert tuple(int(v) for v in _u32(out)) == expected
+
+
+def test_philox_kernel_stream_bit_exact(cuda):
+    import tqf._lib as L
+    out = torch.zeros(4 * 5000, dtype=torch.int32, device=cuda)
+    L.call("tqf_philox4x32_10", 7, 8, 9, 10, 11, 12, 5000, out.data_ptr(), L.stream_ptr())
+    got = _u32(out).reshape(5000, 4)
+    want = ophilox.philox4x32_10((7 + np.arange(5000)).astype(np.uint64), np.full(5000, 8, np.uint64),
+                                 np.full(5000, 9, np.uint64), np.full(5000, 10, np.uint64), 11, 12)
+    np.testing.assert_array_equal(got, np.stack(want, 1))
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("antithetic", [False, True])
+def test_philox_normal_draws_match_oracle(cuda, dtype, antithetic):
+    from tqf.math.random import RandomType
+    from tqf.math.random.multivariate_normal import philox_normal_draws
+    rt = RandomType.STATELESS_ANTITHETIC if antithetic else RandomType.STATELESS
+    steps, N, d = 9, 2048, 3
+    got = philox_normal_draws(rt, [5, 6], d, steps, N, dtype).cpu().numpy()
+    want = ophilox.normal_draws(N, steps, d, 5, 6, dtype=np.float32 if dtype == torch.float32 else np.float64,
+                                antithetic=antithetic)
+    tol = 5e-6 if dtype == torch.float32 else 1e-12
+    np.testing.assert_allclose(got, want, rtol=tol, atol=tol)
+
+
+def test_draws_prefix_stability_and_moments(cuda):
+    from tqf.math.random import RandomType, mv_normal_sample
+    a = mv_normal_sample([10], mean=np.zeros(4, np.float32), random_type=RandomType.STATELESS, seed=[1, 2])
+    b = mv_normal_sample([16], mean=np.zeros(4, np.float32), random_type=RandomType.STATELESS, seed=[1, 2])
+    torch.testing.assert_close(a, b[:10], rtol=0, atol=0)
+    z = mv_normal_sample([200000], mean=np.zeros(3, np.float64), random_type=RandomType.PSEUDO, seed=4)
+    assert float(z.mean().abs()) < 5e-3 and abs(float(z.std()) - 1) < 5e-3
+    cov = np.array([[1.0, 0.5], [0.5, 2.0]])
+    z = mv_normal_sample([400000], mean=np.array([1.0, -1.0]), covariance_matrix=cov,
+                         random_type=RandomType.STATELESS, seed=[3, 3]).cpu().numpy()
+    np.testing.assert_allclose(np.cov(z.T), cov, atol=2e-2)
+    np.testing.assert_allclose(z.mean(0), [1.0, -1.0], atol=1e-2)
+    s = mv_normal_sample([1000], mean=np.zeros(2), random_type=RandomType.SOBOL, skip=1000)
+    assert s.shape == (1000, 2) and abs(float(s.mean())) < 0.02
+    z = mv_normal_sample([1000], mean=np.array([2.0, 3.0]), random_type=RandomType.PSEUDO_ANTITHETIC, seed=2)
+    torch.testing.assert_close(z[:500] + z[500:], torch.tensor([4.0, 6.0], dtype=z.dtype, device=z.device).expand(500, 2))

@@ -1,0 +1,106 @@
+"""Host-side logic of the drop-in API against the oracle (CPU only)."""
+
+import numpy as np
+import pytest
+
+from oracle import grids as ogrids
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("case", [
+    dict(times=[1.0], time_step=0.01),
+    dict(times=[0.1, 1.0, 2.0], time_step=0.01),
+    dict(times=[0.3, 0.7, 1.0], time_step=0.1),
+    dict(times=[0.5, 1.0], num_time_steps=100),
+    dict(times=[1.0], num_time_steps=252),
+    dict(times=list(np.linspace(1 / 52, 1, 52)), times_grid=np.linspace(0, 1, 253)),
+    dict(times=[0.25, 0.5, 0.77], times_grid=np.linspace(0, 1, 11)),
+])
+def test_prepare_grid_matches_oracle(case, dtype):
+    from tqf.models import utils
+    times = np.asarray(case["times"], dtype=dtype)
+    kw = dict(tolerance=None, num_time_steps=case.get("num_time_steps"), times_grid=case.get("times_grid"))
+    step = case.get("time_step")
+    if step is None and kw["num_time_steps"] is not None:
+        step = times[-1] / dtype(kw["num_time_steps"])
+    a = utils.prepare_grid(times=times, time_step=step, dtype=dtype, **kw)
+    b = ogrids.prepare_grid(times, step, dtype, **kw)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.parametrize("seed", range(20))
+def test_output_slot_plan_matches_oracle(seed):
+    from tqf.models import utils
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(2, 30))
+    keep = rng.random(n) < 0.3
+    k = max(int(keep.sum()), 1) + int(rng.integers(0, 2))
+    init = int(rng.integers(0, 2))
+    a = utils.plan_output_slots(keep, k, init)
+    b = ogrids.write_slots(keep, k, init)
+    np.testing.assert_array_equal(a[0], b[0])
+    assert a[1:] == b[1:]
+
+
+def test_heston_grid_matches_oracle():
+    from tqf.math.piecewise import PiecewiseConstantFunc
+    from tqf.models.heston_model import HestonModel
+    k = PiecewiseConstantFunc([0.1, 0.2], [0.3, 0.3, 0.3], dtype=np.float64)
+    m = HestonModel(k, 0.05, 0.02, 0.1, dtype=np.float64)
+    times = np.array([0.5, 1.0])
+    a = m._prepare_grid(times, 0.01, None, None)
+    b = ogrids.heston_prepare_grid(times, 0.01, np.float64, jump_locations=[[0.1, 0.2]])
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    m2 = HestonModel(2.0, 0.04, 0.3, -0.7)
+    a = m2._prepare_grid(np.array([1.0], np.float32), np.float32(1.0) / np.float32(252), 252, None)
+    b = ogrids.heston_prepare_grid(np.array([1.0], np.float32), np.float32(1.0) / np.float32(252), np.float32,
+                                   num_time_steps=252)
+    np.testing.assert_array_equal(a[0], b[0])
+    assert len(a[0]) == 253
+
+
+def test_argument_errors_follow_the_reference():
+    from tqf import InvalidArgumentError
+    from tqf.math.random import sobol
+    from tqf.models import euler_sampling, HestonModel
+    drift = lambda t, x: x  # noqa: E731
+    with pytest.raises(ValueError):  # neither time_step nor num_time_steps
+        euler_sampling.sample(1, drift, drift, times=[1.0])
+    with pytest.raises(ValueError):  # both
+        euler_sampling.sample(1, drift, drift, times=[1.0], time_step=0.1, num_time_steps=10)
+    with pytest.raises(InvalidArgumentError):  # times not increasing
+        euler_sampling.sample(1, drift, drift, times=[1.0, 0.5], time_step=0.1, validate_args=True)
+    with pytest.raises(ValueError):  # dim mismatch with normal_draws
+        euler_sampling.sample(2, drift, drift, times=[1.0], time_step=0.1, normal_draws=np.zeros((4, 10, 1)))
+    with pytest.raises(InvalidArgumentError):  # draws steps mismatch
+        euler_sampling.sample(1, drift, drift, times=[1.0], time_step=0.1, normal_draws=np.zeros((4, 7, 1)),
+                              validate_args=True)
+    with pytest.raises(ValueError):
+        sobol.sample(0, 5, validate_args=True)
+    with pytest.raises(InvalidArgumentError):
+        sobol.sample(2, 5, skip=-10, validate_args=True)
+    with pytest.raises(InvalidArgumentError):
+        sobol.sample(2, 0, validate_args=True)
+    with pytest.raises(InvalidArgumentError):
+        sobol.sample(1, 4, skip=2 ** 31 - 5, validate_args=True)
+    m = HestonModel(2.0, 0.04, 0.3, -0.7)
+    with pytest.raises(ValueError):
+        m.sample_paths([1.0], [0.0, 0.04])
+    with pytest.raises(ValueError):
+        m.sample_paths([1.0], [0.0, 0.04], time_step=0.1, num_time_steps=10)
+
+
+def test_piecewise_left_continuous():
+    from tqf.math.piecewise import PiecewiseConstantFunc
+    f = PiecewiseConstantFunc([0.1, 10], [3, 4, 5], dtype=np.float64)
+    np.testing.assert_array_equal(f(np.array([0.0, 0.1, 2.0, 11.0])), [3, 3, 4, 5])
+
+
+def test_seed_conventions():
+    from tqf.math.random.multivariate_normal import RandomType, philox_key
+    assert philox_key(RandomType.STATELESS, [3, 4]) == (3, 4)
+    assert philox_key(RandomType.PSEUDO, 42) == (42, 0)
+    with pytest.raises(ValueError):
+        philox_key(RandomType.STATELESS, None)

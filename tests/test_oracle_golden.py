@@ -1,0 +1,141 @@
+"""The oracle pinned on the reference's own known-answer tests (CPU)."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import closed_form, grids, heston, philox, sobol
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+SOBOL_GOLDEN = json.load(open(os.path.join(GOLDEN_DIR, "sobol_golden.json")))
+HESTON_GOLDEN = json.load(open(os.path.join(GOLDEN_DIR, "heston_golden.json")))
+
+
+@pytest.mark.parametrize("dtype", [np.float16, np.float32, np.float64])
+def test_sobol_known_values_small_dimension(dtype):
+    # sobol_test.py:28-38 — first five points, dimension 2, original order.
+    g = SOBOL_GOLDEN["dim2_first5"]
+    out = sobol.sample(g["dim"], g["num_results"], dtype=np.float32 if dtype == np.float16 else dtype)
+    np.testing.assert_allclose(out.astype(dtype), np.array(g["expected"], dtype=dtype), rtol=1e-6)
+
+
+def test_sobol_more_known_values_as_set():
+    # sobol_test.py:40-81 — 31 points of dimension 5 (listed in Gray-code
+    # order, compared as a set, as the reference test does).
+    g = SOBOL_GOLDEN["dim5_first31_gray_order"]
+    ours = sobol.sample(g["dim"], g["num_results"], dtype=np.float64)
+    assert sorted(tuple(r) for r in g["expected"]) == sorted(tuple(r) for r in ours)
+
+
+def test_sobol_skip():
+    # sobol_test.py:83-91
+    full = sobol.sample_int(10, 50 + 17, nd=sobol.num_digits(67, 0))
+    part = sobol.sample_int(10, 50, skip=17, nd=sobol.num_digits(67, 0))
+    np.testing.assert_array_equal(full[17:], part)
+    np.testing.assert_allclose(sobol.sample(10, 67)[17:], sobol.sample(10, 50, skip=17))
+
+
+def test_sobol_large_skip():
+    # sobol_test.py:93-98
+    g = SOBOL_GOLDEN["large_skip"]
+    np.testing.assert_allclose(sobol.sample(g["dim"], g["num_results"], skip=g["skip"]), g["expected"])
+
+
+def test_sobol_float_rounds_to_one_at_2_pow_26():
+    # float32(int)/2^27 for dimension 0, index 2^26 - 1 -> int 2^27 - 2 -> 1.0.
+    nd = sobol.num_digits(2 ** 26, 0)
+    assert nd == 27
+    ints = sobol.sample_int(1, 1, skip=2 ** 26 - 2, nd=nd)
+    assert int(ints[0, 0]) == 2 ** 27 - 2
+    assert np.float32(ints[0, 0]) / np.float32(2.0 ** 27) == np.float32(1.0)
+
+
+def test_sobol_num_digits():
+    assert sobol.num_digits(5, 0) == 3
+    assert sobol.num_digits(3, 2 ** 31 - 5) == 31
+    assert sobol.num_digits(2 ** 22, 0) == 23
+
+
+# Random123 known-answer vectors for philox4x32-10.
+PHILOX_KAT = [
+    ((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+    ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+    ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+     (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)),
+]
+
+
+@pytest.mark.parametrize("ctr,key,expected", PHILOX_KAT)
+def test_philox_known_answers(ctr, key, expected):
+    out = philox.philox4x32_10(*[np.array([c], dtype=np.uint64) for c in ctr], *key)
+    assert tuple(int(o[0]) for o in out) == expected
+
+
+def test_philox_normals_moments():
+    z = philox.normals(np.arange(20000), 8, 7, 11)
+    assert abs(z.mean()) < 0.01
+    assert abs(z.std() - 1) < 0.01
+
+
+def test_heston_drift_and_volatility_pinned():
+    # heston_model_test.py:179-219
+    g = HESTON_GOLDEN["piecewise_drift_vol"]
+    k, th, xi, rho = (tuple(tuple(v) for v in g[n]) for n in ("mean_reversion", "theta", "volvol", "rho"))
+    x = np.array([np.log(100), 0.045])
+    np.testing.assert_allclose(heston.drift_fn(k, th, np.float64)(g["t"], x), g["drift"])
+    np.testing.assert_allclose(heston.volatility_fn(xi, rho, np.float64)(g["t"], x), g["volatility"], rtol=1e-6)
+
+
+def test_heston_semi_analytic_price_pinned():
+    # european_option_test.py:30-53
+    g = HESTON_GOLDEN["european_docstring"]
+    p = closed_form.heston_price(forward=g["forwards"], strike=g["strikes"], expiry=g["expiries"],
+                                 v0=g["variances"], kappa=g["mean_reversion"], theta=g["theta"],
+                                 xi=g["volvol"], rho=g["rho"], discount_factor=g["discount_factors"])
+    np.testing.assert_allclose(p, g["price"], rtol=1e-5, atol=1e-5)
+
+
+def test_black_scholes_textbook():
+    np.testing.assert_allclose(closed_form.black_scholes(100, 100, 0.05, 0.2, 1.0), 10.450583572185565, rtol=1e-12)
+    put = closed_form.black_scholes(100, 100, 0.05, 0.2, 1.0, is_call=False)
+    np.testing.assert_allclose(put, 5.573526022256971, rtol=1e-12)
+
+
+def test_euler_grid_from_time_step():
+    # 101 points for times=[1.0], time_step=0.01 (float64)
+    t, mask, ti = grids.prepare_grid([1.0], 0.01, np.float64)
+    assert len(t) == 101 and mask[-1] and mask.sum() == 1 and ti[0] == 100
+    # requested times inside the grid are merged, duplicates removed
+    t, mask, ti = grids.prepare_grid([0.1, 1.0, 2.0], 0.01, np.float64)
+    assert len(t) == 201 and list(ti) == [10, 100, 200]
+
+
+def test_euler_grid_from_num_steps_and_times_grid():
+    t, mask, ti = grids.prepare_grid([0.5, 1.0], 0.01, np.float32, num_time_steps=100)
+    assert len(t) == 101 and t[0] == 0 and list(ti) == [np.searchsorted(t, np.float32(0.5)), 100]
+    tg = np.linspace(0, 1, 253)
+    t, mask, ti = grids.prepare_grid(np.linspace(1 / 52, 1, 52), None, np.float64, times_grid=tg)
+    assert len(t) == 253 and mask.sum() == 52 and ti[-1] == 252
+
+
+def test_heston_grid_keeps_duplicates():
+    t, mask = grids.heston_prepare_grid([0.0, 1.0], 0.25, np.float32)
+    assert list(t) == [0.0, 0.0, 0.25, 0.5, 0.75, 1.0]
+    assert list(mask) == [False, True, False, False, False, True]
+
+
+def test_write_slots():
+    # times=[0.5, 1.0] on a 4-step grid: states after steps 1 and 3 recorded.
+    keep = np.array([False, False, True, False, True])
+    step_slot, init_slot, n, unwritten = grids.write_slots(keep, 2, 0)
+    assert list(step_slot) == [-1, 0, -1, 1] and init_slot == -1 and n == 4 and not unwritten
+    # keep_mask[0] (time 0 requested) keeps the initial state in slot 0.
+    keep = np.array([True, False, True])
+    step_slot, init_slot, n, unwritten = grids.write_slots(keep, 2, 1)
+    assert list(step_slot) == [-1, 1] and init_slot == 0
+    # times_grid past the last requested time: the loop stops early.
+    keep = np.array([False, True, False, False])
+    step_slot, init_slot, n, _ = grids.write_slots(keep, 1, 0)
+    assert n == 1 and list(step_slot) == [0]

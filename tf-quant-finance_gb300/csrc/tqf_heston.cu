@@ -1,0 +1,350 @@
+// Heston path kernels: full-truncation Euler (the reference Euler sampler run
+// with Heston coefficients, tff/models/euler_sampling.py:513-537) and the
+// Andersen QE scheme of HestonModel.sample_paths
+// (tff/models/heston/heston_model.py:322-460, 522-572).
+//
+// One thread per path, state (log-spot, variance) in registers, the per-step
+// table staged once per CTA into shared memory by a TMA bulk copy, draws
+// generated in-kernel (Philox4x32-10, one block = two steps of two normals)
+// or read from memory.  Optional coalescing-friendly stores of the recorded
+// states and a fused European payoff over up to 1024 strikes with FP64
+// cross-path accumulation in a fixed order (deterministic).  The CTA loop is
+// persistent: grid = SMs x resident CTAs, each CTA walks path tiles.
+#include "tqf_internal.cuh"
+
+namespace tqf {
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kFtCols = 8;
+constexpr int kQeCols = 12;
+constexpr size_t kMaxStagedTable = 96 * 1024;
+
+struct SmemLayout {
+  size_t bar, table, acc, spot, strike, call, total;
+};
+
+template <typename T>
+SmemLayout smem_layout(int steps, int cols, int ns, bool staged) {
+  SmemLayout L;
+  size_t off = 0;
+  L.bar = off;
+  off += 16;
+  L.table = off;
+  if (staged) off += (size_t)steps * cols * sizeof(T);
+  off = (off + 15) & ~(size_t)15;
+  L.acc = off;
+  off += (size_t)ns * 4 * 2 * sizeof(double);
+  L.spot = off;
+  off += (ns > 0 ? kBlock : 0) * sizeof(T);
+  L.strike = off;
+  off += (size_t)ns * sizeof(T);
+  L.call = off;
+  off += (size_t)ns;
+  L.total = (off + 15) & ~(size_t)15;
+  return L;
+}
+
+// ---- one step of each scheme ---------------------------------------------
+template <typename T>
+__device__ __forceinline__ void ft_step(const T* __restrict__ row, T z0, T z1, T& x, T& v) {
+  const T dt = row[0], sdt = row[1], r = row[2], kappa = row[3], theta = row[4];
+  const T xirho = row[5], xisq = row[6];
+  const T vp = v > T(0) ? v : T(0);
+  const T sq = sqrt(vp);
+  const T dw0 = z0 * sdt;
+  const T dw1 = z1 * sdt;
+  const T x_next = x + dt * (r - T(0.5) * vp) + sq * dw0;
+  const T v_next = v + dt * (kappa * (theta - vp)) + ((xirho * sq) * dw0 + (xisq * sq) * dw1);
+  x = x_next;
+  v = v_next;
+}
+
+template <typename T>
+__device__ __forceinline__ T qe_erf(T x);
+template <>
+__device__ __forceinline__ float qe_erf<float>(float x) { return erff(x); }
+template <>
+__device__ __forceinline__ double qe_erf<double>(double x) { return erf(x); }
+
+template <typename T>
+__device__ __forceinline__ void qe_step(const T* __restrict__ row, T zv, T zx, T& x, T& v) {
+  if (row[0] != T(0)) return;  // dt <= tolerance: state kept, draws consumed
+  const T theta = row[1], E = row[2], A = row[3], B = row[4];
+  const T m = theta + (v - theta) * E;
+  const T s2 = v * A + B;
+  const T psi = s2 / (m * m);
+  T v_next;
+  if (psi < T(1.5)) {
+    const T psi_inv = T(2) / psi;
+    const T b2 = psi_inv - T(1) + sqrt(psi_inv * (psi_inv - T(1)));
+    const T a = m / (T(1) + b2);
+    const T t = sqrt(b2) + zv;
+    v_next = a * (t * t);
+  } else {
+    const T p = (psi - T(1)) / (psi + T(1));
+    const T beta = (T(1) - p) / m;
+    const T u = T(0.5) * (T(1) + qe_erf<T>(zv / T(1.41421356237309504880)));
+    v_next = u > p ? (log(T(1) - p) - log(T(1) - u)) / beta : T(0);
+  }
+  const T k0 = row[5], k1 = row[6], k2 = row[7], k3 = row[8], k4 = row[9];
+  x = x + k0 + k1 * v + k2 * v_next + sqrt(k3 * v + k4 * v_next) * zx;
+  v = v_next;
+}
+
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<float> {
+  using type = float2;
+};
+template <>
+struct Vec2<double> {
+  using type = double2;
+};
+
+template <typename T>
+__device__ __forceinline__ void store_state(const tqf_path_output& o, int64_t path, int slot, T x,
+                                            T v) {
+  using V2 = typename Vec2<T>::type;
+  V2 w;
+  w.x = x;
+  w.y = v;
+  reinterpret_cast<V2*>(o.ptr)[path * o.num_slots + slot] = w;
+}
+
+// SCHEME 0 = full-truncation Euler, 1 = QE.  SRC = TQF_DRAWS_* (compile-time).
+template <typename T, int SCHEME, int SRC, bool STORE, bool PRICE>
+__global__ void __launch_bounds__(kBlock)
+    heston_kernel(tqf_heston_args a, int staged, SmemLayout L) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int COLS = SCHEME == 0 ? kFtCols : kQeCols;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L.bar);
+  const T* table = staged ? reinterpret_cast<const T*>(smem + L.table)
+                          : static_cast<const T*>(a.step_table);
+  const int steps = a.num_steps;
+  if (staged) {
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    uint32_t phase = 0;
+    if (!stage_to_smem(smem + L.table, a.step_table, (uint32_t)(steps * COLS * sizeof(T)), bar,
+                       phase, a.dev_status))
+      return;
+  }
+  double* acc = reinterpret_cast<double*>(smem + L.acc);
+  T* s_spot = reinterpret_cast<T*>(smem + L.spot);
+  T* s_strike = reinterpret_cast<T*>(smem + L.strike);
+  uint8_t* s_call = smem + L.call;
+  const int ns = a.payoff.num_strikes;
+  if (PRICE) {
+    for (int i = threadIdx.x; i < 8 * ns; i += kBlock) acc[i] = 0.0;
+    for (int i = threadIdx.x; i < ns; i += kBlock) {
+      s_strike[i] = static_cast<const T*>(a.payoff.strikes)[i];
+      s_call[i] = a.payoff.is_call ? a.payoff.is_call[i] : (uint8_t)1;
+    }
+    __syncthreads();
+  }
+  const T x0 = (T)a.x0, v0 = (T)a.v0;
+  const T spot_scale = (T)a.payoff.spot_scale;
+  const int64_t N = a.num_paths;
+  const int64_t per_round = (int64_t)gridDim.x * kBlock;
+  for (int64_t base = 0; base < N; base += per_round) {
+    const int64_t path = base + (int64_t)blockIdx.x * kBlock + threadIdx.x;
+    const bool valid = path < N;
+    T x = x0, v = v0;
+    if (valid) {
+      if (STORE && a.output.init_slot >= 0) store_state<T>(a.output, path, a.output.init_slot, x, v);
+      if (SRC == TQF_DRAWS_PHILOX && sizeof(T) == 4) {
+        // Canonical stream, 2 normals per step: block b = steps 2b, 2b+1.
+        int64_t p = path;
+        float sign = 1.f;
+        if (a.draws.antithetic && p >= a.draws.antithetic_half) {
+          p -= a.draws.antithetic_half;
+          sign = -1.f;
+        }
+        p += a.draws.path_offset;
+        int i = 0;
+        for (; i + 1 < steps; i += 2) {
+          float z[4];
+          philox_normals4_f32(i >> 1, p, a.draws.key0, a.draws.key1, z);
+          const T* r0 = table + (size_t)i * COLS;
+          if (SCHEME == 0) ft_step<T>(r0, (T)(sign * z[0]), (T)(sign * z[1]), x, v);
+          else qe_step<T>(r0, (T)(sign * z[0]), (T)(sign * z[1]), x, v);
+          if (STORE) {
+            const int slot = (int)r0[COLS - 1];
+            if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+          }
+          const T* r1 = r0 + COLS;
+          if (SCHEME == 0) ft_step<T>(r1, (T)(sign * z[2]), (T)(sign * z[3]), x, v);
+          else qe_step<T>(r1, (T)(sign * z[2]), (T)(sign * z[3]), x, v);
+          if (STORE) {
+            const int slot = (int)r1[COLS - 1];
+            if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+          }
+        }
+        if (i < steps) {
+          float z[4];
+          philox_normals4_f32(i >> 1, p, a.draws.key0, a.draws.key1, z);
+          const T* r0 = table + (size_t)i * COLS;
+          if (SCHEME == 0) ft_step<T>(r0, (T)(sign * z[0]), (T)(sign * z[1]), x, v);
+          else qe_step<T>(r0, (T)(sign * z[0]), (T)(sign * z[1]), x, v);
+          if (STORE) {
+            const int slot = (int)r0[COLS - 1];
+            if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+          }
+        }
+      } else {
+        DrawSource<T> src(a.draws, path, 2);
+        for (int i = 0; i < steps; ++i) {
+          const T z0 = src.get(i, 0);
+          const T z1 = src.get(i, 1);
+          const T* r0 = table + (size_t)i * COLS;
+          if (SCHEME == 0) ft_step<T>(r0, z0, z1, x, v);
+          else qe_step<T>(r0, z0, z1, x, v);
+          if (STORE) {
+            const int slot = (int)r0[COLS - 1];
+            if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+          }
+        }
+      }
+    }
+    if (PRICE) {
+      __syncthreads();
+      s_spot[threadIdx.x] = valid ? spot_scale * exp(x) : T(NAN);
+      __syncthreads();
+      payoff_round<kBlock, T>(s_spot, s_strike, s_call, ns, acc);
+    }
+  }
+  if (PRICE) {
+    __syncthreads();
+    payoff_flush(acc, ns, 4, static_cast<double*>(a.payoff.workspace));
+  }
+}
+
+template <typename T, int SCHEME>
+using KernelFn = void (*)(tqf_heston_args, int, SmemLayout);
+
+template <typename T, int SCHEME, int SRC>
+KernelFn<T, SCHEME> pick(bool store, bool price) {
+  if (store && price) return heston_kernel<T, SCHEME, SRC, true, true>;
+  if (store) return heston_kernel<T, SCHEME, SRC, true, false>;
+  if (price) return heston_kernel<T, SCHEME, SRC, false, true>;
+  return heston_kernel<T, SCHEME, SRC, false, false>;
+}
+
+template <typename T, int SCHEME>
+KernelFn<T, SCHEME> pick_kernel(int src, bool store, bool price) {
+  return src == TQF_DRAWS_PHILOX ? pick<T, SCHEME, TQF_DRAWS_PHILOX>(store, price)
+                                 : pick<T, SCHEME, TQF_DRAWS_MEMORY>(store, price);
+}
+
+template <typename T, int SCHEME>
+int grid_for(int64_t N, int ns, int steps, bool staged, int src, bool store, bool price,
+             SmemLayout* out_layout) {
+  const int cols = SCHEME == 0 ? kFtCols : kQeCols;
+  SmemLayout L = smem_layout<T>(steps, cols, price ? ns : 0, staged);
+  if (out_layout) *out_layout = L;
+  auto k = pick_kernel<T, SCHEME>(src, store, price);
+  if (L.total > 48 * 1024)
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, L.total) != cudaSuccess ||
+      occ < 1)
+    occ = 1;
+  int64_t blocks = (N + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)num_sms() * occ;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (int)blocks;
+}
+
+bool table_staged(const void* table, int steps, int cols, size_t elt) {
+  const size_t bytes = (size_t)steps * cols * elt;
+  return bytes > 0 && bytes <= kMaxStagedTable && (reinterpret_cast<uintptr_t>(table) & 15u) == 0;
+}
+
+template <typename T, int SCHEME>
+int run(const tqf_heston_args& a, cudaStream_t s) {
+  const int cols = SCHEME == 0 ? kFtCols : kQeCols;
+  const bool store = a.output.ptr != nullptr;
+  const bool price = a.payoff.num_strikes > 0;
+  const bool staged = table_staged(a.step_table, a.num_steps, cols, sizeof(T));
+  SmemLayout L;
+  const int grid = grid_for<T, SCHEME>(a.num_paths, a.payoff.num_strikes, a.num_steps, staged,
+                                       a.draws.source, store, price, &L);
+  if (price) {
+    const size_t need = (size_t)grid * a.payoff.num_strikes * 2 * sizeof(double);
+    TQF_REQUIRE(a.payoff.workspace && a.payoff.workspace_bytes >= need,
+                "heston: payoff workspace %zu bytes < required %zu", a.payoff.workspace_bytes, need);
+  }
+  auto k = pick_kernel<T, SCHEME>(a.draws.source, store, price);
+  k<<<grid, kBlock, L.total, s>>>(a, staged ? 1 : 0, L);
+  int rc = check_launch(SCHEME == 0 ? "heston_kernel<FT>" : "heston_kernel<QE>");
+  if (rc || !price || a.payoff.out == nullptr) return rc;
+  return reduce_partials(static_cast<const double*>(a.payoff.workspace), grid,
+                         2 * a.payoff.num_strikes, a.payoff.out, s);
+}
+
+int validate(const tqf_heston_args* a, const char* who) {
+  TQF_REQUIRE(a != nullptr, "%s: null args", who);
+  TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "%s: bad dtype %d", who, a->dtype);
+  TQF_REQUIRE(a->num_paths >= 1, "%s: num_paths must be >= 1", who);
+  TQF_REQUIRE(a->num_steps >= 0, "%s: num_steps must be >= 0", who);
+  TQF_REQUIRE(a->num_steps == 0 || a->step_table != nullptr, "%s: null step_table", who);
+  TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.source == TQF_DRAWS_MEMORY,
+              "%s: bad draws.source %d", who, a->draws.source);
+  TQF_REQUIRE(a->draws.source != TQF_DRAWS_MEMORY || a->num_steps == 0 || a->draws.ptr != nullptr,
+              "%s: memory draws need draws.ptr", who);
+  TQF_REQUIRE(!a->draws.antithetic || 2 * a->draws.antithetic_half == a->num_paths,
+              "%s: antithetic needs num_paths == 2 * antithetic_half", who);
+  if (a->output.ptr) {
+    TQF_REQUIRE(a->output.num_slots >= 1, "%s: output.num_slots must be >= 1", who);
+    TQF_REQUIRE(a->output.init_slot < a->output.num_slots, "%s: init_slot out of range", who);
+  }
+  TQF_REQUIRE(a->payoff.num_strikes >= 0 && a->payoff.num_strikes <= 1024,
+              "%s: num_strikes must be in [0, 1024]", who);
+  TQF_REQUIRE(a->payoff.num_strikes == 0 || a->payoff.strikes, "%s: payoff needs strikes", who);
+  return TQF_OK;
+}
+
+}  // namespace
+}  // namespace tqf
+
+using namespace tqf;
+
+extern "C" int tqf_heston_euler(const tqf_heston_args* a, void* stream) {
+  clear_error();
+  int rc = validate(a, "tqf_heston_euler");
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a->dtype == TQF_F32 ? run<float, 0>(*a, s) : run<double, 0>(*a, s);
+}
+
+extern "C" int tqf_heston_qe(const tqf_heston_args* a, void* stream) {
+  clear_error();
+  int rc = validate(a, "tqf_heston_qe");
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a->dtype == TQF_F32 ? run<float, 1>(*a, s) : run<double, 1>(*a, s);
+}
+
+extern "C" size_t tqf_heston_workspace_bytes(int32_t dtype, int32_t qe, int64_t num_paths,
+                                             int32_t num_strikes) {
+  if (num_strikes <= 0) return 0;
+  // The grid does not depend on the step count or staging beyond smem size;
+  // use the largest layout (unstaged table is smaller, so occupancy >=).
+  int grid;
+  if (dtype == TQF_F32)
+    grid = qe ? grid_for<float, 1>(num_paths, num_strikes, 0, false, TQF_DRAWS_PHILOX, false, true, nullptr)
+              : grid_for<float, 0>(num_paths, num_strikes, 0, false, TQF_DRAWS_PHILOX, false, true, nullptr);
+  else
+    grid = qe ? grid_for<double, 1>(num_paths, num_strikes, 0, false, TQF_DRAWS_PHILOX, false, true, nullptr)
+              : grid_for<double, 0>(num_paths, num_strikes, 0, false, TQF_DRAWS_PHILOX, false, true, nullptr);
+  // Occupancy may differ between kernel variants; size for the largest
+  // possible grid (all SMs x the maximum resident CTAs of 256 threads).
+  int64_t cap = (int64_t)num_sms() * 8;
+  int64_t blocks = (num_paths + kBlock - 1) / kBlock;
+  if (blocks > cap) blocks = cap;
+  if (blocks < grid) blocks = grid;
+  return (size_t)blocks * num_strikes * 2 * sizeof(double);
+}

@@ -1,0 +1,360 @@
+// Internal helpers shared by the tqf CUDA translation units: error state,
+// launch accounting, Philox4x32-10, Box–Muller, TMA bulk staging with bounded
+// mbarrier waits, and the FP64 payoff accumulator used by the path kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tqf.h"
+
+namespace tqf {
+
+// ---- host-side error state ----------------------------------------------
+void set_error(const char* fmt, ...);
+void clear_error();
+int check_cuda(cudaError_t e, const char* where);
+void note_launch(uint64_t n = 1);
+int num_sms();
+// Checks the launch just issued; returns TQF_OK or TQF_E_CUDA.
+int check_launch(const char* kernel_name);
+
+#define TQF_REQUIRE(cond, ...)        \
+  do {                                \
+    if (!(cond)) {                    \
+      ::tqf::set_error(__VA_ARGS__);  \
+      return TQF_E_INVALID;           \
+    }                                 \
+  } while (0)
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------
+// Ten rounds of the published round function; the key is bumped by the
+// Weyl constants between rounds.
+constexpr uint32_t kPhiloxM0 = 0xD2511F53u;
+constexpr uint32_t kPhiloxM1 = 0xCD9E8D57u;
+constexpr uint32_t kPhiloxW0 = 0x9E3779B9u;
+constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
+
+__host__ __device__ __forceinline__ void mulhilo32(uint32_t a, uint32_t b,
+                                                   uint32_t& hi, uint32_t& lo) {
+#ifdef __CUDA_ARCH__
+  lo = a * b;
+  hi = __umulhi(a, b);
+#else
+  uint64_t p = (uint64_t)a * (uint64_t)b;
+  lo = (uint32_t)p;
+  hi = (uint32_t)(p >> 32);
+#endif
+}
+
+__host__ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0,
+                                                        uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mulhilo32(kPhiloxM0, c.x, hi0, lo0);
+    mulhilo32(kPhiloxM1, c.z, hi1, lo1);
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += kPhiloxW0;
+    k1 += kPhiloxW1;
+  }
+  return c;
+}
+
+// Counter of the canonical normal stream: block b of path n.
+__device__ __forceinline__ uint4 philox_counter(int64_t block, int64_t path) {
+  return make_uint4((uint32_t)block, (uint32_t)path,
+                    (uint32_t)((uint64_t)path >> 32), (uint32_t)((uint64_t)block >> 32));
+}
+
+// ---- uniform -> normal (Box–Muller) ---------------------------------------
+// float32: u1 in (0, 1] with 2^-32 resolution assembled from the 32 random
+// bits through two exponent-trick conversions (no integer->float convert),
+// u2 in [0, 1) with 2^-23 resolution for the angle.
+__device__ __forceinline__ float u01_oc_f32(uint32_t r) {
+  float hi = __uint_as_float(0x3f800000u | (r >> 9));          // [1, 2)
+  float lo = __uint_as_float(0x3f800000u | (r << 23 >> 9)) - 1.0f; // [0, 1), low 9 bits
+  // (2 - hi) in {2^-23, ..., 1}; subtract lo * 2^-23 for the low bits.
+  return __fmaf_rn(lo, -1.1920928955078125e-07f, 2.0f - hi);
+}
+__device__ __forceinline__ float u01_co_f32(uint32_t r) {
+  return __uint_as_float(0x3f800000u | (r >> 9)) - 1.0f;
+}
+
+// Two N(0,1) from two 32-bit words (radius from a, angle from b).  Uses the
+// SFU approximations (lg2, sqrt, sin, cos); the angle is taken in [-pi, pi)
+// where the hardware sin/cos are accurate.
+__device__ __forceinline__ void box_muller_f32(uint32_t a, uint32_t b, float& z0,
+                                               float& z1) {
+  const float u1 = u01_oc_f32(a);
+  const float u2 = u01_co_f32(b);
+  const float rad = __fsqrt_rn(__fmul_rn(-1.3862943611198906f, __log2f(u1)));  // -2 ln u1
+  const float ang = __fmul_rn(__fsub_rn(u2, 0.5f), 6.283185307179586f);
+  float s, c;
+  __sincosf(ang, &s, &c);
+  z0 = __fmul_rn(rad, c);
+  z1 = __fmul_rn(rad, s);
+}
+
+// float64: 53-bit uniforms from word pairs.
+__device__ __forceinline__ double u01_oc_f64(uint32_t a, uint32_t b) {
+  uint64_t m = ((uint64_t)a << 21) ^ (uint64_t)(b >> 11);  // 53 bits
+  return ((double)m + 1.0) * 1.1102230246251565e-16;       // (m+1) * 2^-53
+}
+__device__ __forceinline__ double u01_co_f64(uint32_t a, uint32_t b) {
+  uint64_t m = ((uint64_t)a << 21) ^ (uint64_t)(b >> 11);
+  return (double)m * 1.1102230246251565e-16;
+}
+__device__ __forceinline__ void box_muller_f64(uint4 r, double& z0, double& z1) {
+  const double u1 = u01_oc_f64(r.x, r.y);
+  const double u2 = u01_co_f64(r.z, r.w);
+  const double rad = sqrt(-2.0 * log(u1));
+  double s, c;
+  sincospi(2.0 * u2, &s, &c);
+  z0 = rad * c;
+  z1 = rad * s;
+}
+
+// Four float normals of block b for path n: draw dims 4b..4b+3.
+__device__ __forceinline__ void philox_normals4_f32(int64_t block, int64_t path,
+                                                    uint32_t k0, uint32_t k1,
+                                                    float z[4]) {
+  uint4 r = philox4x32_10(philox_counter(block, path), k0, k1);
+  box_muller_f32(r.x, r.y, z[0], z[1]);
+  box_muller_f32(r.z, r.w, z[2], z[3]);
+}
+// Two double normals of block b: draw dims 2b, 2b+1.
+__device__ __forceinline__ void philox_normals2_f64(int64_t block, int64_t path,
+                                                    uint32_t k0, uint32_t k1,
+                                                    double z[2]) {
+  uint4 r = philox4x32_10(philox_counter(block, path), k0, k1);
+  box_muller_f64(r, z[0], z[1]);
+}
+
+template <typename T>
+struct NormalsPerBlock;
+template <>
+struct NormalsPerBlock<float> {
+  static constexpr int value = 4;
+};
+template <>
+struct NormalsPerBlock<double> {
+  static constexpr int value = 2;
+};
+
+// Sequential reader of the canonical stream for one path: get(k) for
+// non-decreasing k regenerates a block only when k leaves it.  Register-only
+// (selects instead of a dynamically indexed array).
+template <typename T>
+struct PhiloxReader;
+
+template <>
+struct PhiloxReader<float> {
+  int64_t path;
+  uint32_t k0, k1;
+  int64_t blk;
+  float z0, z1, z2, z3;
+  __device__ __forceinline__ PhiloxReader(int64_t p, uint32_t a, uint32_t b)
+      : path(p), k0(a), k1(b), blk(-1), z0(0), z1(0), z2(0), z3(0) {}
+  __device__ __forceinline__ float get(int64_t k) {
+    const int64_t b = k >> 2;
+    if (b != blk) {
+      float z[4];
+      philox_normals4_f32(b, path, k0, k1, z);
+      z0 = z[0]; z1 = z[1]; z2 = z[2]; z3 = z[3];
+      blk = b;
+    }
+    const int l = (int)(k & 3);
+    return l == 0 ? z0 : (l == 1 ? z1 : (l == 2 ? z2 : z3));
+  }
+};
+
+template <>
+struct PhiloxReader<double> {
+  int64_t path;
+  uint32_t k0, k1;
+  int64_t blk;
+  double z0, z1;
+  __device__ __forceinline__ PhiloxReader(int64_t p, uint32_t a, uint32_t b)
+      : path(p), k0(a), k1(b), blk(-1), z0(0), z1(0) {}
+  __device__ __forceinline__ double get(int64_t k) {
+    const int64_t b = k >> 1;
+    if (b != blk) {
+      double z[2];
+      philox_normals2_f64(b, path, k0, k1, z);
+      z0 = z[0]; z1 = z[1];
+      blk = b;
+    }
+    return (k & 1) ? z1 : z0;
+  }
+};
+
+// Per-path view of a tqf_draws block: resolves antithetic pairing and the
+// global path index once, then serves draws by (step, component).
+template <typename T>
+struct DrawSource {
+  const T* base;
+  int64_t s_step, s_comp;
+  T sign;
+  PhiloxReader<T> rng;
+  int d;
+  bool mem;
+  __device__ __forceinline__ DrawSource(const tqf_draws& dr, int64_t path, int dim)
+      : base(nullptr), s_step(0), s_comp(0), sign(T(1)), rng(0, dr.key0, dr.key1),
+        d(dim), mem(dr.source == TQF_DRAWS_MEMORY) {
+    if (mem) {
+      base = static_cast<const T*>(dr.ptr) + path * dr.stride_path;
+      s_step = dr.stride_step;
+      s_comp = dr.stride_comp;
+    } else {
+      int64_t p = path;
+      if (dr.antithetic && p >= dr.antithetic_half) {
+        p -= dr.antithetic_half;
+        sign = T(-1);
+      }
+      rng.path = p + dr.path_offset;
+    }
+  }
+  __device__ __forceinline__ T get(int step, int comp) {
+    if (mem) return base[step * s_step + comp * s_comp];
+    return sign * rng.get((int64_t)step * d + comp);
+  }
+};
+
+// ---- shared-memory staging by TMA bulk copy -------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// 1-D bulk copy global -> this CTA's shared memory; src, dst 16-byte aligned,
+// bytes a multiple of 16.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes,
+                                              uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: gives up after ~`limit` polls (tens of ms), never hangs.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  int limit = 1 << 20) {
+  for (int it = 0; it < limit; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    __nanosleep(64);
+  }
+  return false;
+}
+
+// Stages `nbytes` (multiple of 16) from global `src` into shared `dst` with
+// one elected thread issuing bulk copies of <= 64 KiB; every thread of the
+// CTA returns true once the data is visible, or false (uniformly) after a
+// timed-out wait, having recorded TQF_E_TIMEOUT in *status.
+__device__ __forceinline__ bool stage_to_smem(void* dst, const void* src, uint32_t nbytes,
+                                              uint64_t* bar, uint32_t& phase, int32_t* status) {
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(bar, nbytes);
+    uint32_t off = 0;
+    while (off < nbytes) {
+      uint32_t chunk = nbytes - off;
+      if (chunk > 65536u) chunk = 65536u;
+      bulk_copy_g2s(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, chunk,
+                    bar);
+      off += chunk;
+    }
+  }
+  bool ok = mbar_wait_bounded(bar, phase);
+  ok = __syncthreads_and(ok) != 0;
+  if (!ok) {
+    if (threadIdx.x == 0 && status) atomicExch(status, TQF_E_TIMEOUT);
+    mbar_wait_bounded(bar, phase);  // let in-flight copies land before exit
+    __syncthreads();
+    return false;
+  }
+  phase ^= 1u;
+  return true;
+}
+
+// ---- FP64 European payoff accumulation --------------------------------------
+// Each round, the CTA's BLOCK threads have one terminal spot each in
+// s_spot[] (NaN for no path).  Work item w = (strike j, quarter q) sums
+// payoffs of the paths of quarter q in FP32 and folds them into its own FP64
+// accumulators acc[w] — fixed order, no atomics.
+template <int BLOCK>
+struct PayoffAccum {
+  static constexpr int kQuarters = 4;
+  static constexpr int kPathsPerQuarter = BLOCK / kQuarters;
+};
+
+template <int BLOCK, typename T>
+__device__ __forceinline__ void payoff_round(const T* s_spot, const T* s_strike,
+                                             const uint8_t* s_call, int num_strikes,
+                                             double* acc /* smem [num_strikes*4][2] */) {
+  constexpr int Q = PayoffAccum<BLOCK>::kQuarters;
+  constexpr int PPQ = PayoffAccum<BLOCK>::kPathsPerQuarter;
+  const int items = num_strikes * Q;
+  for (int w = threadIdx.x; w < items; w += BLOCK) {
+    const int j = w % num_strikes;
+    const int q = w / num_strikes;
+    const T K = s_strike[j];
+    const bool call = s_call[j] != 0;
+    T s1 = T(0), s2 = T(0);
+#pragma unroll 8
+    for (int p = 0; p < PPQ; ++p) {
+      const T S = s_spot[q * PPQ + p];
+      T f = call ? (S - K) : (K - S);
+      f = f > T(0) ? f : T(0);  // NaN spot (no path) -> 0
+      s1 += f;
+      s2 = fma(f, f, s2);
+    }
+    acc[2 * w] += (double)s1;
+    acc[2 * w + 1] += (double)s2;
+  }
+}
+
+// Writes the CTA's partial sums (quarters folded in order) to
+// workspace[blockIdx.x][num_strikes][2].
+__device__ __forceinline__ void payoff_flush(const double* acc, int num_strikes, int quarters,
+                                             double* workspace) {
+  for (int j = threadIdx.x; j < num_strikes; j += blockDim.x) {
+    double a = 0.0, b = 0.0;
+    for (int q = 0; q < quarters; ++q) {
+      a += acc[2 * (q * num_strikes + j)];
+      b += acc[2 * (q * num_strikes + j) + 1];
+    }
+    workspace[((size_t)blockIdx.x * num_strikes + j) * 2] = a;
+    workspace[((size_t)blockIdx.x * num_strikes + j) * 2 + 1] = b;
+  }
+}
+
+// Host: launches the fixed-order reduction of `num_partials` partial rows of
+// width `width` doubles into out[width].
+int reduce_partials(const double* partials, int num_partials, int width, double* out,
+                    cudaStream_t stream);
+
+}  // namespace tqf

@@ -1,0 +1,46 @@
+"""Batch-free piecewise-constant functions (tff/math/piecewise.py:19-176).
+
+Used by the Heston model for time-dependent parameters; evaluated on the
+host into per-step parameter tables before a kernel launch.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+
+class PiecewiseConstantFunc:
+    """f(x) = values[i] on (jump_locations[i-1], jump_locations[i]] (left-continuous)."""
+
+    def __init__(self, jump_locations, values, dtype=None, name=None):
+        self._name = name or "PiecewiseConstantFunc"
+        self.is_piecewise_constant = True
+        dtype = np.dtype(dtype) if dtype is not None else None
+        jl = np.asarray(jump_locations, dtype=dtype)
+        self._dtype = dtype or (jl.dtype if jl.dtype.kind == "f" else np.dtype(np.float32))
+        self._jump_locations = jl.astype(self._dtype)
+        self._values = np.asarray(values, dtype=self._dtype)
+        if self._jump_locations.ndim != 1:
+            raise NotImplementedError("batched PiecewiseConstantFunc is not supported")
+        if self._values.shape[0] - 1 != self._jump_locations.shape[-1]:
+            raise ValueError(
+                "Event shape of `values` should have one more element than the event shape of "
+                f"`jump_locations` but are {self._values.shape[0]} and {self._jump_locations.shape[-1]}")
+
+    def dtype(self):
+        return self._dtype
+
+    def values(self):
+        return self._values
+
+    def jump_locations(self):
+        return self._jump_locations
+
+    def name(self):
+        return self._name
+
+    def __call__(self, x, left_continuous=True, name=None):
+        x = np.asarray(x, dtype=self._dtype)
+        side = "left" if left_continuous else "right"
+        idx = np.searchsorted(self._jump_locations, x, side=side)
+        return self._values[idx]

@@ -1,0 +1,165 @@
+"""Grid construction, draw generation and output-slot planning
+(tff/models/utils.py:20-128, 209-320).
+
+Grids are small host-side arrays; they are built with NumPy in the dtype of
+the request, reproducing TensorFlow's arithmetic: tf.range(a, b, d) has
+ceil((b - a)/d) points a + i*d and tf.linspace(a, b, n) is
+[a, a + d, ..., a + (n-2) d, b] with d = (b - a)/(n - 1).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from tqf import _lib
+from tqf.math.random import multivariate_normal as mvn
+from tqf.math.random.multivariate_normal import RandomType
+
+
+def np_dtype(dtype) -> np.dtype:
+    if isinstance(dtype, torch.dtype):
+        return np.dtype({torch.float32: np.float32, torch.float64: np.float64}[dtype])
+    return np.dtype(dtype)
+
+
+def torch_dtype(dtype) -> torch.dtype:
+    if isinstance(dtype, torch.dtype):
+        return dtype
+    return {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64}[np.dtype(dtype)]
+
+
+def to_numpy(x, dtype=None) -> np.ndarray:
+    if isinstance(x, torch.Tensor):
+        x = x.detach().cpu().numpy()
+    a = np.asarray(x)
+    return a.astype(dtype) if dtype is not None else a
+
+
+def infer_dtype(x) -> np.dtype:
+    """TensorFlow's convert_to_tensor dtype: Python floats -> float32."""
+    if isinstance(x, torch.Tensor):
+        return np_dtype(x.dtype)
+    if isinstance(x, np.ndarray) and x.dtype.kind == "f":
+        return x.dtype
+    if isinstance(x, np.floating):
+        return np.dtype(type(x))
+    return np.dtype(np.float32)
+
+
+def tf_range(start, limit, delta, dtype) -> np.ndarray:
+    t = np.dtype(dtype).type
+    start, limit, delta = t(start), t(limit), t(delta)
+    n = int(np.ceil(np.abs((limit - start) / delta)))
+    return (start + np.arange(n).astype(dtype) * delta).astype(dtype)
+
+
+def tf_linspace(start, stop, num, dtype) -> np.ndarray:
+    t = np.dtype(dtype).type
+    start, stop, num = t(start), t(stop), int(num)
+    if num <= 0:
+        return np.zeros(0, dtype=dtype)
+    if num == 1:
+        return np.array([start], dtype=dtype)
+    d = (stop - start) / t(num - 1)
+    inner = (start + d * np.arange(1, num - 1).astype(dtype)).astype(dtype)
+    return np.concatenate([[start], inner, [stop]]).astype(dtype)
+
+
+def prepare_grid(*, times, time_step, dtype, tolerance=None, num_time_steps=None, times_grid=None):
+    """Returns (all_times, keep_mask, time_indices) as NumPy arrays
+    (tff/models/utils.py:209-282)."""
+    dtype = np_dtype(dtype)
+    t = dtype.type
+    times = to_numpy(times, dtype).reshape(-1)
+    if tolerance is None:
+        tolerance = 1e-10 if dtype == np.float64 else 1e-6
+    tol = t(tolerance)
+    if times_grid is None:
+        if num_time_steps is None:
+            grid = tf_range(0.0, times[-1], to_numpy(time_step, dtype), dtype)
+            all_times = np.sort(np.concatenate([times, grid]), kind="stable").astype(dtype)
+            diffs = np.concatenate([[t(1.0)], np.diff(all_times)]).astype(dtype)
+            all_times = all_times[diffs > tol]
+            ti = np.searchsorted(all_times, times, side="left")
+            ti = np.minimum(ti, len(all_times) - 1)
+            ti = np.where(all_times[ti] - times > tol, ti - 1, ti)
+        else:
+            step = t(to_numpy(time_step, dtype))
+            uniform = tf_linspace(step, times[-1] - step, max(int(num_time_steps) - len(times), 0), dtype)
+            grid = np.sort(np.concatenate([uniform, times]), kind="stable").astype(dtype)
+            all_times = np.concatenate([[t(0)], grid]).astype(dtype)
+            ti = np.searchsorted(all_times, times, side="left")
+    else:
+        all_times = to_numpy(times_grid, dtype).reshape(-1)
+        ti = np.searchsorted(all_times, times, side="left")
+        near = all_times[np.minimum(ti, len(all_times) - 1)] - times
+        prev = all_times[np.maximum(ti - 1, 0)] - times
+        ti = np.where(np.abs(prev) > np.abs(near), ti, np.maximum(ti - 1, 0))
+    ti = ti.astype(np.int32)
+    mask = np.zeros(len(all_times), dtype=bool)
+    mask[ti] = True
+    return all_times, mask, ti
+
+
+def plan_output_slots(keep_mask, num_requested: int, initial_written_count: int):
+    """Replays the reference's written_count recursion (euler_sampling.py:424-455;
+    heston_model.py:441-446 starts it at 0) on the host.
+
+    Returns (step_slot[steps_exec] int32, init_slot, steps_exec, unwritten):
+    step_slot[i] is the slot that finally holds the state after step i (-1 if
+    a later step overwrites it), init_slot the slot that keeps the initial
+    state (-1 if none), steps_exec the number of steps the loop runs before
+    written_count reaches num_requested, and `unwritten` the slots no write
+    reaches (left as zeros).
+    """
+    steps = len(keep_mask) - 1
+    wc = int(initial_written_count)
+    owner = {0: -1}
+    i = 0
+    while i < steps and wc < num_requested:
+        owner[wc] = i
+        wc += int(keep_mask[i + 1])
+        i += 1
+    step_slot = np.full(i, -1, dtype=np.int32)
+    for slot, step in owner.items():
+        if step >= 0:
+            step_slot[step] = slot
+    init_slot = 0 if owner[0] == -1 else -1
+    unwritten = [s for s in range(num_requested) if s not in owner]
+    return step_slot, init_slot, i, unwritten
+
+
+def generate_mc_normal_draws(num_normal_draws, num_time_steps, num_sample_paths, random_type,
+                             batch_shape=None, skip=0, seed=None, dtype=None, name=None):
+    """[num_time_steps] + batch_shape + [num_sample_paths, num_normal_draws]
+    draws (tff/models/utils.py:20-128).  Sobol dimension of (step i,
+    component c) is i * num_normal_draws + c, point index skip + 1 + path."""
+    del name
+    dtype = torch.float32 if dtype is None else torch_dtype(dtype)
+    batch_shape = tuple(int(b) for b in (batch_shape or ()))
+    nb = int(np.prod(batch_shape)) if batch_shape else 1
+    total = nb * int(num_sample_paths)
+    if random_type is None:
+        random_type = RandomType.PSEUDO
+    if random_type == RandomType.SOBOL:
+        if batch_shape:
+            raise NotImplementedError("SOBOL draws with a batch_shape are not supported")
+        from tqf.math.random import sobol
+        return sobol.normal_draws(int(num_normal_draws), int(num_time_steps), int(num_sample_paths),
+                                  skip=int(skip or 0), dtype=dtype)
+    if random_type in (RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
+        raise NotImplementedError("HALTON random types are not built in this engine")
+    if mvn.is_antithetic(random_type) and batch_shape:
+        raise NotImplementedError("antithetic draws with a batch_shape are not supported")
+    draws = mvn.philox_normal_draws(random_type, seed, int(num_normal_draws), int(num_time_steps),
+                                    total, dtype)
+    return draws.reshape((int(num_time_steps),) + batch_shape + (int(num_sample_paths), int(num_normal_draws)))
+
+
+def step_table(rows: np.ndarray, dtype: torch.dtype, device) -> torch.Tensor:
+    """Uploads a [steps, cols] host table (16-byte aligned device copy)."""
+    return torch.as_tensor(np.ascontiguousarray(rows), dtype=dtype).to(device, non_blocking=False)
+
+
+__all__ = ["prepare_grid", "generate_mc_normal_draws", "plan_output_slots", "tf_range", "tf_linspace"]

@@ -1,0 +1,83 @@
+"""European payoff statistics over stored terminal values (``tqf_european_payoff_sums``)."""
+
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+import torch
+
+from tqf import _lib
+from tqf.models import utils
+
+_workspaces: dict[tuple[int, str], torch.Tensor] = {}
+
+
+def workspace(nbytes: int, device: torch.device, tag: str) -> torch.Tensor:
+    """Reusable device scratch of at least `nbytes` bytes (per device and tag)."""
+    idx = device.index if device.index is not None else torch.cuda.current_device()
+    key = (idx, tag)
+    buf = _workspaces.get(key)
+    if buf is None or buf.numel() < nbytes:
+        buf = torch.empty(max(int(nbytes), 16), dtype=torch.uint8, device=device)
+        _workspaces[key] = buf
+    return buf
+
+
+@dataclasses.dataclass
+class MonteCarloResult:
+    """Discounted prices and standard errors per strike (FP64, on device)."""
+
+    price: torch.Tensor
+    standard_error: torch.Tensor
+    sums: torch.Tensor  # [n_strikes, 2] raw (sum, sum of squares) of undiscounted payoffs
+    num_paths: int
+    discount: float
+
+
+def stats_from_sums(sums: torch.Tensor, n: int, discount: float) -> MonteCarloResult:
+    s1 = sums[:, 0]
+    s2 = sums[:, 1]
+    mean = s1 / n
+    var = torch.clamp(s2 / n - mean * mean, min=0.0) * (n / max(n - 1, 1))
+    se = torch.sqrt(var / n)
+    return MonteCarloResult(price=discount * mean, standard_error=discount * se, sums=sums,
+                            num_paths=n, discount=discount)
+
+
+def make_payoff(strikes, is_call, dtype, device, num_paths, ws_bytes_fn, tag):
+    k = torch.as_tensor(utils.to_numpy(strikes, np.float64).reshape(-1), dtype=dtype).to(device)
+    ns = int(k.numel())
+    calls = None
+    if is_call is not None:
+        calls = torch.as_tensor(np.broadcast_to(np.asarray(is_call, dtype=np.uint8), (ns,)).copy()).to(device)
+    out = torch.zeros((ns, 2), dtype=torch.float64, device=device)
+    nbytes = int(ws_bytes_fn(ns))
+    ws = workspace(nbytes, device, tag)
+    p = _lib.Payoff()
+    p.num_strikes = ns
+    p.strikes = k.data_ptr()
+    p.is_call = calls.data_ptr() if calls is not None else None
+    p.spot_scale = 1.0
+    p.out = out.data_ptr()
+    p.workspace = ws.data_ptr()
+    p.workspace_bytes = ws.numel()
+    return p, out, (k, calls, ws)
+
+
+def european_payoff_stats(values: torch.Tensor, strikes, is_call=None, discount: float = 1.0,
+                          log_values: bool = False, spot_scale: float = 1.0) -> MonteCarloResult:
+    """Mean discounted max(S - K, 0) (or put) over S = spot_scale * values
+    (or spot_scale * exp(values)) with FP64 accumulation."""
+    device = _lib.require_cuda()
+    v = values.reshape(-1)
+    if not v.is_contiguous():
+        v = v.contiguous()
+    n = int(v.numel())
+    p, out, keep = make_payoff(strikes, is_call, v.dtype, device, n,
+                               lambda ns: _lib.load().tqf_european_workspace_bytes(n, ns), "european")
+    p.spot_scale = float(spot_scale)
+    _lib.call("tqf_european_payoff_sums", _lib.dtype_code(v.dtype), v.data_ptr(), 1, n,
+              1 if log_values else 0, p, _lib.stream_ptr(device))
+    del keep
+    return stats_from_sums(out, n, discount)

@@ -1,0 +1,88 @@
+"""Fused Heston European pricing: path simulation, payoff over a strike
+batch and FP64 accumulation in one kernel pass.
+
+``scheme="full_truncation"``: log-spot full-truncation Euler with the rate in
+the drift (``tqf_heston_euler``), the reference Euler sampler's arithmetic
+for the coefficients of ``coefficients.heston_full_truncation``.
+``scheme="qe"``: the reference HestonModel QE scheme (``tqf_heston_qe``);
+it has no rate term, so S_T = exp(X_T + r T) as in heston_model_test.py:349-352.
+Both use a uniform grid of ``num_time_steps`` steps to ``expiry``.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from tqf import _lib
+from tqf.math.random import multivariate_normal as mvn
+from tqf.math.random.multivariate_normal import RandomType
+from tqf.models import heston_model
+from tqf.models import utils
+from tqf.models.coefficients import HestonFullTruncation
+from tqf.pricing.european import make_payoff, stats_from_sums
+
+_tables: dict = {}
+
+
+def _table(key, build, td, device):
+    t = _tables.get(key)
+    if t is None:
+        t = utils.step_table(build(), td, device)
+        _tables[key] = t
+    return t
+
+
+def heston_european_mc(*, strikes, expiry, spot, variance, mean_reversion, theta, volvol, rho,
+                       discount_rate=0.0, is_call_options=None, num_samples, num_time_steps,
+                       scheme="full_truncation", random_type=RandomType.STATELESS, seed=(1, 2),
+                       dtype=torch.float32, path_offset=0, normal_draws=None):
+    """Returns a MonteCarloResult with per-strike discounted prices and
+    standard errors (FP64 on the device)."""
+    device = _lib.require_cuda()
+    td = utils.torch_dtype(dtype)
+    np_dt = utils.np_dtype(td)
+    T, r = float(expiry), float(discount_rate)
+    steps = int(num_time_steps)
+    N = int(num_samples)
+    all_times = np.linspace(0.0, T, steps + 1).astype(np_dt)
+    dt = (all_times[1:] - all_times[:-1]).astype(np_dt)
+    sqrt_dt = np.sqrt(dt).astype(np_dt)
+    no_slots = np.full(steps, -1, dtype=np.int32)
+    qe = scheme == "qe"
+    params = (float(mean_reversion), float(theta), float(volvol), float(rho))
+    if qe:
+        model = heston_model.HestonModel(*params, dtype=np_dt)
+        key = ("qe", np_dt.str, T, steps, params, device.index)
+        tab = _table(key, lambda: model._qe_table(all_times, 1e-6, no_slots, steps), td, device)
+        x0, scale = float(np.log(spot)), float(np.exp(r * T))
+    else:
+        h = HestonFullTruncation(r, *params)
+        key = ("ft", np_dt.str, T, steps, params, r, device.index)
+        tab = _table(key, lambda: heston_model.full_truncation_table(h, all_times, dt, sqrt_dt, no_slots, steps),
+                     td, device)
+        x0, scale = float(np.log(spot)), 1.0
+    if normal_draws is not None:
+        draws = mvn.memory_draws(normal_draws, path_axis=0, step_axis=1)
+    else:
+        draws = mvn.philox_draws(random_type, seed, N, path_offset)
+    qe_flag = 1 if qe else 0
+    p, out, keep = make_payoff(strikes, is_call_options, td, device, N,
+                               lambda ns: _lib.load().tqf_heston_workspace_bytes(_lib.dtype_code(td), qe_flag, N, ns),
+                               "heston")
+    p.spot_scale = scale
+    args = _lib.HestonArgs()
+    args.dtype = _lib.dtype_code(td)
+    args.num_steps = steps
+    args.num_paths = N
+    args.step_table = tab.data_ptr()
+    args.x0, args.v0 = x0, float(variance)
+    args.draws = draws
+    args.payoff = p
+    args.dev_status = _lib.status_buffer(device).data_ptr()
+    _lib.call("tqf_heston_qe" if qe else "tqf_heston_euler", args, _lib.stream_ptr(device))
+    del keep
+    return stats_from_sums(out, N, float(np.exp(-r * T)))
+
+
+__all__ = ["heston_european_mc"]
