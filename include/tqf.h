@@ -260,10 +260,106 @@ TQF_API int tqf_heston_euler(const tqf_heston_args* args, void* stream);
  * (log-spot, variance). */
 TQF_API int tqf_heston_qe(const tqf_heston_args* args, void* stream);
 
+/* Pathwise adjoint of the full-truncation Euler European pricer (no
+ * reference counterpart beyond the GradientTape of the Euler sampler with
+ * watch_params, tff/models/euler_sampling.py:467-510): replays the paths of
+ * tqf_heston_euler from the same draws with forward tangents of (x, v) with
+ * respect to (log S0, v0, kappa, theta, xi, rho, r) and writes
+ * out[7] (device, FP64) = sum_paths c_p S_T,p dx_T,p/dparam with
+ * c_p = sum_j weights_j dPayoff_j/dS_T.  step_table as tqf_heston_euler
+ * with constant parameters; xi and rho passed explicitly. */
+typedef struct tqf_heston_adjoint_args {
+  int32_t dtype;
+  int32_t num_steps;
+  int64_t num_paths;
+  const void* step_table;
+  double x0;
+  double v0;
+  double xi;
+  double rho;
+  tqf_draws draws;
+  int32_t num_strikes;
+  int32_t pad0;
+  const void* strikes;    /* [num_strikes] dtype */
+  const uint8_t* is_call; /* [num_strikes] or NULL */
+  const void* weights;    /* [num_strikes] dtype */
+  double* out;            /* [7] */
+  void* workspace;
+  size_t workspace_bytes;
+  int32_t* dev_status;
+} tqf_heston_adjoint_args;
+
+TQF_API int tqf_heston_euler_adjoint(const tqf_heston_adjoint_args* args, void* stream);
+TQF_API size_t tqf_heston_adjoint_workspace_bytes(int64_t num_paths);
+
 /* Workspace bytes that tqf_heston_euler / tqf_heston_qe need in
  * payoff.workspace for a given dtype, path count and strike count. */
 TQF_API size_t tqf_heston_workspace_bytes(int32_t dtype, int32_t qe, int64_t num_paths,
                                   int32_t num_strikes);
+
+/* ---- correlated GBM (multivariate_geometric_brownian_motion.py) ------------ */
+
+/* Exact log scheme of MultivariateGeometricBrownianMotion.sample_paths
+ * (tff/models/geometric_brownian_motion/multivariate_geometric_brownian_motion.py:229-281):
+ * cumsum_i += drift_i dt + sqrt(dt) vol_i (L z)_i, state x0_i exp(cumsum_i)
+ * stored at the slots of step_table [num_steps][4] = (dt, sqrt_dt, slot, 0).
+ * drift = mu - vol^2/2 ([dim]), vol [dim], chol = L [dim, dim] row-major
+ * lower-triangular or NULL (independent components), dim <= 16. */
+typedef struct tqf_mvgbm_args {
+  int32_t dtype;
+  int32_t dim;
+  int64_t num_paths;
+  int32_t num_steps;
+  int32_t x0_per_path;
+  const void* step_table;
+  const void* x0;
+  const void* drift;
+  const void* vol;
+  const void* chol;
+  tqf_draws draws;
+  tqf_path_output output;
+  int32_t* dev_status;
+} tqf_mvgbm_args;
+
+/* FP64 Cholesky factor L (row-major, lower) of an n x n symmetric positive
+ * definite matrix, n <= 64, on the GPU in one CTA (replaces
+ * tf.linalg.cholesky at multivariate_geometric_brownian_motion.py:264 and
+ * multivariate_normal.py:436).  *info (device int) = 0 on success, k + 1
+ * when the k-th pivot is not positive. */
+TQF_API int tqf_cholesky_f64(const double* a, int32_t n, double* l, int32_t* info, void* stream);
+
+TQF_API int tqf_mvgbm_paths(const tqf_mvgbm_args* args, void* stream);
+
+/* Arithmetic-basket European option on correlated GBM at the last step, with
+ * pathwise sensitivities, FP64 accumulation.  out[2 + 2*dim] (device) =
+ * (sum P, sum P^2, sum_p g_i (i < dim), sum_p g_i (y_i - vol_i T) (i < dim))
+ * with P the undiscounted payoff on B = sum_i weights_i S_T,i,
+ * g_i = dP/dB * weights_i * S_T,i and y = L sum_k sqrt(dt_k) z_k, so that
+ * dP/dS0_i = g_i / S0_i, dP/dvol_i = g_i (y_i - vol_i T), dP/dmu_i = g_i T.
+ * With out == NULL the per-CTA partials stay in the workspace. */
+typedef struct tqf_basket_args {
+  int32_t dtype;
+  int32_t dim;
+  int64_t num_paths;
+  int32_t num_steps;
+  int32_t is_call;
+  const void* sqrt_dt; /* [num_steps] */
+  double total_time;
+  double strike;
+  const void* spot;    /* [dim] */
+  const void* drift;   /* [dim] mu - vol^2/2 */
+  const void* vol;     /* [dim] */
+  const void* chol;    /* [dim, dim] or NULL */
+  const void* weights; /* [dim] */
+  tqf_draws draws;
+  double* out;
+  void* workspace;
+  size_t workspace_bytes;
+  int32_t* dev_status;
+} tqf_basket_args;
+
+TQF_API int tqf_basket_price(const tqf_basket_args* args, void* stream);
+TQF_API size_t tqf_basket_workspace_bytes(int32_t dtype, int32_t dim, int64_t num_paths);
 
 /* ---- payoff reduction over stored values ----------------------------------- */
 

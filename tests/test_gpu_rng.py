@@ -137,8 +137,17 @@ def test_philox_normal_draws_match_oracle(cuda, dtype, antithetic):
     got = philox_normal_draws(rt, [5, 6], d, steps, N, dtype).cpu().numpy()
     want = ophilox.normal_draws(N, steps, d, 5, 6, dtype=np.float32 if dtype == torch.float32 else np.float64,
                                 antithetic=antithetic)
-    tol = 5e-6 if dtype == torch.float32 else 1e-12
-    np.testing.assert_allclose(got, want, rtol=tol, atol=tol)
+    if dtype == torch.float32:
+        # Device float32 Box–Muller uses the SFU lg2 (absolute error ~2^-22),
+        # so |dz| <= 4e-6 + 2.5e-7 / r with r the Box–Muller radius of the pair.
+        flat = want.transpose(1, 0, 2).reshape(N, -1)
+        pairs = flat.reshape(N, -1, 2)
+        rad = np.sqrt((pairs ** 2).sum(-1))
+        rad = np.repeat(rad, 2, axis=1).reshape(N, steps, d).transpose(1, 0, 2)
+        bound = 4e-6 * (1 + np.abs(want)) + 2.5e-7 / rad
+        assert np.all(np.abs(got - want) <= bound)
+    else:
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12)
 
 
 def test_draws_prefix_stability_and_moments(cuda):

@@ -221,6 +221,145 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// ---- pathwise adjoint of the full-truncation Euler pricer ------------------
+// Replays each path from its counter-based draws carrying forward tangents
+// of (x, v) with respect to P = (log S0, v0, kappa, theta, xi, rho, r), then
+// contracts with the upstream weights: per path
+//   c = sum_j w_j dPayoff_j/dS_T (call: 1{S > K_j}, put: -1{S < K_j}),
+//   out_p += c * S_T * dx_T/dP_p.
+// Parameters are constant in time here (the pricing API's grid).
+constexpr int kAdjParams = 7;
+
+template <int P, typename T>
+__device__ __forceinline__ void adj_param_step(T dt, T dw0, T dw1, T vp, T sq, T dsq, T kappa, T theta,
+                                               T A, T B, T rho, T xi, T sr, T& xd, T& vd) {
+  // explicit derivatives of the step coefficients w.r.t. parameter P
+  constexpr bool is_k = P == 2, is_th = P == 3, is_xi = P == 4, is_rho = P == 5, is_r = P == 6;
+  const T vpd = vp > T(0) ? vd : T(0);
+  const T sqd = dsq * vpd;
+  T xdn = xd + dt * (-T(0.5) * vpd) + sqd * dw0;
+  if (is_r) xdn += dt;
+  T vdn = vd + dt * (-kappa * vpd);
+  if (is_k) vdn += dt * (theta - vp);
+  if (is_th) vdn += dt * kappa;
+  T Ad = T(0), Bd = T(0);
+  if (is_xi) {
+    Ad = rho;
+    Bd = sr;
+  }
+  if (is_rho) {
+    Ad = xi;
+    Bd = -xi * rho / sr;
+  }
+  vdn += (Ad * sq + A * sqd) * dw0 + (Bd * sq + B * sqd) * dw1;
+  xd = xdn;
+  vd = vdn;
+}
+
+template <typename T, int SRC>
+__global__ void __launch_bounds__(kBlock) heston_adjoint_kernel(tqf_heston_adjoint_args a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* s_strike = reinterpret_cast<T*>(smem);
+  T* s_w = s_strike + a.num_strikes;
+  uint8_t* s_call = reinterpret_cast<uint8_t*>(s_w + a.num_strikes);
+  __shared__ double acc[kBlock / 32][kAdjParams];
+  for (int i = threadIdx.x; i < a.num_strikes; i += kBlock) {
+    s_strike[i] = static_cast<const T*>(a.strikes)[i];
+    s_w[i] = static_cast<const T*>(a.weights)[i];
+    s_call[i] = a.is_call ? a.is_call[i] : (uint8_t)1;
+  }
+  for (int i = threadIdx.x; i < (kBlock / 32) * kAdjParams; i += kBlock) (&acc[0][0])[i] = 0.0;
+  __syncthreads();
+  const T* table = static_cast<const T*>(a.step_table);
+  const T xi = (T)a.xi, rho = (T)a.rho, sr = sqrt(T(1) - rho * rho);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t per_round = (int64_t)gridDim.x * kBlock;
+  for (int64_t base = 0; base < a.num_paths; base += per_round) {
+    const int64_t path = base + (int64_t)blockIdx.x * kBlock + threadIdx.x;
+    T q[kAdjParams];
+#pragma unroll
+    for (int p = 0; p < kAdjParams; ++p) q[p] = T(0);
+    if (path < a.num_paths) {
+      T x = (T)a.x0, v = (T)a.v0;
+      T xd[kAdjParams], vd[kAdjParams];
+#pragma unroll
+      for (int p = 0; p < kAdjParams; ++p) {
+        xd[p] = p == 0 ? T(1) : T(0);
+        vd[p] = p == 1 ? T(1) : T(0);
+      }
+      DrawSource<T> src(a.draws, path, 2);
+      for (int i = 0; i < a.num_steps; ++i) {
+        const T* row = table + (size_t)i * kFtCols;
+        const T dt = row[0], sdt = row[1], kappa = row[3], theta = row[4], A = row[5], B = row[6];
+        const T z0 = src.get(i, 0), z1 = src.get(i, 1);
+        const T vp = v > T(0) ? v : T(0);
+        const T sq = sqrt(vp);
+        const T dsq = sq > T(0) ? T(0.5) / sq : T(0);
+        const T dw0 = z0 * sdt, dw1 = z1 * sdt;
+        adj_param_step<0, T>(dt, dw0, dw1, vp, sq, dsq, kappa, theta, A, B, rho, xi, sr, xd[0], vd[0]);
+        adj_param_step<1, T>(dt, dw0, dw1, vp, sq, dsq, kappa, theta, A, B, rho, xi, sr, xd[1], vd[1]);
+        adj_param_step<2, T>(dt, dw0, dw1, vp, sq, dsq, kappa, theta, A, B, rho, xi, sr, xd[2], vd[2]);
+        adj_param_step<3, T>(dt, dw0, dw1, vp, sq, dsq, kappa, theta, A, B, rho, xi, sr, xd[3], vd[3]);
+        adj_param_step<4, T>(dt, dw0, dw1, vp, sq, dsq, kappa, theta, A, B, rho, xi, sr, xd[4], vd[4]);
+        adj_param_step<5, T>(dt, dw0, dw1, vp, sq, dsq, kappa, theta, A, B, rho, xi, sr, xd[5], vd[5]);
+        adj_param_step<6, T>(dt, dw0, dw1, vp, sq, dsq, kappa, theta, A, B, rho, xi, sr, xd[6], vd[6]);
+        ft_step<T>(row, z0, z1, x, v);
+      }
+      const T S = exp(x);
+      T c = T(0);
+      for (int j = 0; j < a.num_strikes; ++j) {
+        const bool call = s_call[j] != 0;
+        if (call ? (S > s_strike[j]) : (S < s_strike[j])) c += call ? s_w[j] : -s_w[j];
+      }
+#pragma unroll
+      for (int p = 0; p < kAdjParams; ++p) q[p] = c * S * xd[p];
+    }
+#pragma unroll
+    for (int p = 0; p < kAdjParams; ++p) {
+      T v = q[p];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      if (lane == 0) acc[warp][p] += (double)v;
+    }
+  }
+  __syncthreads();
+  double* ws = static_cast<double*>(a.workspace);
+  for (int p = threadIdx.x; p < kAdjParams; p += kBlock) {
+    double s = 0.0;
+    for (int w = 0; w < kBlock / 32; ++w) s += acc[w][p];
+    ws[(size_t)blockIdx.x * kAdjParams + p] = s;
+  }
+}
+
+template <typename T, int SRC>
+int adjoint_grid(int64_t n, size_t smem) {
+  int occ = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, heston_adjoint_kernel<T, SRC>, kBlock, smem);
+  if (occ < 1) occ = 1;
+  int64_t g = (n + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)num_sms() * occ;
+  if (g > cap) g = cap;
+  return (int)(g < 1 ? 1 : g);
+}
+
+template <typename T>
+int run_adjoint(const tqf_heston_adjoint_args& a, cudaStream_t s) {
+  const size_t smem = (size_t)a.num_strikes * (2 * sizeof(T) + 1) + 16;
+  const bool philox = a.draws.source == TQF_DRAWS_PHILOX;
+  const int grid = philox ? adjoint_grid<T, TQF_DRAWS_PHILOX>(a.num_paths, smem)
+                          : adjoint_grid<T, TQF_DRAWS_MEMORY>(a.num_paths, smem);
+  const size_t need = (size_t)grid * kAdjParams * sizeof(double);
+  TQF_REQUIRE(a.workspace && a.workspace_bytes >= need, "tqf_heston_euler_adjoint: workspace %zu < %zu",
+              a.workspace_bytes, need);
+  if (philox)
+    heston_adjoint_kernel<T, TQF_DRAWS_PHILOX><<<grid, kBlock, smem, s>>>(a);
+  else
+    heston_adjoint_kernel<T, TQF_DRAWS_MEMORY><<<grid, kBlock, smem, s>>>(a);
+  int rc = check_launch("heston_adjoint_kernel");
+  if (rc) return rc;
+  return reduce_partials(static_cast<const double*>(a.workspace), grid, kAdjParams, a.out, s);
+}
+
 template <typename T, int SCHEME>
 using KernelFn = void (*)(tqf_heston_args, int, SmemLayout);
 
@@ -326,6 +465,29 @@ extern "C" int tqf_heston_qe(const tqf_heston_args* a, void* stream) {
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   return a->dtype == TQF_F32 ? run<float, 1>(*a, s) : run<double, 1>(*a, s);
+}
+
+extern "C" int tqf_heston_euler_adjoint(const tqf_heston_adjoint_args* a, void* stream) {
+  clear_error();
+  TQF_REQUIRE(a != nullptr, "tqf_heston_euler_adjoint: null args");
+  TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "tqf_heston_euler_adjoint: bad dtype");
+  TQF_REQUIRE(a->num_paths >= 1 && a->num_steps >= 1, "tqf_heston_euler_adjoint: bad sizes");
+  TQF_REQUIRE(a->step_table && a->strikes && a->weights && a->out, "tqf_heston_euler_adjoint: null pointer");
+  TQF_REQUIRE(a->num_strikes >= 1 && a->num_strikes <= 4096, "tqf_heston_euler_adjoint: bad num_strikes");
+  TQF_REQUIRE(a->rho > -1.0 && a->rho < 1.0, "tqf_heston_euler_adjoint: rho must be in (-1, 1)");
+  TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.ptr, "tqf_heston_euler_adjoint: memory draws need ptr");
+  TQF_REQUIRE(!a->draws.antithetic || 2 * a->draws.antithetic_half == a->num_paths,
+              "tqf_heston_euler_adjoint: antithetic needs num_paths == 2 * antithetic_half");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a->dtype == TQF_F32 ? run_adjoint<float>(*a, s) : run_adjoint<double>(*a, s);
+}
+
+extern "C" size_t tqf_heston_adjoint_workspace_bytes(int64_t num_paths) {
+  int64_t g = (num_paths + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)num_sms() * 8;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (size_t)g * kAdjParams * sizeof(double);
 }
 
 extern "C" size_t tqf_heston_workspace_bytes(int32_t dtype, int32_t qe, int64_t num_paths,

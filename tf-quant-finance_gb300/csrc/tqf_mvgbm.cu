@@ -1,0 +1,319 @@
+// Correlated geometric Brownian motion (the exact log scheme of
+// MultivariateGeometricBrownianMotion._sample_paths,
+// tff/models/geometric_brownian_motion/multivariate_geometric_brownian_motion.py:229-281)
+// and a fused arithmetic-basket pricer with pathwise Greeks.
+//
+// mvgbm_paths_kernel: one thread per path, log-state (the running cumsum of
+//   (mu - sigma^2/2) dt + sqrt(dt) sigma (L z)) in registers; L staged in
+//   shared memory; states x0 * exp(cumsum) stored at their slots as
+//   contiguous [dim] rows (16-byte vector stores).
+// basket_price_kernel: the terminal log-state is linear in the draws,
+//   log S_T,i = log S0_i + (mu_i - sigma_i^2/2) T + sigma_i (L w)_i with
+//   w = sum_k sqrt(dt_k) z_k, so the kernel accumulates w (dim FMAs per
+//   step) and applies L once per path.  Per path it forms the basket
+//   B = sum_i a_i S_T,i, the payoff and g_i = 1{B > K} a_i S_T,i, from which
+//   dP/dS0_i = g_i / S0_i, dP/dsigma_i = g_i (y_i - sigma_i T), dP/dmu_i =
+//   g_i T.  Warp-level FP32 partial sums feed per-warp FP64 accumulators
+//   (fixed order, deterministic).
+#include "tqf_internal.cuh"
+
+namespace tqf {
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kWarps = kBlock / 32;
+constexpr int kMaxDim = 16;
+
+template <typename T, int DM>
+struct GbmCoef {
+  T L[DM * DM];
+  T drift[DM];  // mu - sigma^2 / 2
+  T sigma[DM];
+};
+
+template <typename T, int DM>
+__device__ __forceinline__ void load_coef(GbmCoef<T, DM>* c, int dim, const void* chol,
+                                          const void* drift, const void* sigma) {
+  for (int i = threadIdx.x; i < DM * DM; i += blockDim.x) {
+    const int r = i / DM, q = i % DM;
+    T v = T(0);
+    if (r < dim && q < dim) {
+      v = chol ? static_cast<const T*>(chol)[r * dim + q] : (r == q ? T(1) : T(0));
+    }
+    c->L[i] = v;
+  }
+  for (int i = threadIdx.x; i < DM; i += blockDim.x) {
+    c->drift[i] = i < dim ? static_cast<const T*>(drift)[i] : T(0);
+    c->sigma[i] = i < dim ? static_cast<const T*>(sigma)[i] : T(0);
+  }
+}
+
+template <typename T, int DM>
+__global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
+  __shared__ GbmCoef<T, DM> coef;
+  const int dim = a.dim;
+  load_coef<T, DM>(&coef, dim, a.chol, a.drift, a.vol);
+  __syncthreads();
+  const T* table = static_cast<const T*>(a.step_table);
+  T* out = static_cast<T*>(a.output.ptr);
+  const int ns = a.output.num_slots;
+  for (int64_t path = (int64_t)blockIdx.x * kBlock + threadIdx.x; path < a.num_paths;
+       path += (int64_t)gridDim.x * kBlock) {
+    const T* x0p = static_cast<const T*>(a.x0) + (a.x0_per_path ? path * dim : 0);
+    T x0[DM], cs[DM];
+#pragma unroll
+    for (int j = 0; j < DM; ++j) {
+      x0[j] = j < dim ? x0p[j] : T(0);
+      cs[j] = T(0);
+    }
+    if (a.output.init_slot >= 0) {
+      T* o = out + (path * ns + a.output.init_slot) * dim;
+#pragma unroll
+      for (int j = 0; j < DM; ++j)
+        if (j < dim) o[j] = x0[j];
+    }
+    DrawSource<T> src(a.draws, path, dim);
+    for (int i = 0; i < a.num_steps; ++i) {
+      const T dt = table[i * 4], sdt = table[i * 4 + 1];
+      const int slot = (int)table[i * 4 + 2];
+      T z[DM];
+#pragma unroll
+      for (int c = 0; c < DM; ++c) z[c] = c < dim ? src.get(i, c) : T(0);
+#pragma unroll
+      for (int r = 0; r < DM; ++r) {
+        T y = T(0);
+#pragma unroll
+        for (int c = 0; c <= r; ++c) y += coef.L[r * DM + c] * z[c];
+        cs[r] += coef.drift[r] * dt + sdt * coef.sigma[r] * y;
+      }
+      if (slot >= 0) {
+        T* o = out + (path * ns + slot) * dim;
+#pragma unroll
+        for (int j = 0; j < DM; ++j)
+          if (j < dim) o[j] = x0[j] * exp(cs[j]);
+      }
+    }
+  }
+}
+
+// ---- fused basket pricing --------------------------------------------------
+// Per-path quantities reduced: [0] payoff, [1] payoff^2, [2 + i] g_i,
+// [2 + dim + i] g_i (y_i - sigma_i T).
+template <typename T, int DM>
+__global__ void __launch_bounds__(kBlock) basket_price_kernel(tqf_basket_args a) {
+  __shared__ GbmCoef<T, DM> coef;
+  __shared__ T s_spot[DM], s_w[DM];
+  __shared__ double acc[kWarps][2 + 2 * DM];
+  const int dim = a.dim;
+  load_coef<T, DM>(&coef, dim, a.chol, a.drift, a.vol);
+  for (int i = threadIdx.x; i < DM; i += blockDim.x) {
+    s_spot[i] = i < dim ? static_cast<const T*>(a.spot)[i] : T(0);
+    s_w[i] = i < dim ? static_cast<const T*>(a.weights)[i] : T(0);
+  }
+  for (int i = threadIdx.x; i < kWarps * (2 + 2 * DM); i += blockDim.x) (&acc[0][0])[i] = 0.0;
+  __syncthreads();
+  const T* sdt_tab = static_cast<const T*>(a.sqrt_dt);
+  const T T_total = (T)a.total_time;
+  const T K = (T)a.strike;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t per_round = (int64_t)gridDim.x * kBlock;
+  for (int64_t base = 0; base < a.num_paths; base += per_round) {
+    const int64_t path = base + (int64_t)blockIdx.x * kBlock + threadIdx.x;
+    const bool valid = path < a.num_paths;
+    T q[2 + 2 * DM];
+#pragma unroll
+    for (int j = 0; j < 2 + 2 * DM; ++j) q[j] = T(0);
+    if (valid) {
+      T w[DM];
+#pragma unroll
+      for (int j = 0; j < DM; ++j) w[j] = T(0);
+      DrawSource<T> src(a.draws, path, dim);
+      for (int i = 0; i < a.num_steps; ++i) {
+        const T sdt = sdt_tab[i];
+#pragma unroll
+        for (int c = 0; c < DM; ++c)
+          if (c < dim) w[c] += sdt * src.get(i, c);
+      }
+      T S[DM], y[DM];
+      T B = T(0);
+#pragma unroll
+      for (int r = 0; r < DM; ++r) {
+        T acc_y = T(0);
+#pragma unroll
+        for (int c = 0; c <= r; ++c) acc_y += coef.L[r * DM + c] * w[c];
+        y[r] = acc_y;
+        S[r] = r < dim ? s_spot[r] * exp(coef.drift[r] * T_total + coef.sigma[r] * acc_y) : T(0);
+        B += s_w[r] * S[r];
+      }
+      const T pay = a.is_call ? (B - K) : (K - B);
+      const bool itm = pay > T(0);
+      q[0] = itm ? pay : T(0);
+      q[1] = q[0] * q[0];
+      const T sign = a.is_call ? T(1) : T(-1);
+#pragma unroll
+      for (int r = 0; r < DM; ++r) {
+        const T g = itm ? sign * s_w[r] * S[r] : T(0);
+        q[2 + r] = g;
+        q[2 + DM + r] = g * (y[r] - coef.sigma[r] * T_total);
+      }
+    }
+    // warp sums in the path dtype, then FP64 per warp (lane 0), fixed order
+#pragma unroll
+    for (int j = 0; j < 2 + 2 * DM; ++j) {
+      T v = q[j];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      if (lane == 0) acc[warp][j] += (double)v;
+    }
+  }
+  __syncthreads();
+  double* ws = static_cast<double*>(a.workspace);
+  const int width = 2 + 2 * dim;
+  for (int j = threadIdx.x; j < width; j += blockDim.x) {
+    const int src_j = j < 2 ? j : (j < 2 + dim ? j : j - dim + DM);  // compact [2 + 2*dim]
+    double s = 0.0;
+    for (int wi = 0; wi < kWarps; ++wi) s += acc[wi][src_j];
+    ws[(size_t)blockIdx.x * width + j] = s;
+  }
+}
+
+// FP64 Cholesky of an n x n SPD matrix (n <= 64) in one CTA: right-looking,
+// column by column in shared memory.  info = 0, or k + 1 if the k-th pivot is
+// not positive (the matrix is not positive definite).
+constexpr int kCholMax = 64;
+__global__ void __launch_bounds__(256) cholesky_f64_kernel(const double* __restrict__ A, int n,
+                                                          double* __restrict__ L, int* info) {
+  __shared__ double s[kCholMax * kCholMax];
+  __shared__ int bad;
+  for (int i = threadIdx.x; i < n * n; i += blockDim.x) s[i] = A[i];
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      const double d = s[k * n + k];
+      if (!(d > 0.0) && bad == 0) bad = k + 1;
+      s[k * n + k] = d > 0.0 ? sqrt(d) : 0.0;
+    }
+    __syncthreads();
+    const double piv = s[k * n + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) s[i * n + k] = piv > 0.0 ? s[i * n + k] / piv : 0.0;
+    __syncthreads();
+    const int m = n - k - 1;
+    for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+      const int i = k + 1 + t / m, j = k + 1 + t % m;
+      if (j <= i) s[i * n + j] -= s[i * n + k] * s[j * n + k];
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+    const int i = t / n, j = t % n;
+    L[t] = j <= i ? s[t] : 0.0;
+  }
+  if (threadIdx.x == 0) *info = bad;
+}
+
+template <typename T, int DM>
+int launch_paths(const tqf_mvgbm_args& a, cudaStream_t s) {
+  int occ = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mvgbm_paths_kernel<T, DM>, kBlock, 0);
+  if (occ < 1) occ = 1;
+  int64_t grid = (a.num_paths + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)num_sms() * occ;
+  if (grid > cap) grid = cap;
+  mvgbm_paths_kernel<T, DM><<<(unsigned)grid, kBlock, 0, s>>>(a);
+  return check_launch("mvgbm_paths_kernel");
+}
+
+template <typename T, int DM>
+int basket_grid(int64_t n) {
+  int occ = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, basket_price_kernel<T, DM>, kBlock, 0);
+  if (occ < 1) occ = 1;
+  int64_t grid = (n + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)num_sms() * occ;
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  return (int)grid;
+}
+
+template <typename T, int DM>
+int launch_basket(const tqf_basket_args& a, cudaStream_t s) {
+  const int grid = basket_grid<T, DM>(a.num_paths);
+  const int width = 2 + 2 * a.dim;
+  const size_t need = (size_t)grid * width * sizeof(double);
+  TQF_REQUIRE(a.workspace && a.workspace_bytes >= need, "tqf_basket_price: workspace %zu < required %zu",
+              a.workspace_bytes, need);
+  basket_price_kernel<T, DM><<<grid, kBlock, 0, s>>>(a);
+  int rc = check_launch("basket_price_kernel");
+  if (rc || a.out == nullptr) return rc;
+  return reduce_partials(static_cast<const double*>(a.workspace), grid, width, a.out, s);
+}
+
+template <typename T>
+int dispatch_paths(const tqf_mvgbm_args& a, cudaStream_t s) {
+  if (a.dim <= 1) return launch_paths<T, 1>(a, s);
+  if (a.dim <= 2) return launch_paths<T, 2>(a, s);
+  if (a.dim <= 4) return launch_paths<T, 4>(a, s);
+  if (a.dim <= 8) return launch_paths<T, 8>(a, s);
+  return launch_paths<T, 16>(a, s);
+}
+
+template <typename T>
+int dispatch_basket(const tqf_basket_args& a, cudaStream_t s) {
+  if (a.dim <= 4) return launch_basket<T, 4>(a, s);
+  if (a.dim <= 8) return launch_basket<T, 8>(a, s);
+  return launch_basket<T, 16>(a, s);
+}
+
+}  // namespace
+}  // namespace tqf
+
+using namespace tqf;
+
+extern "C" int tqf_cholesky_f64(const double* a, int32_t n, double* l, int32_t* info, void* stream) {
+  clear_error();
+  TQF_REQUIRE(a && l && info, "tqf_cholesky_f64: null pointer");
+  TQF_REQUIRE(n >= 1 && n <= kCholMax, "tqf_cholesky_f64: n must be in [1, %d], got %d", kCholMax, n);
+  cholesky_f64_kernel<<<1, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, n, l, info);
+  return check_launch("cholesky_f64_kernel");
+}
+
+extern "C" int tqf_mvgbm_paths(const tqf_mvgbm_args* a, void* stream) {
+  clear_error();
+  TQF_REQUIRE(a != nullptr, "tqf_mvgbm_paths: null args");
+  TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "tqf_mvgbm_paths: bad dtype");
+  TQF_REQUIRE(a->dim >= 1 && a->dim <= kMaxDim, "tqf_mvgbm_paths: dim must be in [1, 16], got %d", a->dim);
+  TQF_REQUIRE(a->num_paths >= 1 && a->num_steps >= 0, "tqf_mvgbm_paths: bad sizes");
+  TQF_REQUIRE(a->x0 && a->drift && a->vol && (a->num_steps == 0 || a->step_table),
+              "tqf_mvgbm_paths: null pointer");
+  TQF_REQUIRE(a->output.ptr && a->output.num_slots >= 1 && a->output.init_slot < a->output.num_slots,
+              "tqf_mvgbm_paths: output required");
+  TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.ptr || a->num_steps == 0,
+              "tqf_mvgbm_paths: memory draws need draws.ptr");
+  TQF_REQUIRE(!a->draws.antithetic || 2 * a->draws.antithetic_half == a->num_paths,
+              "tqf_mvgbm_paths: antithetic needs num_paths == 2 * antithetic_half");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a->dtype == TQF_F32 ? dispatch_paths<float>(*a, s) : dispatch_paths<double>(*a, s);
+}
+
+extern "C" int tqf_basket_price(const tqf_basket_args* a, void* stream) {
+  clear_error();
+  TQF_REQUIRE(a != nullptr, "tqf_basket_price: null args");
+  TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "tqf_basket_price: bad dtype");
+  TQF_REQUIRE(a->dim >= 1 && a->dim <= kMaxDim, "tqf_basket_price: dim must be in [1, 16], got %d", a->dim);
+  TQF_REQUIRE(a->num_paths >= 1 && a->num_steps >= 1, "tqf_basket_price: bad sizes");
+  TQF_REQUIRE(a->sqrt_dt && a->spot && a->drift && a->vol && a->weights, "tqf_basket_price: null pointer");
+  TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.ptr, "tqf_basket_price: memory draws need ptr");
+  TQF_REQUIRE(!a->draws.antithetic || 2 * a->draws.antithetic_half == a->num_paths,
+              "tqf_basket_price: antithetic needs num_paths == 2 * antithetic_half");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a->dtype == TQF_F32 ? dispatch_basket<float>(*a, s) : dispatch_basket<double>(*a, s);
+}
+
+extern "C" size_t tqf_basket_workspace_bytes(int32_t dtype, int32_t dim, int64_t num_paths) {
+  int grid;
+  if (dim <= 4) grid = dtype == TQF_F32 ? basket_grid<float, 4>(num_paths) : basket_grid<double, 4>(num_paths);
+  else if (dim <= 8) grid = dtype == TQF_F32 ? basket_grid<float, 8>(num_paths) : basket_grid<double, 8>(num_paths);
+  else grid = dtype == TQF_F32 ? basket_grid<float, 16>(num_paths) : basket_grid<double, 16>(num_paths);
+  return (size_t)grid * (2 + 2 * dim) * sizeof(double);
+}

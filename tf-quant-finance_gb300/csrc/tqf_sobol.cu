@@ -52,7 +52,8 @@ template <>
 struct SobolOut<TQF_SOBOL_F32_CENTERED> {
   using T = float;
   __device__ static T conv(uint32_t x, float sc, double) {
-    return (float)(((double)x + 0.5) * (double)sc);
+    // (x + 0.5) 2^-nd rounded to float32, kept below 1.0 (largest float < 1)
+    return fminf(__fmul_rn(__fadd_rn(__uint2float_rn(x), 0.5f), sc), 0.99999994039535522461f);
   }
 };
 

@@ -131,6 +131,70 @@ class HestonArgs(ctypes.Structure):
     ]
 
 
+class HestonAdjointArgs(ctypes.Structure):
+    _fields_ = [
+        ("dtype", c_i32),
+        ("num_steps", c_i32),
+        ("num_paths", c_i64),
+        ("step_table", c_vp),
+        ("x0", ctypes.c_double),
+        ("v0", ctypes.c_double),
+        ("xi", ctypes.c_double),
+        ("rho", ctypes.c_double),
+        ("draws", Draws),
+        ("num_strikes", c_i32),
+        ("pad0", c_i32),
+        ("strikes", c_vp),
+        ("is_call", c_vp),
+        ("weights", c_vp),
+        ("out", c_vp),
+        ("workspace", c_vp),
+        ("workspace_bytes", ctypes.c_size_t),
+        ("dev_status", c_vp),
+    ]
+
+
+class MvgbmArgs(ctypes.Structure):
+    _fields_ = [
+        ("dtype", c_i32),
+        ("dim", c_i32),
+        ("num_paths", c_i64),
+        ("num_steps", c_i32),
+        ("x0_per_path", c_i32),
+        ("step_table", c_vp),
+        ("x0", c_vp),
+        ("drift", c_vp),
+        ("vol", c_vp),
+        ("chol", c_vp),
+        ("draws", Draws),
+        ("output", PathOutput),
+        ("dev_status", c_vp),
+    ]
+
+
+class BasketArgs(ctypes.Structure):
+    _fields_ = [
+        ("dtype", c_i32),
+        ("dim", c_i32),
+        ("num_paths", c_i64),
+        ("num_steps", c_i32),
+        ("is_call", c_i32),
+        ("sqrt_dt", c_vp),
+        ("total_time", ctypes.c_double),
+        ("strike", ctypes.c_double),
+        ("spot", c_vp),
+        ("drift", c_vp),
+        ("vol", c_vp),
+        ("chol", c_vp),
+        ("weights", c_vp),
+        ("draws", Draws),
+        ("out", c_vp),
+        ("workspace", c_vp),
+        ("workspace_bytes", ctypes.c_size_t),
+        ("dev_status", c_vp),
+    ]
+
+
 # name -> (restype, argtypes)
 _SIGNATURES = {
     "tqf_abi_version": (ctypes.c_int, []),
@@ -149,6 +213,12 @@ _SIGNATURES = {
     "tqf_heston_workspace_bytes": (ctypes.c_size_t, [c_i32, c_i32, c_i64, c_i32]),
     "tqf_european_payoff_sums": (ctypes.c_int, [c_i32, c_vp, c_i64, c_i64, c_i32, ctypes.POINTER(Payoff), c_vp]),
     "tqf_european_workspace_bytes": (ctypes.c_size_t, [c_i64, c_i32]),
+    "tqf_heston_euler_adjoint": (ctypes.c_int, [ctypes.POINTER(HestonAdjointArgs), c_vp]),
+    "tqf_heston_adjoint_workspace_bytes": (ctypes.c_size_t, [c_i64]),
+    "tqf_cholesky_f64": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp, c_vp]),
+    "tqf_mvgbm_paths": (ctypes.c_int, [ctypes.POINTER(MvgbmArgs), c_vp]),
+    "tqf_basket_price": (ctypes.c_int, [ctypes.POINTER(BasketArgs), c_vp]),
+    "tqf_basket_workspace_bytes": (ctypes.c_size_t, [c_i32, c_i32, c_i64]),
     "tqf_fma_peak_probe": (ctypes.c_int, [c_i32, c_i32, c_vp, ctypes.POINTER(ctypes.c_double), c_vp]),
 }
 

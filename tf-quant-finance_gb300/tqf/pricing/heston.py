@@ -85,4 +85,88 @@ def heston_european_mc(*, strikes, expiry, spot, variance, mean_reversion, theta
     return stats_from_sums(out, N, float(np.exp(-r * T)))
 
 
-__all__ = ["heston_european_mc"]
+def heston_european_vjp(grad_prices, *, strikes, expiry, spot, variance, mean_reversion, theta, volvol, rho,
+                        discount_rate=0.0, is_call_options=None, num_samples, num_time_steps,
+                        random_type=RandomType.STATELESS, seed=(1, 2), dtype=torch.float32, path_offset=0,
+                        normal_draws=None, prices=None):
+    """Vector-Jacobian product of the full-truncation European prices with
+    respect to (spot, variance, mean_reversion, theta, volvol, rho,
+    discount_rate), by the replaying pathwise adjoint kernel
+    (``tqf_heston_euler_adjoint``).  ``prices`` (the forward result, FP64)
+    supplies the discounting term of the rate sensitivity."""
+    device = _lib.require_cuda()
+    td = utils.torch_dtype(dtype)
+    np_dt = utils.np_dtype(td)
+    T, r, steps, N = float(expiry), float(discount_rate), int(num_time_steps), int(num_samples)
+    all_times = np.linspace(0.0, T, steps + 1).astype(np_dt)
+    dt = (all_times[1:] - all_times[:-1]).astype(np_dt)
+    sqrt_dt = np.sqrt(dt).astype(np_dt)
+    params = (float(mean_reversion), float(theta), float(volvol), float(rho))
+    h = HestonFullTruncation(r, *params)
+    key = ("ft", np_dt.str, T, steps, params, r, device.index)
+    no_slots = np.full(steps, -1, dtype=np.int32)
+    tab = _table(key, lambda: heston_model.full_truncation_table(h, all_times, dt, sqrt_dt, no_slots, steps),
+                 td, device)
+    g = torch.as_tensor(grad_prices, dtype=torch.float64).to(device).reshape(-1)
+    disc = float(np.exp(-r * T))
+    k = torch.as_tensor(utils.to_numpy(strikes, np.float64).reshape(-1), dtype=td).to(device)
+    ns = int(k.numel())
+    w = (g * (disc / N)).to(td).contiguous()
+    calls = None
+    if is_call_options is not None:
+        calls = torch.as_tensor(np.broadcast_to(np.asarray(is_call_options, np.uint8), (ns,)).copy()).to(device)
+    if normal_draws is not None:
+        draws = mvn.memory_draws(normal_draws, path_axis=0, step_axis=1)
+    else:
+        draws = mvn.philox_draws(random_type, seed, N, path_offset)
+    out = torch.zeros(7, dtype=torch.float64, device=device)
+    from tqf.pricing.european import workspace
+    ws = workspace(int(_lib.load().tqf_heston_adjoint_workspace_bytes(N)), device, "heston_adjoint")
+    a = _lib.HestonAdjointArgs()
+    a.dtype = _lib.dtype_code(td)
+    a.num_steps = steps
+    a.num_paths = N
+    a.step_table = tab.data_ptr()
+    a.x0, a.v0 = float(np.log(spot)), float(variance)
+    a.xi, a.rho = float(volvol), float(rho)
+    a.draws = draws
+    a.num_strikes = ns
+    a.strikes = k.data_ptr()
+    a.is_call = calls.data_ptr() if calls is not None else None
+    a.weights = w.data_ptr()
+    a.out = out.data_ptr()
+    a.workspace = ws.data_ptr()
+    a.workspace_bytes = ws.numel()
+    a.dev_status = _lib.status_buffer(device).data_ptr()
+    _lib.call("tqf_heston_euler_adjoint", a, _lib.stream_ptr(device))
+    grad = out.clone()
+    grad[0] = out[0] / float(spot)  # d/dS0 = (1/S0) d/dlog S0
+    if prices is not None:
+        grad[6] = out[6] - T * float((g * prices.to(device)).sum())
+    return grad
+
+
+class HestonEuropeanPrice(torch.autograd.Function):
+    """prices[n_strikes] = HestonEuropeanPrice.apply(params[7], kwargs) with
+    params = (spot, variance, mean_reversion, theta, volvol, rho, rate);
+    full-truncation Euler, Philox draws; backward replays the paths."""
+
+    @staticmethod
+    def forward(ctx, params, kw):
+        p = [float(v) for v in params.detach().cpu()]
+        names = ("spot", "variance", "mean_reversion", "theta", "volvol", "rho", "discount_rate")
+        args = dict(zip(names, p))
+        res = heston_european_mc(**kw, **args, scheme="full_truncation")
+        ctx.kw = kw
+        ctx.args = args
+        ctx.save_for_backward(res.price)
+        return res.price.to(params.device)
+
+    @staticmethod
+    def backward(ctx, g):
+        (prices,) = ctx.saved_tensors
+        grad = heston_european_vjp(g, prices=prices, **ctx.kw, **ctx.args)
+        return grad.to(g.device), None
+
+
+__all__ = ["heston_european_mc", "heston_european_vjp", "HestonEuropeanPrice"]
