@@ -232,9 +232,9 @@ TQF_API int tqf_euler_update(const tqf_euler_update_args* args, void* stream);
 /* Full-truncation Euler for the Heston model in log-spot form, as the
  * reference Euler sampler runs it with drift [r - v+/2, kappa (theta - v+)]
  * and volatility [[sqrt v+, 0], [xi rho sqrt v+, xi sqrt(1-rho^2) sqrt v+]],
- * v+ = max(v, 0), coefficients evaluated at t_{i+1}.  step_table is
- * [num_steps][8] = (dt, sqrt_dt, r, kappa, theta, xi*rho,
- * xi*sqrt(1-rho^2), slot).  Component 0 of the draws drives the log-spot.
+ * v+ = max(v, 0), coefficients evaluated at t_{i+1}.  step_table (16-byte
+ * aligned) is [num_steps][8] = (dt/2, sqrt_dt, r*dt, kappa*dt,
+ * kappa*theta*dt, xi*rho, xi*sqrt(1-rho^2), slot).  Component 0 of the draws drives the log-spot.
  * Optional path store and fused European payoff (S = spot_scale*exp(x_T)). */
 typedef struct tqf_heston_args {
   int32_t dtype;
@@ -267,7 +267,7 @@ TQF_API int tqf_heston_qe(const tqf_heston_args* args, void* stream);
  * respect to (log S0, v0, kappa, theta, xi, rho, r) and writes
  * out[7] (device, FP64) = sum_paths c_p S_T,p dx_T,p/dparam with
  * c_p = sum_j weights_j dPayoff_j/dS_T.  step_table as tqf_heston_euler
- * with constant parameters; xi and rho passed explicitly. */
+ * with constant parameters, also passed explicitly (kappa, theta, xi, rho). */
 typedef struct tqf_heston_adjoint_args {
   int32_t dtype;
   int32_t num_steps;
@@ -275,6 +275,8 @@ typedef struct tqf_heston_adjoint_args {
   const void* step_table;
   double x0;
   double v0;
+  double kappa;
+  double theta;
   double xi;
   double rho;
   tqf_draws draws;

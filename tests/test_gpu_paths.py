@@ -100,7 +100,7 @@ def test_heston_full_truncation_euler_matches_oracle(cuda, dtype):
     from tqf.models import coefficients, euler_sampling
     np_dt = np.float32 if dtype == torch.float32 else np.float64
     N, steps = 4096, 60
-    r, kappa, theta, xi, rho = 0.02, 2.0, 0.04, 0.5, -0.7   # Feller violated: v hits the truncation
+    r, kappa, theta, xi, rho = 0.02, 2.0, 0.04, 0.4, -0.7   # Feller violated: v hits the truncation
     drift, vol = coefficients.heston_full_truncation(r, kappa, theta, xi, rho)
     draws = np.random.default_rng(1).standard_normal((N, steps, 2)).astype(np_dt)
     times = np.array([0.3, 1.0], dtype=np_dt)
@@ -109,17 +109,19 @@ def test_heston_full_truncation_euler_matches_oracle(cuda, dtype):
     all_t, keep, _ = ogrids.prepare_grid(times, times[-1] / np_dt(steps), np_dt, num_time_steps=steps)
     fd, fv = oeuler.heston_ft_coefficients(r, kappa, theta, xi, rho, np_dt)
     min_abs_v = np.full(N, np.inf)
+    min_v = np.full(N, np.inf)
 
     def fd_monitor(t, x):
         np.minimum(min_abs_v, np.abs(x[..., 1]), out=min_abs_v)
+        np.minimum(min_v, x[..., 1], out=min_v)
         return fd(t, x)
 
     want = oeuler.sample_with_draws(fd_monitor, fv, all_t, keep, 2, np.broadcast_to(x0, (N, 2)),
                                     draws.transpose(1, 0, 2), np_dt)
-    kink = 1e-5 if dtype == torch.float32 else 1e-13
+    kink = 1e-4 if dtype == torch.float32 else 1e-12
     ok = min_abs_v > kink
-    assert ok.mean() > 0.9
-    assert (~ok).sum() > 0 or xi < 0.3  # the truncation is exercised
+    assert ok.mean() > 0.85
+    assert (min_v < 0).sum() > 0  # the truncation is exercised
     rtol = 1e-5 if dtype == torch.float32 else 1e-12
     g = got.cpu().numpy()
     _close(g[ok][..., 0], want[ok][..., 0], rtol, 1.0)

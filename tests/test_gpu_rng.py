@@ -139,11 +139,13 @@ def test_philox_normal_draws_match_oracle(cuda, dtype, antithetic):
                                 antithetic=antithetic)
     if dtype == torch.float32:
         # Device float32 Box–Muller uses the SFU lg2 (absolute error ~2^-22),
-        # so |dz| <= 4e-6 + 2.5e-7 / r with r the Box–Muller radius of the pair.
-        flat = want.transpose(1, 0, 2).reshape(N, -1)
-        pairs = flat.reshape(N, -1, 2)
-        rad = np.sqrt((pairs ** 2).sum(-1))
-        rad = np.repeat(rad, 2, axis=1).reshape(N, steps, d).transpose(1, 0, 2)
+        # so |dz| <= 4e-6 (1 + |z|) + 2.5e-7 / r with r the radius of the pair.
+        K = steps * d
+        kpad = (K + 3) // 4 * 4
+        half = N // 2 if antithetic else None
+        full = ophilox.normals(np.arange(N), kpad, 5, 6, antithetic_half=half)
+        rad = np.sqrt((full.reshape(N, kpad // 2, 2) ** 2).sum(-1))
+        rad = np.repeat(rad, 2, axis=1)[:, :K].reshape(N, steps, d).transpose(1, 0, 2)
         bound = 4e-6 * (1 + np.abs(want)) + 2.5e-7 / rad
         assert np.all(np.abs(got - want) <= bound)
     else:

@@ -46,18 +46,46 @@ SmemLayout smem_layout(int steps, int cols, int ns, bool staged) {
 }
 
 // ---- one step of each scheme ---------------------------------------------
+// Full-truncation Euler in the Euler sampler's form with pre-scaled step
+// constants: row = (dt/2, sqrt dt, r dt, kappa dt, kappa theta dt, xi rho,
+// xi sqrt(1 - rho^2), slot):
+//   x' = x + (r dt - dt/2 v+) + sqrt(v+) dw0
+//   v' = v + (kappa theta dt - kappa dt v+) + sqrt(v+) (xi rho dw0 + xi sqrt(1-rho^2) dw1)
 template <typename T>
-__device__ __forceinline__ void ft_step(const T* __restrict__ row, T z0, T z1, T& x, T& v) {
-  const T dt = row[0], sdt = row[1], r = row[2], kappa = row[3], theta = row[4];
-  const T xirho = row[5], xisq = row[6];
+struct FtRow {
+  T hdt, sdt, rdt, kdt, kthdt, xirho, xisq, slot;
+};
+
+template <typename T>
+__device__ __forceinline__ FtRow<T> load_ft_row(const T* __restrict__ row) {
+  FtRow<T> r;
+  if constexpr (sizeof(T) == 4) {
+    const float4 a = reinterpret_cast<const float4*>(row)[0];
+    const float4 b = reinterpret_cast<const float4*>(row)[1];
+    r.hdt = a.x; r.sdt = a.y; r.rdt = a.z; r.kdt = a.w;
+    r.kthdt = b.x; r.xirho = b.y; r.xisq = b.z; r.slot = b.w;
+  } else {
+    r.hdt = row[0]; r.sdt = row[1]; r.rdt = row[2]; r.kdt = row[3];
+    r.kthdt = row[4]; r.xirho = row[5]; r.xisq = row[6]; r.slot = row[7];
+  }
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ void ft_step(const FtRow<T>& c, T z0, T z1, T& x, T& v) {
   const T vp = v > T(0) ? v : T(0);
-  const T sq = sqrt(vp);
-  const T dw0 = z0 * sdt;
-  const T dw1 = z1 * sdt;
-  const T x_next = x + dt * (r - T(0.5) * vp) + sq * dw0;
-  const T v_next = v + dt * (kappa * (theta - vp)) + ((xirho * sq) * dw0 + (xisq * sq) * dw1);
+  const T sq = sqrt_approx(vp);
+  const T dw0 = z0 * c.sdt;
+  const T dw1 = z1 * c.sdt;
+  const T x_next = x + fma(-c.hdt, vp, c.rdt) + sq * dw0;
+  const T v_next = v + fma(-c.kdt, vp, c.kthdt) + sq * fma(c.xisq, dw1, c.xirho * dw0);
   x = x_next;
   v = v_next;
+}
+
+template <typename T>
+__device__ __forceinline__ void ft_step(const T* __restrict__ row, T z0, T z1, T& x, T& v) {
+  ft_step<T>(load_ft_row<T>(row), z0, z1, x, v);
 }
 
 template <typename T>
@@ -113,8 +141,9 @@ __device__ __forceinline__ void store_state(const tqf_path_output& o, int64_t pa
   reinterpret_cast<V2*>(o.ptr)[path * o.num_slots + slot] = w;
 }
 
-// SCHEME 0 = full-truncation Euler, 1 = QE.  SRC = TQF_DRAWS_* (compile-time).
-template <typename T, int SCHEME, int SRC, bool STORE, bool PRICE>
+// SCHEME 0 = full-truncation Euler, 1 = QE.  SRC = TQF_DRAWS_* (compile-time);
+// ANTI: antithetic Philox pairing.
+template <typename T, int SCHEME, int SRC, bool STORE, bool PRICE, bool ANTI>
 __global__ void __launch_bounds__(kBlock)
     heston_kernel(tqf_heston_args a, int staged, SmemLayout L) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -158,40 +187,49 @@ __global__ void __launch_bounds__(kBlock)
         // Canonical stream, 2 normals per step: block b = steps 2b, 2b+1.
         int64_t p = path;
         float sign = 1.f;
-        if (a.draws.antithetic && p >= a.draws.antithetic_half) {
+        if (ANTI && p >= a.draws.antithetic_half) {
           p -= a.draws.antithetic_half;
           sign = -1.f;
         }
         p += a.draws.path_offset;
-        int i = 0;
-        for (; i + 1 < steps; i += 2) {
-          float z[4];
-          philox_normals4_f32(i >> 1, p, a.draws.key0, a.draws.key1, z);
+        const uint32_t k0 = a.draws.key0, k1 = a.draws.key1;
+        const uint32_t plo = (uint32_t)p, phi = (uint32_t)((uint64_t)p >> 32);
+        auto one_step = [&](int i, float za, float zb) {
           const T* r0 = table + (size_t)i * COLS;
-          if (SCHEME == 0) ft_step<T>(r0, (T)(sign * z[0]), (T)(sign * z[1]), x, v);
-          else qe_step<T>(r0, (T)(sign * z[0]), (T)(sign * z[1]), x, v);
-          if (STORE) {
-            const int slot = (int)r0[COLS - 1];
-            if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+          if (ANTI) {
+            za *= sign;
+            zb *= sign;
           }
-          const T* r1 = r0 + COLS;
-          if (SCHEME == 0) ft_step<T>(r1, (T)(sign * z[2]), (T)(sign * z[3]), x, v);
-          else qe_step<T>(r1, (T)(sign * z[2]), (T)(sign * z[3]), x, v);
-          if (STORE) {
-            const int slot = (int)r1[COLS - 1];
-            if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+          if constexpr (SCHEME == 0) {
+            const FtRow<T> row = load_ft_row<T>(r0);
+            ft_step<T>(row, (T)za, (T)zb, x, v);
+            if (STORE) {
+              const int slot = (int)row.slot;
+              if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+            }
+          } else {
+            qe_step<T>(r0, (T)za, (T)zb, x, v);
+            if (STORE) {
+              const int slot = (int)r0[COLS - 1];
+              if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+            }
           }
+        };
+        int i = 0;
+#pragma unroll 2
+        for (; i + 1 < steps; i += 2) {
+          const uint4 r = philox4x32_10(make_uint4((uint32_t)(i >> 1), plo, phi, 0u), k0, k1);
+          float z0, z1, z2, z3;
+          box_muller_f32(r.x, r.y, z0, z1);
+          box_muller_f32(r.z, r.w, z2, z3);
+          one_step(i, z0, z1);
+          one_step(i + 1, z2, z3);
         }
         if (i < steps) {
-          float z[4];
-          philox_normals4_f32(i >> 1, p, a.draws.key0, a.draws.key1, z);
-          const T* r0 = table + (size_t)i * COLS;
-          if (SCHEME == 0) ft_step<T>(r0, (T)(sign * z[0]), (T)(sign * z[1]), x, v);
-          else qe_step<T>(r0, (T)(sign * z[0]), (T)(sign * z[1]), x, v);
-          if (STORE) {
-            const int slot = (int)r0[COLS - 1];
-            if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
-          }
+          const uint4 r = philox4x32_10(make_uint4((uint32_t)(i >> 1), plo, phi, 0u), k0, k1);
+          float z0, z1;
+          box_muller_f32(r.x, r.y, z0, z1);
+          one_step(i, z0, z1);
         }
       } else {
         DrawSource<T> src(a.draws, path, 2);
@@ -289,8 +327,9 @@ __global__ void __launch_bounds__(kBlock) heston_adjoint_kernel(tqf_heston_adjoi
       }
       DrawSource<T> src(a.draws, path, 2);
       for (int i = 0; i < a.num_steps; ++i) {
-        const T* row = table + (size_t)i * kFtCols;
-        const T dt = row[0], sdt = row[1], kappa = row[3], theta = row[4], A = row[5], B = row[6];
+        const FtRow<T> row = load_ft_row<T>(table + (size_t)i * kFtCols);
+        const T dt = T(2) * row.hdt, sdt = row.sdt, kappa = (T)a.kappa;
+        const T theta = (T)a.theta, A = row.xirho, B = row.xisq;
         const T z0 = src.get(i, 0), z1 = src.get(i, 1);
         const T vp = v > T(0) ? v : T(0);
         const T sq = sqrt(vp);
@@ -363,27 +402,28 @@ int run_adjoint(const tqf_heston_adjoint_args& a, cudaStream_t s) {
 template <typename T, int SCHEME>
 using KernelFn = void (*)(tqf_heston_args, int, SmemLayout);
 
-template <typename T, int SCHEME, int SRC>
+template <typename T, int SCHEME, int SRC, bool ANTI>
 KernelFn<T, SCHEME> pick(bool store, bool price) {
-  if (store && price) return heston_kernel<T, SCHEME, SRC, true, true>;
-  if (store) return heston_kernel<T, SCHEME, SRC, true, false>;
-  if (price) return heston_kernel<T, SCHEME, SRC, false, true>;
-  return heston_kernel<T, SCHEME, SRC, false, false>;
+  if (store && price) return heston_kernel<T, SCHEME, SRC, true, true, ANTI>;
+  if (store) return heston_kernel<T, SCHEME, SRC, true, false, ANTI>;
+  if (price) return heston_kernel<T, SCHEME, SRC, false, true, ANTI>;
+  return heston_kernel<T, SCHEME, SRC, false, false, ANTI>;
 }
 
 template <typename T, int SCHEME>
-KernelFn<T, SCHEME> pick_kernel(int src, bool store, bool price) {
-  return src == TQF_DRAWS_PHILOX ? pick<T, SCHEME, TQF_DRAWS_PHILOX>(store, price)
-                                 : pick<T, SCHEME, TQF_DRAWS_MEMORY>(store, price);
+KernelFn<T, SCHEME> pick_kernel(int src, bool store, bool price, bool anti = false) {
+  if (src != TQF_DRAWS_PHILOX) return pick<T, SCHEME, TQF_DRAWS_MEMORY, false>(store, price);
+  return anti ? pick<T, SCHEME, TQF_DRAWS_PHILOX, true>(store, price)
+              : pick<T, SCHEME, TQF_DRAWS_PHILOX, false>(store, price);
 }
 
 template <typename T, int SCHEME>
 int grid_for(int64_t N, int ns, int steps, bool staged, int src, bool store, bool price,
-             SmemLayout* out_layout) {
+             SmemLayout* out_layout, bool anti = false) {
   const int cols = SCHEME == 0 ? kFtCols : kQeCols;
   SmemLayout L = smem_layout<T>(steps, cols, price ? ns : 0, staged);
   if (out_layout) *out_layout = L;
-  auto k = pick_kernel<T, SCHEME>(src, store, price);
+  auto k = pick_kernel<T, SCHEME>(src, store, price, anti);
   if (L.total > 48 * 1024)
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
   int occ = 0;
@@ -410,13 +450,13 @@ int run(const tqf_heston_args& a, cudaStream_t s) {
   const bool staged = table_staged(a.step_table, a.num_steps, cols, sizeof(T));
   SmemLayout L;
   const int grid = grid_for<T, SCHEME>(a.num_paths, a.payoff.num_strikes, a.num_steps, staged,
-                                       a.draws.source, store, price, &L);
+                                       a.draws.source, store, price, &L, a.draws.antithetic != 0);
   if (price) {
     const size_t need = (size_t)grid * a.payoff.num_strikes * 2 * sizeof(double);
     TQF_REQUIRE(a.payoff.workspace && a.payoff.workspace_bytes >= need,
                 "heston: payoff workspace %zu bytes < required %zu", a.payoff.workspace_bytes, need);
   }
-  auto k = pick_kernel<T, SCHEME>(a.draws.source, store, price);
+  auto k = pick_kernel<T, SCHEME>(a.draws.source, store, price, a.draws.antithetic != 0);
   k<<<grid, kBlock, L.total, s>>>(a, staged ? 1 : 0, L);
   int rc = check_launch(SCHEME == 0 ? "heston_kernel<FT>" : "heston_kernel<QE>");
   if (rc || !price || a.payoff.out == nullptr) return rc;
@@ -430,6 +470,7 @@ int validate(const tqf_heston_args* a, const char* who) {
   TQF_REQUIRE(a->num_paths >= 1, "%s: num_paths must be >= 1", who);
   TQF_REQUIRE(a->num_steps >= 0, "%s: num_steps must be >= 0", who);
   TQF_REQUIRE(a->num_steps == 0 || a->step_table != nullptr, "%s: null step_table", who);
+  TQF_REQUIRE((reinterpret_cast<uintptr_t>(a->step_table) & 15u) == 0, "%s: step_table must be 16-byte aligned", who);
   TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.source == TQF_DRAWS_MEMORY,
               "%s: bad draws.source %d", who, a->draws.source);
   TQF_REQUIRE(a->draws.source != TQF_DRAWS_MEMORY || a->num_steps == 0 || a->draws.ptr != nullptr,

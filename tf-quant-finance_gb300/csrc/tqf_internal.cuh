@@ -38,8 +38,9 @@ constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
 __host__ __device__ __forceinline__ void mulhilo32(uint32_t a, uint32_t b,
                                                    uint32_t& hi, uint32_t& lo) {
 #ifdef __CUDA_ARCH__
-  lo = a * b;
-  hi = __umulhi(a, b);
+  const uint64_t p = (uint64_t)a * (uint64_t)b;  // one 32x32->64 wide multiply
+  lo = (uint32_t)p;
+  hi = (uint32_t)(p >> 32);
 #else
   uint64_t p = (uint64_t)a * (uint64_t)b;
   lo = (uint32_t)p;
@@ -81,6 +82,14 @@ __device__ __forceinline__ float u01_co_f32(uint32_t r) {
   return __uint_as_float(0x3f800000u | (r >> 9)) - 1.0f;
 }
 
+// Single-instruction SFU square root (relative error ~2^-23; no IEEE rounding).
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ double sqrt_approx(double x) { return sqrt(x); }
+
 // Two N(0,1) from two 32-bit words (radius from a, angle from b).  Uses the
 // SFU approximations (lg2, sqrt, sin, cos); the angle is taken in [-pi, pi)
 // where the hardware sin/cos are accurate.
@@ -88,7 +97,7 @@ __device__ __forceinline__ void box_muller_f32(uint32_t a, uint32_t b, float& z0
                                                float& z1) {
   const float u1 = u01_oc_f32(a);
   const float u2 = u01_co_f32(b);
-  const float rad = __fsqrt_rn(__fmul_rn(-1.3862943611198906f, __log2f(u1)));  // -2 ln u1
+  const float rad = sqrt_approx(__fmul_rn(-1.3862943611198906f, __log2f(u1)));  // sqrt(-2 ln u1)
   const float ang = __fmul_rn(__fsub_rn(u2, 0.5f), 6.283185307179586f);
   float s, c;
   __sincosf(ang, &s, &c);

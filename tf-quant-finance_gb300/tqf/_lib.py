@@ -139,6 +139,8 @@ class HestonAdjointArgs(ctypes.Structure):
         ("step_table", c_vp),
         ("x0", ctypes.c_double),
         ("v0", ctypes.c_double),
+        ("kappa", ctypes.c_double),
+        ("theta", ctypes.c_double),
         ("xi", ctypes.c_double),
         ("rho", ctypes.c_double),
         ("draws", Draws),

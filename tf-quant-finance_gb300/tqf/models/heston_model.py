@@ -218,13 +218,15 @@ class HestonModel(GenericItoProcess):
 
 
 def full_truncation_table(heston, all_times, dt, sqrt_dt, step_slot, steps_exec):
-    """[steps, 8] rows (dt, sqrt dt, r, kappa, theta, xi rho, xi sqrt(1-rho^2),
-    slot) with parameters at t_{i+1} (euler_sampling.py:519)."""
+    """[steps, 8] rows (dt/2, sqrt dt, r dt, kappa dt, kappa theta dt, xi rho,
+    xi sqrt(1-rho^2), slot) with parameters at t_{i+1} (euler_sampling.py:519)."""
     r, k, th, xirho, xisq = heston.params_at(np.asarray(all_times[1:steps_exec + 1], dtype=np.float64))
+    h = np.asarray(dt[:steps_exec], dtype=np.float64)
     rows = np.zeros((steps_exec, FT_COLS), dtype=np.float64)
-    rows[:, 0] = dt[:steps_exec]
+    rows[:, 0] = 0.5 * h
     rows[:, 1] = sqrt_dt[:steps_exec]
-    rows[:, 2], rows[:, 3], rows[:, 4], rows[:, 5], rows[:, 6] = r, k, th, xirho, xisq
+    rows[:, 2], rows[:, 3], rows[:, 4] = r * h, k * h, k * th * h
+    rows[:, 5], rows[:, 6] = xirho, xisq
     rows[:, 7] = step_slot
     return rows
 

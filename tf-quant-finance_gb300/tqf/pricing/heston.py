@@ -128,6 +128,7 @@ def heston_european_vjp(grad_prices, *, strikes, expiry, spot, variance, mean_re
     a.num_paths = N
     a.step_table = tab.data_ptr()
     a.x0, a.v0 = float(np.log(spot)), float(variance)
+    a.kappa, a.theta = float(mean_reversion), float(theta)
     a.xi, a.rho = float(volvol), float(rho)
     a.draws = draws
     a.num_strikes = ns
