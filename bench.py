@@ -218,8 +218,10 @@ def run_gpu(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     n_paths, n_steps = args.paths, args.time_steps
     k = strikes()
+    from tqf.pricing.sharding import weak_shard
+    offset, _ = weak_shard(n_paths, rank)
     kw = dict(strikes=k, num_samples=n_paths, num_time_steps=n_steps, scheme="full_truncation",
-              random_type=RandomType.STATELESS, seed=[20240, 7], path_offset=rank * n_paths, **PARAMS)
+              random_type=RandomType.STATELESS, seed=[20240, 7], path_offset=offset, **PARAMS)
 
     # Device-resident pieces for the kernel-only timing: everything a step needs
     # is built once; a timed step is the fused kernel + partial-sum reduction.
@@ -244,7 +246,7 @@ def run_gpu(args, rank, world, local_rank):
     hargs.num_paths = n_paths
     hargs.step_table = table.data_ptr()
     hargs.x0, hargs.v0 = math.log(p["spot"]), p["variance"]
-    hargs.draws = mvn.philox_draws(RandomType.STATELESS, [20240, 7], n_paths, rank * n_paths)
+    hargs.draws = mvn.philox_draws(RandomType.STATELESS, [20240, 7], n_paths, offset)
     hargs.payoff = pay
     hargs.dev_status = L.status_buffer(dev).data_ptr()
     stream = torch.cuda.current_stream()
@@ -324,7 +326,8 @@ def run_gpu(args, rank, world, local_rank):
         t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-        dist.all_reduce(out, op=dist.ReduceOp.SUM)
+        from tqf.pricing.sharding import allreduce_sums
+        allreduce_sums(out)  # the one exchange step: FP64 payoff sums
 
     peaks, peak_kind = measured_peaks()
     fp32_peak = fma_peak(torch, L)

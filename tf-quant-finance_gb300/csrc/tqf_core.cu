@@ -55,21 +55,34 @@ int num_sms() {
   return n;
 }
 
-// out[w] = sum_b partials[b * width + w], b ascending (deterministic).
-__global__ void reduce_partials_kernel(const double* __restrict__ partials, int num_partials,
-                                       int width, double* __restrict__ out) {
-  const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= width) return;
-  double s = 0.0;
-  for (int b = 0; b < num_partials; ++b) s += partials[(size_t)b * width + w];
-  out[w] = s;
+// out[w] = sum_b partials[b * width + w] in a fixed order: a CTA owns 32
+// consecutive columns; its 32 row-lanes sum rows r, r + 32, ... (coalesced
+// 256-byte row segments), then the row-lanes are folded by a fixed tree.
+constexpr int kRedCols = 32;
+constexpr int kRedRows = 32;
+__global__ void __launch_bounds__(kRedCols * kRedRows)
+    reduce_partials_kernel(const double* __restrict__ partials, int num_partials, int width,
+                           double* __restrict__ out) {
+  __shared__ double s[kRedRows][kRedCols + 1];
+  const int c = threadIdx.x % kRedCols;
+  const int r = threadIdx.x / kRedCols;
+  const int w = blockIdx.x * kRedCols + c;
+  double acc = 0.0;
+  if (w < width)
+    for (int b = r; b < num_partials; b += kRedRows) acc += partials[(size_t)b * width + w];
+  s[r][c] = acc;
+  __syncthreads();
+  for (int stride = kRedRows / 2; stride > 0; stride >>= 1) {
+    if (r < stride) s[r][c] += s[r + stride][c];
+    __syncthreads();
+  }
+  if (r == 0 && w < width) out[w] = s[0][c];
 }
 
 int reduce_partials(const double* partials, int num_partials, int width, double* out,
                     cudaStream_t stream) {
-  const int threads = 128;
-  const int blocks = (width + threads - 1) / threads;
-  reduce_partials_kernel<<<blocks, threads, 0, stream>>>(partials, num_partials, width, out);
+  const int blocks = (width + kRedCols - 1) / kRedCols;
+  reduce_partials_kernel<<<blocks, kRedCols * kRedRows, 0, stream>>>(partials, num_partials, width, out);
   return check_launch("reduce_partials_kernel");
 }
 
