@@ -10,6 +10,8 @@
 // states and a fused European payoff over up to 1024 strikes with FP64
 // cross-path accumulation in a fixed order (deterministic).  The CTA loop is
 // persistent: grid = SMs x resident CTAs, each CTA walks path tiles.
+#include <mutex>
+
 #include "tqf_internal.cuh"
 
 namespace tqf {
@@ -487,6 +489,58 @@ int validate(const tqf_heston_args* a, const char* who) {
   return TQF_OK;
 }
 
+// ---- allocation-free pricing variant ------------------------------------------
+// For callers that cannot call cudaMalloc (see tqf_heston_euler_price_noalloc
+// in tqf.h): the per-CTA partial sums live in this file-scope device array
+// instead of a caller workspace.  2 MiB = 2048 CTAs x 64 strikes x (sum, sum
+// of squares); every GPU that loads the library holds it until exit.
+constexpr int kNoAllocMaxStrikes = 64;
+constexpr size_t kNoAllocDoubles = (size_t)2048 * kNoAllocMaxStrikes * 2;
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocDoubles];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+
+// Device address of g_noalloc_partials on the current device, looked up once
+// per device (the host-side symbol is only a stand-in, never a device pointer).
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  int rc = check_cuda(cudaGetDevice(&dev), "tqf_heston_euler_price_noalloc: cudaGetDevice");
+  if (rc) return rc;
+  TQF_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "tqf_heston_euler_price_noalloc: device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    rc = check_cuda(cudaGetSymbolAddress(&p, g_noalloc_partials),
+                    "tqf_heston_euler_price_noalloc: cudaGetSymbolAddress");
+    if (rc) return rc;
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return TQF_OK;
+}
+
+template <typename T>
+int run_noalloc(const tqf_heston_args& a, double* scratch, cudaStream_t s) {
+  const bool store = a.output.ptr != nullptr;
+  const bool staged = table_staged(a.step_table, a.num_steps, kFtCols, sizeof(T));
+  SmemLayout L;
+  int grid = grid_for<T, 0>(a.num_paths, a.payoff.num_strikes, a.num_steps, staged, a.draws.source, store,
+                            true, &L, a.draws.antithetic != 0);
+  // The CTA loop is persistent, so a smaller grid still covers every path.
+  const int cap = (int)(kNoAllocDoubles / (2 * (size_t)a.payoff.num_strikes));
+  if (grid > cap) grid = cap;
+  tqf_heston_args b = a;
+  b.payoff.workspace = scratch;
+  b.payoff.workspace_bytes = kNoAllocDoubles * sizeof(double);
+  auto k = pick_kernel<T, 0>(b.draws.source, store, true, b.draws.antithetic != 0);
+  k<<<grid, kBlock, L.total, s>>>(b, staged ? 1 : 0, L);
+  int rc = check_launch("heston_kernel<FT> (no-alloc)");
+  if (rc) return rc;
+  return reduce_partials(scratch, grid, 2 * b.payoff.num_strikes, b.payoff.out, s);
+}
+
 }  // namespace
 }  // namespace tqf
 
@@ -498,6 +552,21 @@ extern "C" int tqf_heston_euler(const tqf_heston_args* a, void* stream) {
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   return a->dtype == TQF_F32 ? run<float, 0>(*a, s) : run<double, 0>(*a, s);
+}
+
+extern "C" int tqf_heston_euler_price_noalloc(const tqf_heston_args* a, void* stream) {
+  clear_error();
+  int rc = validate(a, "tqf_heston_euler_price_noalloc");
+  if (rc) return rc;
+  TQF_REQUIRE(a->payoff.num_strikes >= 1 && a->payoff.num_strikes <= kNoAllocMaxStrikes,
+              "tqf_heston_euler_price_noalloc: num_strikes must be in [1, %d], got %d", kNoAllocMaxStrikes,
+              a->payoff.num_strikes);
+  TQF_REQUIRE(a->payoff.out != nullptr, "tqf_heston_euler_price_noalloc: payoff.out is required");
+  double* scratch = nullptr;
+  rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a->dtype == TQF_F32 ? run_noalloc<float>(*a, scratch, s) : run_noalloc<double>(*a, scratch, s);
 }
 
 extern "C" int tqf_heston_qe(const tqf_heston_args* a, void* stream) {

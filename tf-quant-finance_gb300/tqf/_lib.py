@@ -212,6 +212,7 @@ _SIGNATURES = {
     "tqf_euler_update": (ctypes.c_int, [ctypes.POINTER(EulerUpdateArgs), c_vp]),
     "tqf_heston_euler": (ctypes.c_int, [ctypes.POINTER(HestonArgs), c_vp]),
     "tqf_heston_qe": (ctypes.c_int, [ctypes.POINTER(HestonArgs), c_vp]),
+    "tqf_heston_euler_price_noalloc": (ctypes.c_int, [ctypes.POINTER(HestonArgs), c_vp]),
     "tqf_heston_workspace_bytes": (ctypes.c_size_t, [c_i32, c_i32, c_i64, c_i32]),
     "tqf_european_payoff_sums": (ctypes.c_int, [c_i32, c_vp, c_i64, c_i64, c_i32, ctypes.POINTER(Payoff), c_vp]),
     "tqf_european_workspace_bytes": (ctypes.c_size_t, [c_i64, c_i32]),
