@@ -126,6 +126,15 @@ TQF_API uint64_t tqf_launch_count(void);
 TQF_API int tqf_fma_peak_probe(int32_t iters, int32_t blocks_per_sm, float* out, double* lane_ops,
                                void* stream);
 
+/* tcgen05 self-check (no reference counterpart): D = A B^T with A [m x k]
+ * and B [n x k] row-major BF16 (device), staged in the K-major (a_mn/b_mn = 0)
+ * or MN-major (1) canonical no-swizzle layout and multiplied by tcgen05.mma;
+ * out (device, [128 x n] FP32) receives TMEM lanes 0..127.  m in {64, 128},
+ * n and k multiples of 16 up to 128.  *status (device, may be NULL) is set to
+ * TQF_E_TIMEOUT if the MMA completion wait runs out. */
+TQF_API int tqf_tc_selftest(const uint16_t* a, const uint16_t* b, int32_t m, int32_t n, int32_t k,
+                            int32_t a_mn, int32_t b_mn, float* out, int32_t* status, void* stream);
+
 /* ---- Sobol (tff/math/random_ops/sobol/sobol_impl.py) --------------------- */
 
 /* Host-only.  Parses the Joe–Kuo file (new-joe-kuo-6.21201) and writes the

@@ -222,6 +222,7 @@ _SIGNATURES = {
     "tqf_mvgbm_paths": (ctypes.c_int, [ctypes.POINTER(MvgbmArgs), c_vp]),
     "tqf_basket_price": (ctypes.c_int, [ctypes.POINTER(BasketArgs), c_vp]),
     "tqf_basket_workspace_bytes": (ctypes.c_size_t, [c_i32, c_i32, c_i64]),
+    "tqf_tc_selftest": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp]),
     "tqf_fma_peak_probe": (ctypes.c_int, [c_i32, c_i32, c_vp, ctypes.POINTER(ctypes.c_double), c_vp]),
 }
 
