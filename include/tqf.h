@@ -387,6 +387,107 @@ typedef struct tqf_basket_args {
 TQF_API int tqf_basket_price(const tqf_basket_args* args, void* stream);
 TQF_API size_t tqf_basket_workspace_bytes(int32_t dtype, int32_t dim, int64_t num_paths);
 
+/* ---- neural control variate (no reference counterpart) --------------------- */
+
+/* Network g(t, log S, v) = b3 + w3 . silu(W2 silu(W1 x) + b2), x = (f0, f1, f2,
+ * 1, 0 ... 0) with f_i = (raw_i - feat_shift_i) * feat_scale_i; W1 [64][16]
+ * (column 3 is layer 1's bias, columns 4-15 zero) and W2 [64][64] are BF16
+ * row-major (out, in); silu uses the SFU tanh. */
+typedef struct tqf_mlp_weights {
+  const void* w1_bf16;
+  const void* w2_bf16;
+  const float* b2;
+  const float* w3;
+  const float* b3;
+  float feat_scale[3];
+  float feat_shift[3];
+} tqf_mlp_weights;
+
+/* Full-truncation Euler Heston paths (Philox in-kernel, FP32) with an
+ * arithmetic-Asian payoff Y = discount_T max(mean_k S(t_k) - strike, 0) over
+ * num_dates monitoring dates marked in the step table's slot column (date
+ * index, -1 otherwise; table layout of tqf_heston_euler).  date_table
+ * [num_dates][4] = (t_k, exp(-r t_k), 0, 0).
+ *  mode 0: out[5] (device, FP64) = sums of (Y, Y^2, 0, 0, 0);
+ *  mode 1: pilot data: pilot_feats [N][num_dates][4] = (t, log S, v, 0) at
+ *          each interval start, pilot_dS [N][num_dates] discounted-spot
+ *          increments, pilot_Y [N];
+ *  mode 2: out[5] = sums of (Y, Y^2, C, C^2, Y C), C = sum_k g_k dS~_k the
+ *          martingale control variate with the network evaluated on the
+ *          tensor cores at every interval start.
+ * Estimator of the price: mean(Y - C). */
+typedef struct tqf_heston_asian_args {
+  int32_t mode;
+  int32_t num_steps;
+  int64_t num_paths;
+  const float* step_table;
+  int32_t num_dates;
+  int32_t pad0;
+  const float* date_table;
+  double x0;
+  double v0;
+  double strike;
+  double discount_T;
+  tqf_draws draws;
+  tqf_mlp_weights mlp;
+  float* pilot_feats;
+  float* pilot_dS;
+  float* pilot_Y;
+  double* out;
+  void* workspace;
+  size_t workspace_bytes;
+  int32_t* dev_status;
+} tqf_heston_asian_args;
+
+TQF_API int tqf_heston_asian(const tqf_heston_asian_args* args, void* stream);
+TQF_API size_t tqf_heston_asian_workspace_bytes(int32_t mode, int64_t num_paths, int32_t num_steps);
+
+/* Number of FP32 parameters of the network plus the loss offset c:
+ * [W1 64x16 | W2 64x64 | b2 64 | w3 64 | b3 | c]. */
+TQF_API int tqf_mlp_num_params(void);
+
+/* Gradient of loss = mean_p (Y_p - c - sum_k g(feats_pk) dS_pk)^2 over the
+ * paths [path_begin, path_begin + batch_paths) of the pilot data, one CTA per
+ * 32 paths; grad_partials [batch_paths/32][num_params + 1] receives each CTA's
+ * gradient and (last column) its share of the loss.  Forward and backward
+ * GEMMs run on tcgen05 tensor cores (BF16 operands, FP32 accumulation). */
+typedef struct tqf_mlp_train_args {
+  int32_t num_dates;
+  int32_t batch_paths;
+  int64_t path_begin;
+  const float* feats; /* [N][num_dates][4] */
+  const float* dS;    /* [N][num_dates] */
+  const float* Y;     /* [N] */
+  const float* params;
+  const void* w1_bf16;
+  const void* w2_bf16;
+  float feat_scale[3];
+  float feat_shift[3];
+  float* grad_partials;
+  int32_t* dev_status;
+} tqf_mlp_train_args;
+
+TQF_API int tqf_mlp_train_step(const tqf_mlp_train_args* args, void* stream);
+
+/* Adam update: sums the gradient partials in a fixed order, updates the FP32
+ * master parameters and moments and refreshes the BF16 weight copies;
+ * loss_out[0] (device, may be NULL) receives the minibatch loss.
+ * bias1 = 1 - beta1^t, bias2 = 1 - beta2^t. */
+typedef struct tqf_mlp_adam_args {
+  float* params;
+  float* m;
+  float* v;
+  const float* grad_partials;
+  int32_t num_partials;
+  int32_t pad0;
+  void* w1_bf16;
+  void* w2_bf16;
+  float lr, beta1, beta2, eps, bias1, bias2;
+  float* loss_out;
+} tqf_mlp_adam_args;
+
+TQF_API int tqf_mlp_adam(const tqf_mlp_adam_args* args, void* stream);
+
 /* ---- payoff reduction over stored values ----------------------------------- */
 
 /* FP64 sums of European payoffs over values[p * stride] for p < num_values

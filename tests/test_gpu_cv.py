@@ -1,0 +1,116 @@
+"""Neural control variate kernels against the oracle (GPU)."""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import euler as oeuler
+from oracle import grids as ogrids
+from oracle import mlp as omlp
+
+pytestmark = pytest.mark.gpu
+
+KW = dict(spot=100.0, variance=0.04, mean_reversion=2.0, theta=0.04, volvol=0.3, rho=-0.7, rate=0.02, expiry=1.0,
+          strike=100.0, num_dates=52, num_time_steps=252)
+
+
+def _oracle_pilot(cv, N, seed):
+    """Same paths as mode 1 from the materialised canonical draws, in float32."""
+    from tqf.math.random import RandomType
+    from tqf.math.random.multivariate_normal import philox_normal_draws
+    f32 = np.float32
+    draws = philox_normal_draws(RandomType.STATELESS, list(seed), 2, cv.num_steps, N, torch.float32).cpu().numpy()
+    grid = np.linspace(0.0, cv.T, cv.num_steps + 1).astype(f32)
+    dates = (np.arange(1, cv.num_dates + 1) * (cv.T / cv.num_dates)).astype(f32)
+    _, keep, ti = ogrids.prepare_grid(dates, None, f32, times_grid=grid)
+    fd, fv = oeuler.heston_ft_coefficients(cv.rate, cv.kappa, cv.theta, cv.xi, cv.rho, f32)
+    min_v = np.full(N, np.inf)
+
+    def fdm(t, x):
+        np.minimum(min_v, np.abs(x[..., 1]), out=min_v)
+        return fd(t, x)
+
+    x0 = np.tile(np.array([np.log(cv.spot), cv.v0], f32), (N, 1))
+    keep_all = np.zeros(cv.num_steps + 1, bool)
+    keep_all[ti] = True
+    paths = oeuler.sample_with_draws(fdm, fv, grid, keep_all, cv.num_dates, x0, draws, f32).astype(np.float64)
+    S = np.exp(paths[..., 0])
+    t_d = grid[ti].astype(np.float64)
+    disc = np.exp(-cv.rate * t_d)
+    prev = np.concatenate([np.full((N, 1), cv.spot), disc[None, :-1] * S[:, :-1]], 1)
+    dS = disc[None, :] * S - prev
+    Y = np.exp(-cv.rate * float(grid[-1])) * np.maximum(S.mean(1) - cv.strike, 0)
+    feats = np.zeros((N, cv.num_dates, 3))
+    feats[:, 0] = [0.0, np.log(cv.spot), cv.v0]
+    feats[:, 1:, 0] = t_d[None, :-1]
+    feats[:, 1:, 1] = paths[:, :-1, 0]
+    feats[:, 1:, 2] = paths[:, :-1, 1]
+    return feats, dS, Y, min_v > 1e-4
+
+
+def test_pilot_matches_oracle(cuda):
+    from tqf.pricing import HestonAsianCV
+    cv = HestonAsianCV(**KW)
+    N, seed = 2048, (5, 9)
+    feats, dS, Y = cv.pilot(N, seed=seed)
+    of, odS, oY, ok = _oracle_pilot(cv, N, seed)
+    assert ok.mean() > 0.95
+    f = feats.cpu().numpy()[ok]
+    np.testing.assert_allclose(f[..., 0], of[ok][..., 0], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(f[..., 1], of[ok][..., 1], rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(f[..., 2], of[ok][..., 2], rtol=1e-4, atol=2e-6)
+    np.testing.assert_allclose(dS.cpu().numpy()[ok], odS[ok], rtol=1e-3, atol=5e-3)
+    np.testing.assert_allclose(Y.cpu().numpy()[ok], oY[ok], rtol=1e-4, atol=2e-4)
+
+
+def test_fused_inference_matches_network_restatement(cuda):
+    """Mode 2 (network on the tensor cores inside the path kernel) against the
+    restated network applied to the same paths' pilot data."""
+    from tqf.pricing import HestonAsianCV
+    cv = HestonAsianCV(**KW, init_seed=3)
+    N, seed = 4096, (7, 1)
+    feats, dS, Y = cv.pilot(N, seed=seed)
+    est = cv.price(N, control_variate=True, seed=seed)
+    params = cv.params.cpu()
+    g = omlp.network(params, feats.cpu()[..., :3].double().float(), cv.feat_scale, cv.feat_shift)
+    C = (g.double() * dS.cpu().double()).sum(-1)
+    np.testing.assert_allclose(est.plain_price, float(Y.double().mean()), rtol=1e-6)
+    np.testing.assert_allclose(est.mean_control, float(C.mean()), rtol=2e-2, atol=2e-3 * float(C.abs().mean()))
+
+
+def test_train_step_gradient_matches_autograd(cuda):
+    from tqf.pricing import HestonAsianCV
+    cv = HestonAsianCV(**KW, init_seed=11)
+    cv.pilot(4096, seed=(2, 2))
+    B = 128
+    grad, loss = cv.gradient(0, B)
+    params = cv.params.cpu().clone().requires_grad_(True)
+    feats = cv.feats.cpu()[:B, :, :3]
+    L = omlp.loss(params, feats, cv.dS.cpu()[:B], cv.Y.cpu()[:B], cv.feat_scale, cv.feat_shift)
+    L.backward()
+    ref = params.grad
+    got = grad.cpu()
+    np.testing.assert_allclose(loss, float(L), rtol=2e-2)
+    blocks = {"W1": (0, 1024), "W2": (1024, 5120), "b2": (5120, 5184), "w3": (5184, 5248), "b3": (5248, 5249),
+              "c": (5249, 5250)}
+    for name, (a, b) in blocks.items():
+        r, gg = ref[a:b], got[a:b]
+        cos = float(torch.nn.functional.cosine_similarity(r, gg, dim=0)) if b - a > 1 else 1.0
+        assert cos > 0.98, (name, cos)
+        np.testing.assert_allclose(float(gg.norm()), float(r.norm()), rtol=5e-2, err_msg=name)
+
+
+def test_trained_control_variate_is_unbiased_and_reduces_variance(cuda):
+    from tqf.pricing import HestonAsianCV
+    cv = HestonAsianCV(**KW)
+    cv.pilot(1 << 16, seed=(8, 8))
+    base = cv.price(1 << 16, control_variate=True, seed=(3, 5))  # untrained network: unbiased, no gain expected
+    assert abs(base.mean_control) < 5 * base.se_control
+    losses = cv.train(steps=400, batch_paths=2048)
+    assert losses[-1] < losses[0]
+    est = cv.price(1 << 18, control_variate=True, seed=(13, 17))
+    assert abs(est.mean_control) < 5 * est.se_control  # E[C] = 0
+    assert est.vrf > 5.0, est.vrf
+    assert abs(est.price - est.plain_price) < 5 * est.plain_standard_error

@@ -197,6 +197,81 @@ class BasketArgs(ctypes.Structure):
     ]
 
 
+class MlpWeights(ctypes.Structure):
+    _fields_ = [
+        ("w1_bf16", c_vp),
+        ("w2_bf16", c_vp),
+        ("b2", c_vp),
+        ("w3", c_vp),
+        ("b3", c_vp),
+        ("feat_scale", ctypes.c_float * 3),
+        ("feat_shift", ctypes.c_float * 3),
+    ]
+
+
+class HestonAsianArgs(ctypes.Structure):
+    _fields_ = [
+        ("mode", c_i32),
+        ("num_steps", c_i32),
+        ("num_paths", c_i64),
+        ("step_table", c_vp),
+        ("num_dates", c_i32),
+        ("pad0", c_i32),
+        ("date_table", c_vp),
+        ("x0", ctypes.c_double),
+        ("v0", ctypes.c_double),
+        ("strike", ctypes.c_double),
+        ("discount_T", ctypes.c_double),
+        ("draws", Draws),
+        ("mlp", MlpWeights),
+        ("pilot_feats", c_vp),
+        ("pilot_dS", c_vp),
+        ("pilot_Y", c_vp),
+        ("out", c_vp),
+        ("workspace", c_vp),
+        ("workspace_bytes", ctypes.c_size_t),
+        ("dev_status", c_vp),
+    ]
+
+
+class MlpTrainArgs(ctypes.Structure):
+    _fields_ = [
+        ("num_dates", c_i32),
+        ("batch_paths", c_i32),
+        ("path_begin", c_i64),
+        ("feats", c_vp),
+        ("dS", c_vp),
+        ("Y", c_vp),
+        ("params", c_vp),
+        ("w1_bf16", c_vp),
+        ("w2_bf16", c_vp),
+        ("feat_scale", ctypes.c_float * 3),
+        ("feat_shift", ctypes.c_float * 3),
+        ("grad_partials", c_vp),
+        ("dev_status", c_vp),
+    ]
+
+
+class MlpAdamArgs(ctypes.Structure):
+    _fields_ = [
+        ("params", c_vp),
+        ("m", c_vp),
+        ("v", c_vp),
+        ("grad_partials", c_vp),
+        ("num_partials", c_i32),
+        ("pad0", c_i32),
+        ("w1_bf16", c_vp),
+        ("w2_bf16", c_vp),
+        ("lr", ctypes.c_float),
+        ("beta1", ctypes.c_float),
+        ("beta2", ctypes.c_float),
+        ("eps", ctypes.c_float),
+        ("bias1", ctypes.c_float),
+        ("bias2", ctypes.c_float),
+        ("loss_out", c_vp),
+    ]
+
+
 # name -> (restype, argtypes)
 _SIGNATURES = {
     "tqf_abi_version": (ctypes.c_int, []),
@@ -223,6 +298,11 @@ _SIGNATURES = {
     "tqf_basket_price": (ctypes.c_int, [ctypes.POINTER(BasketArgs), c_vp]),
     "tqf_basket_workspace_bytes": (ctypes.c_size_t, [c_i32, c_i32, c_i64]),
     "tqf_tc_selftest": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp]),
+    "tqf_heston_asian": (ctypes.c_int, [ctypes.POINTER(HestonAsianArgs), c_vp]),
+    "tqf_heston_asian_workspace_bytes": (ctypes.c_size_t, [c_i32, c_i64, c_i32]),
+    "tqf_mlp_num_params": (ctypes.c_int, []),
+    "tqf_mlp_train_step": (ctypes.c_int, [ctypes.POINTER(MlpTrainArgs), c_vp]),
+    "tqf_mlp_adam": (ctypes.c_int, [ctypes.POINTER(MlpAdamArgs), c_vp]),
     "tqf_fma_peak_probe": (ctypes.c_int, [c_i32, c_i32, c_vp, ctypes.POINTER(ctypes.c_double), c_vp]),
 }
 
