@@ -357,6 +357,42 @@ def run_gpu(args, rank, world, local_rank):
     return line
 
 
+def run_neural_cv(pilot_paths=1 << 20, train_steps=2000, eval_paths=1 << 26, batch_paths=1024):
+    """Config C5: Heston arithmetic-Asian call (52 dates, K=100) — pilot paths,
+    2,000 Adam steps (lr 1e-3) on the tcgen05 training kernels, then fused CV
+    pricing vs plain MC on the same evaluation paths; time to a 1e-4 relative
+    95% CI for both (GPU seconds, CUDA events), with and without training."""
+    import torch
+    from tqf.pricing import HestonAsianCV, time_to_ci
+    cv = HestonAsianCV(spot=100.0, variance=0.04, mean_reversion=2.0, theta=0.04, volvol=0.3, rho=-0.7, rate=0.02,
+                       expiry=1.0, strike=100.0, num_dates=52, num_time_steps=252)
+    cv.pilot(pilot_paths, seed=(977, 5))
+    cv.price(1 << 16, control_variate=False, seed=(1, 1))  # warm-up of both pricing kernels
+    cv.price(1 << 16, control_variate=True, seed=(1, 1))
+    losses = cv.train(steps=train_steps, batch_paths=batch_paths)
+    plain = cv.price(eval_paths, control_variate=False, seed=(31, 41))
+    est = cv.price(eval_paths, control_variate=True, seed=(31, 41))
+    t_plain = time_to_ci(plain)
+    t_cv = time_to_ci(est)
+    setup = cv.pilot_seconds + cv.train_seconds
+    torch.cuda.synchronize()
+    return {
+        "config": "Heston FT-Euler FP32, 252 steps, arithmetic Asian 52 dates, K=100; MLP 3-64-64-1 SiLU BF16, "
+                  f"{pilot_paths} pilot paths, {train_steps} Adam steps x {batch_paths} paths, {eval_paths} eval paths",
+        "price_cv": est.price, "se_cv": est.standard_error, "price_plain": plain.price, "se_plain": plain.standard_error,
+        "vrf": est.vrf, "bias_in_se": (est.price - plain.price) / plain.standard_error,
+        "mean_control_in_se": est.mean_control / est.se_control,
+        "eval_seconds_plain": plain.seconds, "eval_seconds_cv": est.seconds,
+        "cost_ratio_cv_over_plain": est.seconds / plain.seconds,
+        "pilot_seconds": cv.pilot_seconds, "train_seconds": cv.train_seconds,
+        "loss_first_last": [losses[0], losses[-1]],
+        "time_to_1e-4_ci_plain_s": t_plain["seconds"], "time_to_1e-4_ci_cv_s": t_cv["seconds"],
+        "time_to_1e-4_ci_cv_incl_training_s": t_cv["seconds"] + setup,
+        "speedup_vs_plain": t_plain["seconds"] / t_cv["seconds"],
+        "speedup_vs_plain_incl_training": t_plain["seconds"] / (t_cv["seconds"] + setup),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -367,6 +403,10 @@ def main():
     ap.add_argument("--time-steps", type=int, default=N_STEPS)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-neural-cv", action="store_true")
+    ap.add_argument("--cv-only", action="store_true", help="run only the neural-CV measurement (small sizes ok)")
+    ap.add_argument("--cv-eval-paths", type=int, default=1 << 26)
+    ap.add_argument("--cv-train-steps", type=int, default=2000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "tqf" else args.warmup
     rank = int(os.environ.get("RANK", "0"))
@@ -388,6 +428,9 @@ def main():
         }))
         return
 
+    if args.cv_only:
+        print(json.dumps({"neural_cv": run_neural_cv(eval_paths=args.cv_eval_paths, train_steps=args.cv_train_steps)}))
+        return
     if world > 1:
         import torch
         import torch.distributed as dist
@@ -400,6 +443,8 @@ def main():
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"oracle full-truncation Euler (numpy f32), {cores} procs x {ppc} paths x {N_STEPS} steps, 2 timed rounds, incl. RNG + 64-strike payoff"}
     line = run_gpu(args, rank, world, local_rank)
+    if rank == 0 and world == 1 and not args.no_neural_cv:
+        line["neural_cv"] = run_neural_cv(eval_paths=args.cv_eval_paths, train_steps=args.cv_train_steps)
     if rank == 0:
         line["cpu_baseline"] = cpu
         print(json.dumps(line))

@@ -393,12 +393,19 @@ TQF_API size_t tqf_basket_workspace_bytes(int32_t dtype, int32_t dim, int64_t nu
  * 1, 0 ... 0) with f_i = (raw_i - feat_shift_i) * feat_scale_i; W1 [64][16]
  * (column 3 is layer 1's bias, columns 4-15 zero) and W2 [64][64] are BF16
  * row-major (out, in); silu uses the SFU tanh. */
+typedef struct tqf_mlp_host_weights {
+  float w1[64][4]; /* (w_j0, w_j1, w_j2, b1_j) — columns 0-3 of W1 */
+  float b2[64];
+  float w3[64];
+  float b3;
+} tqf_mlp_host_weights;
+
+/* Inference weights: W2 as a device BF16 [64][64] array (tensor-core operand)
+ * and the small layers from host memory, passed to the kernel by value so
+ * that they are read from the constant bank. */
 typedef struct tqf_mlp_weights {
-  const void* w1_bf16;
   const void* w2_bf16;
-  const float* b2;
-  const float* w3;
-  const float* b3;
+  const tqf_mlp_host_weights* host;
   float feat_scale[3];
   float feat_shift[3];
 } tqf_mlp_weights;
@@ -441,6 +448,9 @@ typedef struct tqf_heston_asian_args {
 
 TQF_API int tqf_heston_asian(const tqf_heston_asian_args* args, void* stream);
 TQF_API size_t tqf_heston_asian_workspace_bytes(int32_t mode, int64_t num_paths, int32_t num_steps);
+/* Resident CTAs per SM of the tqf_heston_asian kernel for `mode`, or a
+ * negative TQF_E_* code. */
+TQF_API int tqf_heston_asian_occupancy(int32_t mode, int32_t num_steps);
 
 /* Number of FP32 parameters of the network plus the loss offset c:
  * [W1 64x16 | W2 64x64 | b2 64 | w3 64 | b3 | c]. */
@@ -448,12 +458,14 @@ TQF_API int tqf_mlp_num_params(void);
 
 /* Gradient of loss = mean_p (Y_p - c - sum_k g(feats_pk) dS_pk)^2 over the
  * paths [path_begin, path_begin + batch_paths) of the pilot data, one CTA per
- * 32 paths; grad_partials [batch_paths/32][num_params + 1] receives each CTA's
+ * paths_per_cta paths; grad_partials [batch_paths/paths_per_cta][num_params + 1] receives each CTA's
  * gradient and (last column) its share of the loss.  Forward and backward
  * GEMMs run on tcgen05 tensor cores (BF16 operands, FP32 accumulation). */
 typedef struct tqf_mlp_train_args {
   int32_t num_dates;
   int32_t batch_paths;
+  int32_t paths_per_cta; /* 1..32; one CTA handles paths_per_cta x num_dates rows */
+  int32_t pad0;
   int64_t path_begin;
   const float* feats; /* [N][num_dates][4] */
   const float* dS;    /* [N][num_dates] */

@@ -3,10 +3,14 @@
 // with full-truncation Heston coefficients, tff/models/euler_sampling.py:513-537).
 //
 // Network g(t, log S, v): 3 -> 64 -> 64 -> 1, SiLU, BF16 weights and
-// activations, FP32 accumulation.  Layers 1 and 2 run on the tcgen05 tensor
-// cores: a warpgroup's 128 rows (one per thread) form an M = 128 tile; the
-// input row is [f0, f1, f2, 1, 0 ... 0] (K = 16, the 1 carries layer 1's
-// bias in column 3 of W1); layer 3 is a 64-term FP32 dot product.
+// activations, FP32 accumulation.  Layer 2 (64 x 64, the GEMM-shaped part)
+// runs on the tcgen05 tensor cores: a warpgroup's 128 rows (one per thread)
+// form an M = 128 tile with the accumulator in TMEM.  Layer 1 (K = 3) is 192
+// FMAs per row on the CUDA cores with the same BF16-rounded operands the
+// tensor cores would use; W1 column 3 holds its bias (input feature 1).
+// SiLU runs in packed BF16 (one SFU tanh per pair); layer 3 is a 64-term
+// FP32 dot product.  The backward GEMMs (d1 = d2 W2, dW2 = d2^T H1,
+// db2 = d2^T 1, dW1 = d1^T X) are tcgen05 MMAs.
 //
 // heston_asian_kernel<MODE>: full-truncation Euler paths (Philox in-kernel),
 //   num_dates monitoring dates marked in the step table's slot column.
@@ -26,6 +30,7 @@
 // mlp_adam_kernel: fixed-order reduction of the per-CTA gradients and the
 //   Adam update of the FP32 master parameters and their BF16 copies.
 #include <cuda_bf16.h>
+#include <string.h>
 
 #include "tqf_tc.cuh"
 
@@ -48,14 +53,16 @@ constexpr int kOffC = kOffB3 + 1;           // 5249
 constexpr int kNumParams = kOffC + 1;       // 5250
 constexpr int kGradWidth = kNumParams + 1;  // + loss sum
 
-// canonical no-swizzle K-major tiles (byte strides)
-constexpr uint32_t kXLbo = 128, kXSbo = 256;    // [128 x 16]
-constexpr uint32_t kHLbo = 128, kHSbo = 1024;   // [128 x 64]
-constexpr uint32_t kW1Lbo = 128, kW1Sbo = 256;  // [64 x 16]
-constexpr uint32_t kW2Lbo = 128, kW2Sbo = 1024; // [64 x 64]
+// Canonical no-swizzle K-major tiles with the 8-row groups contiguous
+// (SBO = 128 B) and the 8-column groups R/8 x 128 B apart (LBO): a K-slice of
+// the operand is one contiguous block, which the tensor core reads without
+// shared-memory bank conflicts.
+constexpr uint32_t kXLbo = 2048, kXSbo = 128;   // [128 x 16]
+constexpr uint32_t kHLbo = 2048, kHSbo = 128;   // [128 x 64]
+constexpr uint32_t kW2Lbo = 1024, kW2Sbo = 128; // [64 x 64]
+constexpr uint32_t kOnesLbo = 128, kOnesSbo = 2048;  // [16 x 128] read MN-major
 constexpr int kXBytes = 128 * kIn * 2;
 constexpr int kHBytes = 128 * kH * 2;
-constexpr int kW1Bytes = kH * kIn * 2;
 constexpr int kW2Bytes = kH * kH * 2;
 
 __device__ __forceinline__ float tanh_approx(float x) {
@@ -78,6 +85,46 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&v);
 }
+__device__ __forceinline__ float bf16_lo(uint32_t p) { return __uint_as_float(p << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t p) { return __uint_as_float(p & 0xFFFF0000u); }
+__device__ __forceinline__ float round_bf16(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+// SiLU of two values in packed BF16 (one SFU op for the pair):
+// x -> h = bf16(x)/2, s = h + h tanh(h) = x sigmoid(x), returned as bf16x2.
+__device__ __forceinline__ uint32_t silu_bf16x2(float a, float b) {
+  const uint32_t x2 = pack_bf16x2(a, b);
+  uint32_t h2, t2, s2;
+  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(h2) : "r"(x2), "r"(0x3F003F00u));
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t2) : "r"(h2));
+  asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(s2) : "r"(h2), "r"(t2), "r"(h2));
+  return s2;
+}
+
+// Layer 1 on the CUDA cores (K = 3 is not GEMM-shaped): a1_j = w1_j . (f0,
+// f1, f2) + b1_j with BF16-rounded operands (exact products, FP32 sums, as
+// the tensor cores would form them), SiLU in packed BF16, written as row r of
+// the K-major H tile.  s_l1[j] = (w_j0, w_j1, w_j2, b1_j).  If a1 is given,
+// the FP32 pre-activations are also returned.
+__device__ __forceinline__ void layer1_row(const float4* __restrict__ s_l1, float f0, float f1, float f2,
+                                           unsigned char* sH, int r, float* a1 = nullptr) {
+#pragma unroll
+  for (int jc = 0; jc < 8; ++jc) {
+    uint32_t pk[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 wa = s_l1[8 * jc + 2 * q];
+      const float4 wb = s_l1[8 * jc + 2 * q + 1];
+      const float aa = fmaf(wa.x, f0, fmaf(wa.y, f1, fmaf(wa.z, f2, wa.w)));
+      const float ab = fmaf(wb.x, f0, fmaf(wb.y, f1, fmaf(wb.z, f2, wb.w)));
+      if (a1) {
+        a1[8 * jc + 2 * q] = aa;
+        a1[8 * jc + 2 * q + 1] = ab;
+      }
+      pk[q] = silu_bf16x2(aa, ab);
+    }
+    *reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, 8 * jc, kHLbo, kHSbo)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+  }
+}
 
 // Writes 8*nlines values of row r of a K-major BF16 tile (16-byte lines).
 __device__ __forceinline__ void write_row_kmajor(unsigned char* tile, int r, const float* v, int nlines,
@@ -94,17 +141,14 @@ __device__ __forceinline__ void write_row_kmajor(unsigned char* tile, int r, con
   }
 }
 
+// Warpgroup barrier (named barrier 1 or 2, 128 threads).  Immediate barrier
+// ids keep the kernel's barrier count at 3; a register id would reserve all
+// 16 and make the occupancy calculator allow one CTA per SM.
 __device__ __forceinline__ void wg_sync(int wg) {
-  asm volatile("bar.sync %0, %1;" ::"r"(1 + wg), "r"(128) : "memory");
-}
-
-// Loads the BF16 weights (row-major [out][in] in global) into K-major tiles.
-__device__ __forceinline__ void load_weight_tiles(unsigned char* sW1, unsigned char* sW2, const uint16_t* w1,
-                                                  const uint16_t* w2) {
-  for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x)
-    *reinterpret_cast<uint16_t*>(sW1 + tc::kmajor_off(i / kIn, i % kIn, kW1Lbo, kW1Sbo)) = w1[i];
-  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x)
-    *reinterpret_cast<uint16_t*>(sW2 + tc::kmajor_off(i / kH, i % kH, kW2Lbo, kW2Sbo)) = w2[i];
+  if (wg == 0)
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+  else
+    asm volatile("bar.sync 2, 128;" ::: "memory");
 }
 
 // Bounded wait on an MMA-completion mbarrier; on time-out records the status
@@ -121,48 +165,42 @@ __device__ __forceinline__ bool mma_wait(uint64_t* bar, uint32_t& phase, int32_t
 }
 
 struct MlpScalars {
+  float4 l1[kH];  // (w_j0, w_j1, w_j2, b1_j), BF16-rounded
   float b2[kH];
   float w3[kH];
   float b3;
   float fscale[3], fshift[3];
 };
 
-// One warpgroup evaluates g for its 128 rows (this thread: row `tid`).
-// tmem_d: 64 FP32 columns owned by the warpgroup (layer 1 then layer 2).
-__device__ __forceinline__ float mlp_forward_tile(int wg, int tid, unsigned char* sX, unsigned char* sH,
-                                                  const unsigned char* sW1, const unsigned char* sW2,
-                                                  const MlpScalars& ms, uint32_t tmem_d, uint64_t* bar,
-                                                  uint32_t& phase, float f0, float f1, float f2,
-                                                  int32_t* status, float* a1_out = nullptr,
-                                                  float* a2_out = nullptr) {
-  float xin[16];
-  xin[0] = (f0 - ms.fshift[0]) * ms.fscale[0];
-  xin[1] = (f1 - ms.fshift[1]) * ms.fscale[1];
-  xin[2] = (f2 - ms.fshift[2]) * ms.fscale[2];
-  xin[3] = 1.f;
-#pragma unroll
-  for (int j = 4; j < 16; ++j) xin[j] = 0.f;
-  write_row_kmajor(sX, tid, xin, 2, kXLbo, kXSbo);
-  tc::fence_smem_to_async();
-  tc::fence_before_sync();
-  wg_sync(wg);
-  tc::fence_after_sync();
-  if (tid == 0) {
-    tc::mma_bf16(tmem_d, tc::smem_desc(smem_addr(sX), kXLbo, kXSbo), tc::smem_desc(smem_addr(sW1), kW1Lbo, kW1Sbo),
-                 tc::idesc_bf16(128, kH, false, false), 0u);
-    tc::commit(bar);
-  }
-  mma_wait(bar, phase, status);
-  const uint32_t lane_base = (uint32_t)(32 * ((tid >> 5) & 3)) << 16;
-  float h[kH];
-#pragma unroll
-  for (int c = 0; c < kH; c += 16) tc::tmem_ld16(tmem_d + lane_base + (uint32_t)c, h + c);
-#pragma unroll
-  for (int j = 0; j < kH; ++j) {
-    if (a1_out) a1_out[j] = h[j];
-    h[j] = silu_fast(h[j]);
-  }
-  write_row_kmajor(sH, tid, h, 8, kHLbo, kHSbo);
+// The same network weights in kernel parameters (constant bank): inference
+// reads them as direct FMA operands, with no shared-memory load instructions.
+struct MlpConst {
+  float4 l1[kH];
+  float b2[kH];
+  float w3[kH];
+  float b3;
+  float fscale[3], fshift[3];
+};
+
+// Normalised, BF16-rounded input features.
+template <class W>
+__device__ __forceinline__ void features(const W& ms, float t, float x, float v, float& f0, float& f1,
+                                         float& f2) {
+  f0 = round_bf16((t - ms.fshift[0]) * ms.fscale[0]);
+  f1 = round_bf16((x - ms.fshift[1]) * ms.fscale[1]);
+  f2 = round_bf16((v - ms.fshift[2]) * ms.fscale[2]);
+}
+
+// Issue half of one network evaluation for the warpgroup's 128 rows: layer 1
+// on the CUDA cores into the H tile, then (one thread) layer 2 as four
+// tcgen05 MMAs into the warpgroup's 64 TMEM columns, committed to `bar`.
+template <class W>
+__device__ __forceinline__ void mlp_issue(int wg, int tid, const W& ms, unsigned char* sH,
+                                          const unsigned char* sW2, uint32_t tmem_d, uint64_t* bar, float t,
+                                          float x, float v) {
+  float f0, f1, f2;
+  features(ms, t, x, v, f0, f1, f2);
+  layer1_row(ms.l1, f0, f1, f2, sH, tid);
   tc::fence_smem_to_async();
   tc::fence_before_sync();
   wg_sync(wg);
@@ -175,18 +213,54 @@ __device__ __forceinline__ float mlp_forward_tile(int wg, int tid, unsigned char
                    tc::smem_desc(smem_addr(sW2) + 2u * s * kW2Lbo, kW2Lbo, kW2Sbo), idesc, s > 0 ? 1u : 0u);
     tc::commit(bar);
   }
+}
+
+// Completes an evaluation: waits for the MMAs, reads this row's 64 layer-2
+// accumulators, applies bias and SiLU (packed BF16) and the FP32 layer-3 dot
+// product.  Optionally returns the FP32 pre-activations a2 and the BF16
+// activations h2 (as floats).
+template <class W>
+__device__ __forceinline__ float mlp_collect(int tid, const W& ms, uint32_t tmem_d, uint64_t* bar,
+                                             uint32_t& phase, int32_t* status, float* a2 = nullptr,
+                                             float* h2 = nullptr) {
   mma_wait(bar, phase, status);
-#pragma unroll
-  for (int c = 0; c < kH; c += 16) tc::tmem_ld16(tmem_d + lane_base + (uint32_t)c, h + c);
+  const uint32_t lane_base = (uint32_t)(32 * ((tid >> 5) & 3)) << 16;
   float g = ms.b3;
 #pragma unroll
-  for (int j = 0; j < kH; ++j) {
-    const float a2 = h[j] + ms.b2[j];
-    if (a2_out) a2_out[j] = a2;
-    g = fmaf(ms.w3[j], silu_fast(a2), g);
+  for (int c = 0; c < kH; c += 16) {
+    float acc[16];
+    tc::tmem_ld16(tmem_d + lane_base + (uint32_t)c, acc);
+#pragma unroll
+    for (int j = 0; j < 16; j += 2) {
+      const float aa = acc[j] + ms.b2[c + j], ab = acc[j + 1] + ms.b2[c + j + 1];
+      const uint32_t sp = silu_bf16x2(aa, ab);
+      const float ha = bf16_lo(sp), hb = bf16_hi(sp);
+      if (a2) {
+        a2[c + j] = aa;
+        a2[c + j + 1] = ab;
+      }
+      if (h2) {
+        h2[c + j] = ha;
+        h2[c + j + 1] = hb;
+      }
+      g = fmaf(ms.w3[c + j], ha, fmaf(ms.w3[c + j + 1], hb, g));
+    }
   }
-  tc::fence_before_sync();  // the next MMA into tmem_d is ordered after these loads
+  tc::fence_before_sync();  // orders these TMEM reads before the next MMA into tmem_d
   return g;
+}
+
+// Loads W2 (BF16 [64][64] row-major) into its K-major tile and the layer-1
+// weights (BF16-rounded) into ms.l1.
+__device__ __forceinline__ void load_network(MlpScalars* ms, unsigned char* sW2, const uint16_t* w1_bf16,
+                                             const uint16_t* w2_bf16) {
+  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x)
+    *reinterpret_cast<uint16_t*>(sW2 + tc::kmajor_off(i / kH, i % kH, kW2Lbo, kW2Sbo)) = w2_bf16[i];
+  for (int j = threadIdx.x; j < kH; j += blockDim.x) {
+    const uint16_t* w = w1_bf16 + j * kIn;
+    ms->l1[j] = make_float4(__uint_as_float((uint32_t)w[0] << 16), __uint_as_float((uint32_t)w[1] << 16),
+                            __uint_as_float((uint32_t)w[2] << 16), __uint_as_float((uint32_t)w[3] << 16));
+  }
 }
 
 // ---- path kernel -----------------------------------------------------------------
@@ -196,20 +270,21 @@ struct AsianSmem {
   uint32_t pad;
   double acc[kPathThreads / 32][5];
   float date_t[kMaxDates], date_disc[kMaxDates];
-  MlpScalars ms;
 };
 
+// Mode 2 pipelines the network with the simulation: the evaluation for
+// interval k is issued at its start date (layer 1 + the layer-2 MMAs) and
+// collected at its end date, so the tensor-core work overlaps the ~T/D of
+// path stepping in between.  Each warpgroup owns 64 TMEM columns.
 template <int MODE>
-__global__ void __launch_bounds__(kPathThreads) heston_asian_kernel(tqf_heston_asian_args a) {
+__global__ void __launch_bounds__(kPathThreads, MODE == 2 ? 4 : 1)
+    heston_asian_kernel(tqf_heston_asian_args a, const __grid_constant__ MlpConst wc) {
   extern __shared__ __align__(1024) unsigned char smem[];
   AsianSmem* S = reinterpret_cast<AsianSmem*>(smem);
   unsigned char* tiles = smem + ((sizeof(AsianSmem) + 1023) & ~(size_t)1023);
-  unsigned char* sW1 = tiles;
-  unsigned char* sW2 = sW1 + kW1Bytes;
-  unsigned char* sXw = sW2 + kW2Bytes;                 // 2 x [128 x 16]
-  unsigned char* sHw = sXw + 2 * kXBytes;              // 2 x [128 x 64]
-  // step table [steps][8] after the network tiles (mode 2) or right away
-  float* table = reinterpret_cast<float*>(MODE == 2 ? sHw + 2 * kHBytes : tiles);
+  unsigned char* sW2 = tiles;
+  unsigned char* sHw = sW2 + kW2Bytes;  // 2 x [128 x 64]
+  float* table = reinterpret_cast<float*>(MODE == 2 ? sHw + 2 * kHBytes : tiles);  // [steps][8]
   const int tid = threadIdx.x & 127, wg = threadIdx.x >> 7;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int D = a.num_dates;
@@ -220,18 +295,10 @@ __global__ void __launch_bounds__(kPathThreads) heston_asian_kernel(tqf_heston_a
   for (int i = threadIdx.x; i < (kPathThreads / 32) * 5; i += blockDim.x) (&S->acc[0][0])[i] = 0.0;
   for (int i = threadIdx.x; i < a.num_steps * 8; i += blockDim.x) table[i] = a.step_table[i];
   if (MODE == 2) {
-    load_weight_tiles(sW1, sW2, static_cast<const uint16_t*>(a.mlp.w1_bf16),
-                      static_cast<const uint16_t*>(a.mlp.w2_bf16));
-    for (int i = threadIdx.x; i < kH; i += blockDim.x) {
-      S->ms.b2[i] = a.mlp.b2[i];
-      S->ms.w3[i] = a.mlp.w3[i];
-    }
+    const uint16_t* w2 = static_cast<const uint16_t*>(a.mlp.w2_bf16);
+    for (int i = threadIdx.x; i < kH * kH; i += blockDim.x)
+      *reinterpret_cast<uint16_t*>(sW2 + tc::kmajor_off(i / kH, i % kH, kW2Lbo, kW2Sbo)) = w2[i];
     if (threadIdx.x == 0) {
-      S->ms.b3 = a.mlp.b3[0];
-      for (int j = 0; j < 3; ++j) {
-        S->ms.fscale[j] = a.mlp.feat_scale[j];
-        S->ms.fshift[j] = a.mlp.feat_shift[j];
-      }
       mbar_init(&S->bar[0], 1);
       mbar_init(&S->bar[1], 1);
     }
@@ -242,8 +309,8 @@ __global__ void __launch_bounds__(kPathThreads) heston_asian_kernel(tqf_heston_a
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem_d = MODE == 2 ? S->tmem_slot + (uint32_t)(wg * kH) : 0u;
-  unsigned char* sX = sXw + wg * kXBytes;
   unsigned char* sH = sHw + wg * kHBytes;
+  uint64_t* bar = &S->bar[wg];
   uint32_t phase = 0;
   const float K = (float)a.strike, discT = (float)a.discount_T, x0 = (float)a.x0, v0 = (float)a.v0;
   const float S0 = __expf(x0);
@@ -256,9 +323,7 @@ __global__ void __launch_bounds__(kPathThreads) heston_asian_kernel(tqf_heston_a
     const int64_t p = (valid ? path : 0) + a.draws.path_offset;
     const uint32_t plo = (uint32_t)p, phi = (uint32_t)((uint64_t)p >> 32);
     float x = x0, v = v0, avg = 0.f, cv = 0.f, prev = S0;
-    float g = 0.f;
-    if (MODE == 2) g = mlp_forward_tile(wg, tid, sX, sH, sW1, sW2, S->ms, tmem_d, &S->bar[wg], phase, 0.f, x0, v0,
-                                        a.dev_status);
+    if (MODE == 2) mlp_issue(wg, tid, wc, sH, sW2, tmem_d, bar, 0.f, x0, v0);
     if (MODE == 1 && valid) reinterpret_cast<float4*>(a.pilot_feats)[path * D] = make_float4(0.f, x0, v0, 0.f);
     float zbuf[4];
     for (int i = 0; i < a.num_steps; ++i) {
@@ -285,16 +350,17 @@ __global__ void __launch_bounds__(kPathThreads) heston_asian_kernel(tqf_heston_a
         const float Sk = __expf(x);
         const float dsk = S->date_disc[k] * Sk - prev;
         avg += Sk;
-        if (MODE == 2) cv = fmaf(g, dsk, cv);
+        if (MODE == 2) {
+          const float g = mlp_collect(tid, wc, tmem_d, bar, phase, a.dev_status);
+          cv = fmaf(g, dsk, cv);
+        }
         if (MODE == 1 && valid) {
           a.pilot_dS[path * D + k] = dsk;
           if (k + 1 < D)
             reinterpret_cast<float4*>(a.pilot_feats)[path * D + k + 1] = make_float4(S->date_t[k], x, v, 0.f);
         }
         prev = S->date_disc[k] * Sk;
-        if (MODE == 2 && k + 1 < D)
-          g = mlp_forward_tile(wg, tid, sX, sH, sW1, sW2, S->ms, tmem_d, &S->bar[wg], phase, S->date_t[k], x, v,
-                               a.dev_status);
+        if (MODE == 2 && k + 1 < D) mlp_issue(wg, tid, wc, sH, sW2, tmem_d, bar, S->date_t[k], x, v);
       }
     }
     const float Y = discT * fmaxf(avg * inv_D - K, 0.f);
@@ -329,23 +395,28 @@ __global__ void __launch_bounds__(kPathThreads) heston_asian_kernel(tqf_heston_a
   }
 }
 
-// Mode 2 also holds the network tiles; its ~60 KB keeps at most 3 CTAs (3 x 128
-// TMEM columns <= 512) on an SM, so no TMEM allocation ever has to wait.
+// Mode 2 holds W2 and two H tiles; its 45..56 KB of shared memory lets at most
+// 4 CTAs (4 x 128 TMEM columns = the SM's 512) share an SM, so no TMEM
+// allocation ever has to wait.
 size_t asian_smem_bytes(int mode, int steps) {
   const size_t head = (sizeof(AsianSmem) + 1023) & ~(size_t)1023;
-  const size_t tiles = mode == 2 ? (size_t)kW1Bytes + kW2Bytes + 2 * kXBytes + 2 * kHBytes : 0;
+  const size_t tiles = mode == 2 ? (size_t)kW2Bytes + 2 * kHBytes : 0;
   size_t total = head + tiles + (size_t)steps * 8 * sizeof(float);
-  if (mode == 2 && total < 58 * 1024) total = 58 * 1024;
+  if (mode == 2 && total < 46 * 1024) total = 46 * 1024;
   return total;
 }
 
 template <int MODE>
 int asian_grid(int64_t n, size_t smem) {
   auto k = heston_asian_kernel<MODE>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem_config(k, smem);
   int occ = 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kPathThreads, smem) != cudaSuccess || occ < 1) occ = 1;
-  if (MODE == 2 && occ > 4) occ = 4;  // 4 CTAs x 128 TMEM columns = the SM's 512
+  // The runtime reports one resident CTA for this tcgen05 kernel although its
+  // registers (64), shared memory and barriers allow four (ncu: all limits 4);
+  // size the persistent grid for four, the most whose 128 TMEM columns fit
+  // the SM's 512.
+  if (MODE == 2) occ = 4;
   int64_t g = (n + kPathThreads - 1) / kPathThreads;
   const int64_t cap = (int64_t)num_sms() * occ;
   if (g > cap) g = cap;
@@ -361,7 +432,6 @@ struct TrainSmem {
   float c;
   float resid[kTrainPaths];
   float Y[kTrainPaths];
-  float w3acc[4][kH];
   float b3acc[4];
   float lossacc;
   float cacc;
@@ -371,34 +441,36 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
   extern __shared__ __align__(1024) unsigned char smem[];
   TrainSmem* S = reinterpret_cast<TrainSmem*>(smem);
   unsigned char* t0 = smem + ((sizeof(TrainSmem) + 1023) & ~(size_t)1023);
-  unsigned char* sW1 = t0;
-  unsigned char* sW2 = sW1 + kW1Bytes;
+  unsigned char* sW2 = t0;
   unsigned char* sX = sW2 + kW2Bytes;
   unsigned char* sH = sX + kXBytes;
-  unsigned char* sD2 = sH + kHBytes;
+  unsigned char* sH2 = sH + kHBytes;
+  unsigned char* sD2 = sH2 + kHBytes;
   unsigned char* sD1 = sD2 + kHBytes;
-  unsigned char* sOnes = sD1 + kHBytes;              // [16 x 128] MN-major, all ones
-  float* g_rows = reinterpret_cast<float*>(sOnes + 16 * 128 * 2);
+  unsigned char* sOnes = sD1 + kHBytes;  // [16 x 128] MN-major, all ones
+  unsigned char* sT3 = sOnes + 16 * 128 * 2;  // [16 x 128] MN-major, column 0 = d3
+  float* g_rows = reinterpret_cast<float*>(sT3 + 16 * 128 * 2);
   const int D = a.num_dates;
-  const int rows = kTrainPaths * D;
+  const int P = a.paths_per_cta;
+  const int rows = P * D;
   float* ds_rows = g_rows + rows;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t p0 = a.path_begin + (int64_t)blockIdx.x * kTrainPaths;
+  const int64_t p0 = a.path_begin + (int64_t)blockIdx.x * P;
   const float inv_B = 1.f / (float)a.batch_paths;
-  // weights (BF16 tiles) and scalars
-  load_weight_tiles(sW1, sW2, static_cast<const uint16_t*>(a.w1_bf16), static_cast<const uint16_t*>(a.w2_bf16));
-  const float* P = a.params;
+  load_network(&S->ms, sW2, static_cast<const uint16_t*>(a.w1_bf16), static_cast<const uint16_t*>(a.w2_bf16));
+  const float* Pm = a.params;
   for (int i = tid; i < kH; i += kTrainThreads) {
-    S->ms.b2[i] = P[kOffB2 + i];
-    S->ms.w3[i] = P[kOffW3 + i];
-    for (int w = 0; w < 4; ++w) S->w3acc[w][i] = 0.f;
+    S->ms.b2[i] = Pm[kOffB2 + i];
+    S->ms.w3[i] = Pm[kOffW3 + i];
   }
-  for (int i = tid; i < 16 * 128; i += kTrainThreads)
-    *reinterpret_cast<uint16_t*>(sOnes + 2 * i) = (uint16_t)0x3F80u;  // bf16 1.0 everywhere
-  if (tid < kTrainPaths) S->Y[tid] = a.Y[p0 + tid];
+  for (int i = tid; i < 16 * 128; i += kTrainThreads) {
+    *reinterpret_cast<uint16_t*>(sOnes + 2 * i) = (uint16_t)0x3F80u;  // bf16 1.0
+    *reinterpret_cast<uint16_t*>(sT3 + 2 * i) = (uint16_t)0u;
+  }
+  if (tid < P) S->Y[tid] = a.Y[p0 + tid];
   if (tid == 0) {
-    S->ms.b3 = P[kOffB3];
-    S->c = P[kOffC];
+    S->ms.b3 = Pm[kOffB3];
+    S->c = Pm[kOffC];
     for (int j = 0; j < 3; ++j) {
       S->ms.fscale[j] = a.feat_scale[j];
       S->ms.fshift[j] = a.feat_shift[j];
@@ -408,13 +480,13 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
     S->cacc = 0.f;
     mbar_init(&S->bar, 1);
   }
-  if (warp == 0) tc::tmem_alloc(&S->tmem_slot, 512);
+  if (warp == 0) tc::tmem_alloc(&S->tmem_slot, 256);
   tc::fence_smem_to_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tm = S->tmem_slot;
-  const uint32_t t_d1 = tm, t_d2 = tm + 64, t_d3 = tm + 128, t_dw2 = tm + 192, t_db2 = tm + 256, t_dw1 = tm + 272;
+  const uint32_t t_d2 = tm, t_d3 = tm + 64, t_dw2 = tm + 128, t_db2 = tm + 192, t_dw1 = tm + 208, t_dw3 = tm + 224;
   uint32_t phase = 0;
   const int tiles = (rows + 127) / 128;
   const float4* feats = reinterpret_cast<const float4*>(a.feats);
@@ -424,8 +496,8 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
     const bool in = r < rows;
     const int pl = in ? r / D : 0, d = in ? r % D : 0;
     const float4 f = in ? feats[(p0 + pl) * D + d] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float gg = mlp_forward_tile(0, tid, sX, sH, sW1, sW2, S->ms, t_d1, &S->bar, phase, f.x, f.y, f.z,
-                                      a.dev_status);
+    mlp_issue(0, tid, S->ms, sH, sW2, t_d2, &S->bar, f.x, f.y, f.z);
+    const float gg = mlp_collect(tid, S->ms, t_d2, &S->bar, phase, a.dev_status);
     if (in) {
       g_rows[r] = gg;
       ds_rows[r] = a.dS[(p0 + pl) * D + d];
@@ -433,14 +505,14 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
   }
   __syncthreads();
   // ---- phase B: per-path residuals r_p = Y_p - c - sum_k g_pk dS_pk
-  if (tid < kTrainPaths) {
+  if (tid < P) {
     float s = 0.f;
     for (int d = 0; d < D; ++d) s = fmaf(g_rows[tid * D + d], ds_rows[tid * D + d], s);
     S->resid[tid] = S->Y[tid] - S->c - s;
   }
   __syncthreads();
   if (warp == 0) {
-    float rr = S->resid[lane];
+    const float rr = lane < P ? S->resid[lane] : 0.f;
     float l = rr * rr, cc = rr;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -459,24 +531,39 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
     const bool in = r < rows;
     const int pl = in ? r / D : 0, d = in ? r % D : 0;
     const float4 f = in ? feats[(p0 + pl) * D + d] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float a1[kH], a2[kH];
-    mlp_forward_tile(0, tid, sX, sH, sW1, sW2, S->ms, t_d1, &S->bar, phase, f.x, f.y, f.z, a.dev_status, a1, a2);
+    // forward again, keeping pre-activations; X row (with the bias 1) for dW1
+    float f0, f1, f2;
+    features(S->ms, f.x, f.y, f.z, f0, f1, f2);
+    float xin[16] = {f0, f1, f2, 1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    write_row_kmajor(sX, tid, xin, 2, kXLbo, kXSbo);
+    float a1[kH], a2[kH], h2[kH];
+    layer1_row(S->ms.l1, f0, f1, f2, sH, tid, a1);
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+      const uint32_t idesc = tc::idesc_bf16(128, kH, false, false);
+#pragma unroll
+      for (int s = 0; s < 4; ++s)
+        tc::mma_bf16(t_d2, tc::smem_desc(smem_addr(sH) + 2u * s * kHLbo, kHLbo, kHSbo),
+                     tc::smem_desc(smem_addr(sW2) + 2u * s * kW2Lbo, kW2Lbo, kW2Sbo), idesc, s > 0 ? 1u : 0u);
+      tc::commit(&S->bar);
+    }
+    mlp_collect(tid, S->ms, t_d2, &S->bar, phase, a.dev_status, a2, h2);
     const float d3 = in ? -2.f * S->resid[pl] * ds_rows[r] * inv_B : 0.f;
     float d2[kH];
+#pragma unroll
+    for (int j = 0; j < kH; ++j) d2[j] = d3 * S->ms.w3[j] * dsilu_fast(a2[j]);
     float b3p = d3;
-#pragma unroll
-    for (int j = 0; j < kH; ++j) {
-      const float h2 = silu_fast(a2[j]);
-      float w = d3 * h2;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) w += __shfl_xor_sync(0xffffffffu, w, off);
-      if (lane == 0) S->w3acc[warp][j] += w;
-      d2[j] = d3 * S->ms.w3[j] * dsilu_fast(a2[j]);
-    }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) b3p += __shfl_xor_sync(0xffffffffu, b3p, off);
     if (lane == 0) S->b3acc[warp] += b3p;
     write_row_kmajor(sD2, tid, d2, 8, kHLbo, kHSbo);
+    write_row_kmajor(sH2, tid, h2, 8, kHLbo, kHSbo);
+    // d3 into column 0 of the [16 x 128] MN-major operand (line of row r: n = 0..7)
+    *reinterpret_cast<uint4*>(sT3 + tc::mnmajor_off(0, tid, kOnesLbo, kOnesSbo)) =
+        make_uint4(pack_bf16x2(d3, 0.f), 0u, 0u, 0u);
     tc::fence_smem_to_async();
     tc::fence_before_sync();
     __syncthreads();
@@ -488,16 +575,18 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
       for (int s = 0; s < 4; ++s)
         tc::mma_bf16(t_d3, tc::smem_desc(smem_addr(sD2) + 2u * s * kHLbo, kHLbo, kHSbo),
                      tc::smem_desc(smem_addr(sW2) + 2u * s * kW2Sbo, kW2Sbo, kW2Lbo), id_b1, s > 0 ? 1u : 0u);
-      // dW2 += d2^T H1: A = d2 read MN-major (M = out), B = H1 read MN-major (N = in), K = rows
+      // dW2 += d2^T H1, db2 += d2^T 1, dw3 += h2^T d3 (A read MN-major with M = 64, K = rows)
       const uint32_t id_w2 = tc::idesc_bf16(64, kH, true, true);
-      const uint32_t id_b2 = tc::idesc_bf16(64, 16, true, true);
+      const uint32_t id_n16 = tc::idesc_bf16(64, 16, true, true);
 #pragma unroll
       for (int s = 0; s < 8; ++s) {
         const uint32_t acc = (t > 0 || s > 0) ? 1u : 0u;
-        tc::mma_bf16(t_dw2, tc::smem_desc(smem_addr(sD2) + 2u * s * kHSbo, kHSbo, kHLbo),
-                     tc::smem_desc(smem_addr(sH) + 2u * s * kHSbo, kHSbo, kHLbo), id_w2, acc);
-        tc::mma_bf16(t_db2, tc::smem_desc(smem_addr(sD2) + 2u * s * kHSbo, kHSbo, kHLbo),
-                     tc::smem_desc(smem_addr(sOnes) + 2u * s * 256u, 256u, 128u), id_b2, acc);
+        const uint64_t dd2 = tc::smem_desc(smem_addr(sD2) + 2u * s * kHSbo, kHSbo, kHLbo);
+        tc::mma_bf16(t_dw2, dd2, tc::smem_desc(smem_addr(sH) + 2u * s * kHSbo, kHSbo, kHLbo), id_w2, acc);
+        tc::mma_bf16(t_db2, dd2, tc::smem_desc(smem_addr(sOnes) + 2u * s * kOnesLbo, kOnesLbo, kOnesSbo), id_n16,
+                     acc);
+        tc::mma_bf16(t_dw3, tc::smem_desc(smem_addr(sH2) + 2u * s * kHSbo, kHSbo, kHLbo),
+                     tc::smem_desc(smem_addr(sT3) + 2u * s * kOnesLbo, kOnesLbo, kOnesSbo), id_n16, acc);
       }
       tc::commit(&S->bar);
     }
@@ -531,24 +620,21 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
     float v[kH];
 #pragma unroll
     for (int c = 0; c < kH; c += 16) tc::tmem_ld16(t_dw2 + lane_base + (uint32_t)c, v + c);
-    float vb[16], vw1[16];
+    float vb[16], vw1[16], vw3[16];
     tc::tmem_ld16(t_db2 + lane_base, vb);
     tc::tmem_ld16(t_dw1 + lane_base, vw1);
+    tc::tmem_ld16(t_dw3 + lane_base, vw3);
     if (lane < 16) {
       const int m = 16 * warp + lane;
 #pragma unroll
       for (int j = 0; j < kH; ++j) G[kOffW2 + m * kH + j] = v[j];
       G[kOffB2 + m] = vb[0];
+      G[kOffW3 + m] = vw3[0];
 #pragma unroll
       for (int j = 0; j < kIn; ++j) G[kOffW1 + m * kIn + j] = j < 4 ? vw1[j] : 0.f;
     }
   }
   __syncthreads();
-  if (tid < kH) {
-    float s = 0.f;
-    for (int w = 0; w < 4; ++w) s += S->w3acc[w][tid];
-    G[kOffW3 + tid] = s;
-  }
   if (tid == 0) {
     float s = 0.f;
     for (int w = 0; w < 4; ++w) s += S->b3acc[w];
@@ -560,16 +646,16 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
   __syncthreads();
   if (warp == 0) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(tm, 512);
+    tc::tmem_dealloc(tm, 256);
   }
 }
 
-// The training CTA holds all 512 TMEM columns; >= 116 KB of shared memory keeps
-// it alone on its SM so that no allocation has to wait.
-size_t train_smem_bytes(int dates) {
-  size_t total = ((sizeof(TrainSmem) + 1023) & ~(size_t)1023) + kW1Bytes + kW2Bytes + kXBytes + 3 * kHBytes +
-                 16 * 128 * 2 + (size_t)2 * kTrainPaths * dates * sizeof(float);
-  if (total < 116 * 1024) total = 116 * 1024;
+// 256 TMEM columns per training CTA; >= 76 KB of shared memory keeps at most
+// two such CTAs on an SM (2 x 256 = 512 columns).
+size_t train_smem_bytes(int dates, int paths) {
+  size_t total = ((sizeof(TrainSmem) + 1023) & ~(size_t)1023) + kW2Bytes + kXBytes + 4 * kHBytes + 2 * 16 * 128 * 2 +
+                 (size_t)2 * paths * dates * sizeof(float);
+  if (total < 76 * 1024) total = 76 * 1024;
   return total;
 }
 
@@ -601,6 +687,17 @@ __global__ void mlp_adam_kernel(tqf_mlp_adam_args a) {
 
 using namespace tqf;
 
+// Host-side round-to-nearest-even to BF16 (the device's __float2bfloat16_rn).
+static float bf16_round_host(float x) {
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  if ((u & 0x7F800000u) != 0x7F800000u) u += 0x7FFFu + ((u >> 16) & 1u);
+  u &= 0xFFFF0000u;
+  float r;
+  memcpy(&r, &u, 4);
+  return r;
+}
+
 extern "C" size_t tqf_heston_asian_workspace_bytes(int32_t mode, int64_t num_paths, int32_t num_steps) {
   const size_t smem = asian_smem_bytes(mode, num_steps);
   int grid = mode == 2 ? asian_grid<2>(num_paths, smem) : asian_grid<0>(num_paths, smem);
@@ -621,8 +718,7 @@ extern "C" int tqf_heston_asian(const tqf_heston_asian_args* a, void* stream) {
   if (a->mode == 1)
     TQF_REQUIRE(a->pilot_feats && a->pilot_dS && a->pilot_Y, "tqf_heston_asian: pilot outputs required");
   if (a->mode == 2)
-    TQF_REQUIRE(a->mlp.w1_bf16 && a->mlp.w2_bf16 && a->mlp.b2 && a->mlp.w3 && a->mlp.b3,
-                "tqf_heston_asian: network weights required");
+    TQF_REQUIRE(a->mlp.w2_bf16 && a->mlp.host, "tqf_heston_asian: network weights required (w2_bf16, host)");
   const size_t smem = asian_smem_bytes(a->mode, a->num_steps);
   TQF_REQUIRE(smem <= 227 * 1024, "tqf_heston_asian: step table too large for shared memory");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -635,12 +731,45 @@ extern "C" int tqf_heston_asian(const tqf_heston_asian_args* a, void* stream) {
     TQF_REQUIRE(a->out && a->workspace && a->workspace_bytes >= need, "tqf_heston_asian: workspace %zu < %zu",
                 a->workspace_bytes, need);
   }
-  if (a->mode == 0) heston_asian_kernel<0><<<grid, kPathThreads, smem, s>>>(*a);
-  else if (a->mode == 1) heston_asian_kernel<1><<<grid, kPathThreads, smem, s>>>(*a);
-  else heston_asian_kernel<2><<<grid, kPathThreads, smem, s>>>(*a);
+  MlpConst wc;
+  memset(&wc, 0, sizeof(wc));
+  if (a->mode == 2) {
+    const tqf_mlp_host_weights* h = a->mlp.host;
+    for (int j = 0; j < kH; ++j) {
+      // layer-1 weights and bias as the BF16 values the training kernels use
+      wc.l1[j] = make_float4(bf16_round_host(h->w1[j][0]), bf16_round_host(h->w1[j][1]),
+                             bf16_round_host(h->w1[j][2]), bf16_round_host(h->w1[j][3]));
+      wc.b2[j] = h->b2[j];
+      wc.w3[j] = h->w3[j];
+    }
+    wc.b3 = h->b3;
+    for (int j = 0; j < 3; ++j) {
+      wc.fscale[j] = a->mlp.feat_scale[j];
+      wc.fshift[j] = a->mlp.feat_shift[j];
+    }
+  }
+  if (a->mode == 0) heston_asian_kernel<0><<<grid, kPathThreads, smem, s>>>(*a, wc);
+  else if (a->mode == 1) heston_asian_kernel<1><<<grid, kPathThreads, smem, s>>>(*a, wc);
+  else heston_asian_kernel<2><<<grid, kPathThreads, smem, s>>>(*a, wc);
   int rc = check_launch("heston_asian_kernel");
   if (rc || a->mode == 1) return rc;
   return reduce_partials(static_cast<const double*>(a->workspace), grid, 5, a->out, s);
+}
+
+extern "C" int tqf_heston_asian_occupancy(int32_t mode, int32_t num_steps) {
+  clear_error();
+  const size_t smem = asian_smem_bytes(mode, num_steps);
+  int occ = -1;
+  cudaError_t e;
+  if (mode == 2) {
+    set_smem_config(heston_asian_kernel<2>, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, heston_asian_kernel<2>, kPathThreads, smem);
+  } else {
+    set_smem_config(heston_asian_kernel<0>, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, heston_asian_kernel<0>, kPathThreads, smem);
+  }
+  if (e != cudaSuccess) return check_cuda(e, "tqf_heston_asian_occupancy");
+  return occ;
 }
 
 extern "C" int tqf_mlp_num_params(void) { return kNumParams; }
@@ -649,14 +778,16 @@ extern "C" int tqf_mlp_train_step(const tqf_mlp_train_args* a, void* stream) {
   clear_error();
   TQF_REQUIRE(a != nullptr, "tqf_mlp_train_step: null args");
   TQF_REQUIRE(a->num_dates >= 1 && a->num_dates <= kMaxDates, "tqf_mlp_train_step: bad num_dates");
-  TQF_REQUIRE(a->batch_paths >= kTrainPaths && a->batch_paths % kTrainPaths == 0,
-              "tqf_mlp_train_step: batch_paths must be a positive multiple of %d", kTrainPaths);
+  TQF_REQUIRE(a->paths_per_cta >= 1 && a->paths_per_cta <= kTrainPaths,
+              "tqf_mlp_train_step: paths_per_cta must be in [1, %d]", kTrainPaths);
+  TQF_REQUIRE(a->batch_paths >= a->paths_per_cta && a->batch_paths % a->paths_per_cta == 0,
+              "tqf_mlp_train_step: batch_paths must be a positive multiple of paths_per_cta");
   TQF_REQUIRE(a->feats && a->dS && a->Y && a->params && a->w1_bf16 && a->w2_bf16 && a->grad_partials,
               "tqf_mlp_train_step: null pointer");
-  const int grid = a->batch_paths / kTrainPaths;
-  const size_t smem = train_smem_bytes(a->num_dates);
+  const int grid = a->batch_paths / a->paths_per_cta;
+  const size_t smem = train_smem_bytes(a->num_dates, a->paths_per_cta);
   TQF_REQUIRE(smem <= 227 * 1024, "tqf_mlp_train_step: too many dates");
-  cudaFuncSetAttribute(mlp_train_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem_config(mlp_train_step_kernel, smem);
   mlp_train_step_kernel<<<grid, kTrainThreads, smem, static_cast<cudaStream_t>(stream)>>>(*a);
   return check_launch("mlp_train_step_kernel");
 }

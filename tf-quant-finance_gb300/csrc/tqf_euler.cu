@@ -143,7 +143,7 @@ int launch_affine(const tqf_euler_affine_args& a, cudaStream_t s) {
   void (*k)(tqf_euler_affine_args, int) =
       a.draws.source == TQF_DRAWS_PHILOX ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX>
                                          : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY>;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 48 * 1024) set_smem_config(k, smem);
   int occ = 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem) != cudaSuccess || occ < 1)
     occ = 1;

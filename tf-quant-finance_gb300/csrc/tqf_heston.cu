@@ -426,8 +426,7 @@ int grid_for(int64_t N, int ns, int steps, bool staged, int src, bool store, boo
   SmemLayout L = smem_layout<T>(steps, cols, price ? ns : 0, staged);
   if (out_layout) *out_layout = L;
   auto k = pick_kernel<T, SCHEME>(src, store, price, anti);
-  if (L.total > 48 * 1024)
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+  set_smem_config(k, L.total);
   int occ = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, L.total) != cudaSuccess ||
       occ < 1)

@@ -27,6 +27,15 @@ int check_launch(const char* kernel_name);
     }                                 \
   } while (0)
 
+// Opts a kernel into `smem` bytes of dynamic shared memory and the maximum
+// shared-memory carveout, so that occupancy queries (and launches) see the
+// full shared-memory configuration.
+template <typename K>
+inline void set_smem_config(K kernel, size_t smem) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+}
+
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------
 // Ten rounds of the published round function; the key is bumped by the
 // Weyl constants between rounds.

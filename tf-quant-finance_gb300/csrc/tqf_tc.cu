@@ -86,7 +86,7 @@ extern "C" int tqf_tc_selftest(const uint16_t* a, const uint16_t* b, int32_t m, 
   TQF_REQUIRE(n >= 16 && n <= 128 && n % 16 == 0, "tqf_tc_selftest: n must be a multiple of 16 in [16, 128]");
   TQF_REQUIRE(k >= 16 && k <= 128 && k % 16 == 0, "tqf_tc_selftest: k must be a multiple of 16 in [16, 128]");
   const size_t smem = 1024 + 2 * (size_t)kTcOperandBytes;
-  cudaFuncSetAttribute(tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem_config(tc_selftest_kernel, smem);
   tc_selftest_kernel<<<1, kTcThreads, smem, static_cast<cudaStream_t>(stream)>>>(a, b, m, n, k, a_mn, b_mn,
                                                                                  out, status);
   return check_launch("tc_selftest_kernel");

@@ -197,13 +197,19 @@ class BasketArgs(ctypes.Structure):
     ]
 
 
+class MlpHostWeights(ctypes.Structure):
+    _fields_ = [
+        ("w1", (ctypes.c_float * 4) * 64),
+        ("b2", ctypes.c_float * 64),
+        ("w3", ctypes.c_float * 64),
+        ("b3", ctypes.c_float),
+    ]
+
+
 class MlpWeights(ctypes.Structure):
     _fields_ = [
-        ("w1_bf16", c_vp),
         ("w2_bf16", c_vp),
-        ("b2", c_vp),
-        ("w3", c_vp),
-        ("b3", c_vp),
+        ("host", ctypes.POINTER(MlpHostWeights)),
         ("feat_scale", ctypes.c_float * 3),
         ("feat_shift", ctypes.c_float * 3),
     ]
@@ -238,6 +244,8 @@ class MlpTrainArgs(ctypes.Structure):
     _fields_ = [
         ("num_dates", c_i32),
         ("batch_paths", c_i32),
+        ("paths_per_cta", c_i32),
+        ("pad0", c_i32),
         ("path_begin", c_i64),
         ("feats", c_vp),
         ("dS", c_vp),
@@ -300,6 +308,7 @@ _SIGNATURES = {
     "tqf_tc_selftest": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp]),
     "tqf_heston_asian": (ctypes.c_int, [ctypes.POINTER(HestonAsianArgs), c_vp]),
     "tqf_heston_asian_workspace_bytes": (ctypes.c_size_t, [c_i32, c_i64, c_i32]),
+    "tqf_heston_asian_occupancy": (ctypes.c_int, [c_i32, c_i32]),
     "tqf_mlp_num_params": (ctypes.c_int, []),
     "tqf_mlp_train_step": (ctypes.c_int, [ctypes.POINTER(MlpTrainArgs), c_vp]),
     "tqf_mlp_adam": (ctypes.c_int, [ctypes.POINTER(MlpAdamArgs), c_vp]),
