@@ -393,6 +393,59 @@ def run_neural_cv(pilot_paths=1 << 20, train_steps=2000, eval_paths=1 << 26, bat
     }
 
 
+def run_basket(paths_n=1 << 20, price_paths=1 << 22, n_steps=64, reps=10):
+    """Config C4: 16-asset correlated GBM (FP32, 64 steps, in-kernel Philox).
+    (1) sample_paths writing every date, [paths, 64, 16] float32, with L z on
+    the tensor cores (split BF16, three products) and on CUDA cores; (2) the
+    fused basket call pricer with pathwise delta/vega (L applied once per path
+    to w = sum sqrt(dt) z).  Device time from CUDA events, mean of `reps`."""
+    import torch
+    from tqf.math.random import RandomType
+    from tqf.models import MultivariateGeometricBrownianMotion
+    from tqf.pricing import basket_european_mc
+    d = 16
+    rng = np.random.default_rng(7)
+    vols = rng.uniform(0.1, 0.4, d)
+    q, _ = np.linalg.qr(rng.standard_normal((d, d)))
+    c = q @ np.diag(rng.uniform(0.1, 2.0, d)) @ q.T
+    s = np.sqrt(np.diag(c))
+    corr = c / np.outer(s, s)
+    proc = MultivariateGeometricBrownianMotion(d, means=0.02, volatilities=vols, corr_matrix=corr, dtype=np.float32)
+    times = np.linspace(1.0 / n_steps, 1.0, n_steps)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps / 1e3
+
+    res = {"config": f"16 assets, vols U[0.1,0.4], random-orthogonal correlation, {n_steps} steps, FP32, Philox"}
+    bytes_out = paths_n * n_steps * d * 4
+    for mode, tag in [(0, "tensor_core_lz"), (1, "cuda_core_lz")]:
+        launch, out = proc.paths_launcher(times, initial_state=np.full(d, 100.0, np.float32), num_samples=paths_n,
+                                          random_type=RandomType.STATELESS, seed=[3, 4], lz_mode=mode)
+        sec = timed(launch)
+        res[f"paths_{tag}"] = {"paths": paths_n, "seconds": sec, "path_steps_per_s": paths_n * n_steps / sec,
+                               "store_gbs": bytes_out / sec / 1e9}
+        del out
+    torch.cuda.empty_cache()
+    kw = dict(spots=np.full(d, 100.0), vols=vols, rate=0.02, corr=corr, strike=100.0, expiry=1.0,
+              num_time_steps=n_steps, num_samples=price_paths, dtype=torch.float32)
+    basket_european_mc(**kw, seed=(5, 6))
+    t0 = time.perf_counter()
+    b = basket_european_mc(**kw, seed=(5, 6))
+    sec = time.perf_counter() - t0
+    res["basket_price"] = {"paths": price_paths, "price": b.price, "se": b.standard_error,
+                           "wall_seconds_incl_host": sec, "path_steps_per_s": price_paths * n_steps / sec}
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -407,6 +460,9 @@ def main():
     ap.add_argument("--cv-only", action="store_true", help="run only the neural-CV measurement (small sizes ok)")
     ap.add_argument("--cv-eval-paths", type=int, default=1 << 26)
     ap.add_argument("--cv-train-steps", type=int, default=2000)
+    ap.add_argument("--no-basket", action="store_true")
+    ap.add_argument("--basket-only", action="store_true", help="run only the 16-asset basket measurement")
+    ap.add_argument("--basket-paths", type=int, default=1 << 20)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "tqf" else args.warmup
     rank = int(os.environ.get("RANK", "0"))
@@ -428,6 +484,9 @@ def main():
         }))
         return
 
+    if args.basket_only:
+        print(json.dumps({"basket": run_basket(paths_n=args.basket_paths)}))
+        return
     if args.cv_only:
         print(json.dumps({"neural_cv": run_neural_cv(eval_paths=args.cv_eval_paths, train_steps=args.cv_train_steps)}))
         return
@@ -445,6 +504,8 @@ def main():
     line = run_gpu(args, rank, world, local_rank)
     if rank == 0 and world == 1 and not args.no_neural_cv:
         line["neural_cv"] = run_neural_cv(eval_paths=args.cv_eval_paths, train_steps=args.cv_train_steps)
+    if rank == 0 and world == 1 and not args.no_basket:
+        line["basket"] = run_basket(paths_n=args.basket_paths)
     if rank == 0:
         line["cpu_baseline"] = cpu
         print(json.dumps(line))

@@ -345,6 +345,8 @@ typedef struct tqf_mvgbm_args {
   tqf_draws draws;
   tqf_path_output output;
   int32_t* dev_status;
+  int32_t lz_mode; /* 0: tensor-core split-BF16 L z when dim == 16 (float32), else CUDA cores; 1: CUDA cores */
+  int32_t pad0;
 } tqf_mvgbm_args;
 
 /* FP64 Cholesky factor L (row-major, lower) of an n x n symmetric positive

@@ -131,3 +131,41 @@ def test_basket_autograd_function(cuda):
     np.testing.assert_allclose(spots.grad.numpy(), ref.delta.numpy())
     np.testing.assert_allclose(v.grad.numpy(), ref.vega.numpy())
     np.testing.assert_allclose(float(r.grad), ref.rho)
+
+
+@pytest.mark.parametrize("N", [3000, 128 * 152 * 8 + 77])
+def test_mvgbm_16_factor_tensor_core_lz(cuda, N):
+    """16 factors in FP32 take the tensor-core split-BF16 L z path; its paths
+    match the oracle and the CUDA-core path within 1e-5 relative (64 steps,
+    ragged path count, per-path initial states)."""
+    from tqf.models import MultivariateGeometricBrownianMotion
+    d = 16
+    vols, corr = basket_config(d)
+    times = np.linspace(1.0 / 64, 1.0, 64).astype(np.float32)
+    draws = np.random.default_rng(11).standard_normal((N, 64, d)).astype(np.float32)
+    x0 = np.random.default_rng(12).uniform(50, 150, (N, d)).astype(np.float32)
+    proc = MultivariateGeometricBrownianMotion(d, means=0.03, volatilities=vols, corr_matrix=corr, dtype=np.float32)
+    tc = proc.sample_paths(times, initial_state=x0, normal_draws=draws, lz_mode=0).cpu().numpy()
+    fma = proc.sample_paths(times, initial_state=x0, normal_draws=draws, lz_mode=1).cpu().numpy()
+    np.testing.assert_allclose(tc, fma, rtol=1e-5, atol=0)
+    if N <= 3000:
+        want = omvgbm.sample_with_draws(np.full(d, 0.03), vols, corr, times, np.ones(d, np.float32),
+                                        draws.transpose(1, 0, 2), np.float32) * x0[:, None, :]
+        np.testing.assert_allclose(tc, want, rtol=1e-5, atol=0)
+    # the tensor path is not the CUDA-core path with the products rounded to BF16
+    assert np.abs(tc / fma - 1).max() > 0
+
+
+def test_mvgbm_16_factor_tensor_core_philox(cuda):
+    """In-kernel Philox draws: both L z paths agree and the mean is right."""
+    from tqf.math.random import RandomType
+    from tqf.models import MultivariateGeometricBrownianMotion
+    d = 16
+    vols, corr = basket_config(d)
+    proc = MultivariateGeometricBrownianMotion(d, means=0.01, volatilities=vols, corr_matrix=corr, dtype=np.float32)
+    kw = dict(times=np.linspace(1.0 / 32, 1.0, 32), initial_state=np.full(d, 100.0, np.float32),
+              num_samples=50000, random_type=RandomType.STATELESS, seed=[1, 2])
+    tc = proc.sample_paths(**kw, lz_mode=0).cpu().numpy()
+    fma = proc.sample_paths(**kw, lz_mode=1).cpu().numpy()
+    np.testing.assert_allclose(tc, fma, rtol=1e-5, atol=0)
+    np.testing.assert_allclose(tc[:, -1].mean(0), 100 * np.exp(0.01), rtol=1e-2)

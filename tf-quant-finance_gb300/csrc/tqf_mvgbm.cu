@@ -15,7 +15,9 @@
 //   dP/dS0_i = g_i / S0_i, dP/dsigma_i = g_i (y_i - sigma_i T), dP/dmu_i =
 //   g_i T.  Warp-level FP32 partial sums feed per-warp FP64 accumulators
 //   (fixed order, deterministic).
-#include "tqf_internal.cuh"
+#include <cuda_bf16.h>
+
+#include "tqf_tc.cuh"
 
 namespace tqf {
 namespace {
@@ -93,6 +95,157 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
           if (j < dim) o[j] = x0[j] * exp(cs[j]);
       }
     }
+  }
+}
+
+// ---- tensor-core L z for 16 factors (split BF16, three products) -----------------
+// One warpgroup = 128 paths = one M = 128 tile.  Per step each thread writes
+// its 16 normals split as z = hi + lo (BF16 each) into A_hi / A_lo
+// [128 x 16]; D = A_hi L_hi^T + A_hi L_lo^T + A_lo L_hi^T (M = 128, N = 16,
+// K = 16) accumulates y = L z in FP32 in TMEM.  The step's three MMAs are
+// issued one step ahead (double-buffered tiles and TMEM columns), so the
+// tensor core works while the threads consume the previous step's y.
+constexpr int kLzThreads = 128;
+constexpr uint32_t kLzALbo = 2048, kLzASbo = 128;  // [128 x 16], 8-row groups contiguous
+constexpr uint32_t kLzBLbo = 256, kLzBSbo = 128;   // [16 x 16]
+constexpr int kLzATile = 128 * 16 * 2;              // 4 KiB
+constexpr int kLzBTile = 16 * 16 * 2;
+
+__device__ __forceinline__ uint32_t pack2_bf16(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+struct LzSmem {
+  uint64_t bar[2];
+  uint32_t tmem_slot;
+  uint32_t pad;
+  float drift[16], sigma[16];
+};
+
+__global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_args a) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  LzSmem* S = reinterpret_cast<LzSmem*>(smem);
+  unsigned char* sA = smem + 1024;               // [2 buffers][hi, lo] x 4 KiB
+  unsigned char* sB = sA + 4 * kLzATile;         // L_hi, L_lo
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // split L (row-major [16][16], lower) into BF16 hi/lo B tiles: B[n][k] = L[n][k]
+  for (int i = tid; i < 256; i += kLzThreads) {
+    const int n = i / 16, k = i % 16;
+    const float l = a.chol ? static_cast<const float*>(a.chol)[i] : (n == k ? 1.f : 0.f);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(l);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(l - __bfloat162float(hi));
+    *reinterpret_cast<__nv_bfloat16*>(sB + tc::kmajor_off(n, k, kLzBLbo, kLzBSbo)) = hi;
+    *reinterpret_cast<__nv_bfloat16*>(sB + kLzBTile + tc::kmajor_off(n, k, kLzBLbo, kLzBSbo)) = lo;
+  }
+  if (tid < 16) {
+    S->drift[tid] = static_cast<const float*>(a.drift)[tid];
+    S->sigma[tid] = static_cast<const float*>(a.vol)[tid];
+  }
+  if (tid == 0) {
+    mbar_init(&S->bar[0], 1);
+    mbar_init(&S->bar[1], 1);
+  }
+  if (warp == 0) tc::tmem_alloc(&S->tmem_slot, 32);
+  tc::fence_smem_to_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = S->tmem_slot;
+  const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+  const uint32_t idesc = tc::idesc_bf16(128, 16, false, false);
+  const float* table = static_cast<const float*>(a.step_table);
+  float* out = static_cast<float*>(a.output.ptr);
+  const int ns = a.output.num_slots;
+  const int steps = a.num_steps;
+  uint32_t phase[2] = {0u, 0u};
+  const int64_t per_round = (int64_t)gridDim.x * kLzThreads;
+  for (int64_t base = 0; base < a.num_paths; base += per_round) {
+    const int64_t path = base + (int64_t)blockIdx.x * kLzThreads + tid;
+    const bool valid = path < a.num_paths;
+    const int64_t pp = valid ? path : 0;
+    DrawSource<float> src(a.draws, pp, 16);
+    const float* x0p = static_cast<const float*>(a.x0) + (a.x0_per_path ? pp * 16 : 0);
+    float cs[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) cs[j] = 0.f;
+    if (valid && a.output.init_slot >= 0) {
+      float4* o = reinterpret_cast<float4*>(out + (pp * ns + a.output.init_slot) * 16);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) o[q] = make_float4(x0p[4 * q], x0p[4 * q + 1], x0p[4 * q + 2], x0p[4 * q + 3]);
+    }
+    // write the split normals of `step` into buffer b
+    auto stage = [&](int step, int b) {
+      float z[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) z[c] = src.get(step, c);
+      uint32_t hi[8], lo[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        hi[q] = pack2_bf16(z[2 * q], z[2 * q + 1]);
+        const float h0 = __uint_as_float(hi[q] << 16), h1 = __uint_as_float(hi[q] & 0xFFFF0000u);
+        lo[q] = pack2_bf16(z[2 * q] - h0, z[2 * q + 1] - h1);
+      }
+      unsigned char* th = sA + (2 * b) * kLzATile;
+      unsigned char* tl = th + kLzATile;
+      *reinterpret_cast<uint4*>(th + tc::kmajor_off(tid, 0, kLzALbo, kLzASbo)) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+      *reinterpret_cast<uint4*>(th + tc::kmajor_off(tid, 8, kLzALbo, kLzASbo)) = make_uint4(hi[4], hi[5], hi[6], hi[7]);
+      *reinterpret_cast<uint4*>(tl + tc::kmajor_off(tid, 0, kLzALbo, kLzASbo)) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+      *reinterpret_cast<uint4*>(tl + tc::kmajor_off(tid, 8, kLzALbo, kLzASbo)) = make_uint4(lo[4], lo[5], lo[6], lo[7]);
+    };
+    auto issue = [&](int b) {
+      tc::fence_smem_to_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      tc::fence_after_sync();
+      if (tid == 0) {
+        const uint32_t ah = smem_addr(sA + (2 * b) * kLzATile), al = ah + kLzATile;
+        const uint32_t bh = smem_addr(sB), bl = bh + kLzBTile;
+        const uint32_t d = tmem + (uint32_t)(16 * b);
+        tc::mma_bf16(d, tc::smem_desc(ah, kLzALbo, kLzASbo), tc::smem_desc(bh, kLzBLbo, kLzBSbo), idesc, 0u);
+        tc::mma_bf16(d, tc::smem_desc(ah, kLzALbo, kLzASbo), tc::smem_desc(bl, kLzBLbo, kLzBSbo), idesc, 1u);
+        tc::mma_bf16(d, tc::smem_desc(al, kLzALbo, kLzASbo), tc::smem_desc(bh, kLzBLbo, kLzBSbo), idesc, 1u);
+        tc::commit(&S->bar[b]);
+      }
+    };
+    if (steps > 0) {
+      stage(0, 0);
+      issue(0);
+    }
+    for (int i = 0; i < steps; ++i) {
+      const int b = i & 1;
+      if (i + 1 < steps) {
+        stage(i + 1, b ^ 1);
+        issue(b ^ 1);
+      }
+      bool ok = mbar_wait_bounded(&S->bar[b], phase[b]);
+      if (!ok) {
+        if (a.dev_status) atomicExch(a.dev_status, TQF_E_TIMEOUT);
+        mbar_wait_bounded(&S->bar[b], phase[b]);
+      }
+      phase[b] ^= 1u;
+      tc::fence_after_sync();
+      float y[16];
+      tc::tmem_ld16(tmem + lane_base + (uint32_t)(16 * b), y);
+      tc::fence_before_sync();
+      const float dt = table[i * 4], sdt = table[i * 4 + 1];
+      const int slot = (int)table[i * 4 + 2];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) cs[j] += S->drift[j] * dt + sdt * S->sigma[j] * y[j];
+      if (valid && slot >= 0) {
+        float4* o = reinterpret_cast<float4*>(out + (pp * ns + slot) * 16);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          o[q] = make_float4(x0p[4 * q] * expf(cs[4 * q]), x0p[4 * q + 1] * expf(cs[4 * q + 1]),
+                             x0p[4 * q + 2] * expf(cs[4 * q + 2]), x0p[4 * q + 3] * expf(cs[4 * q + 3]));
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 32);
   }
 }
 
@@ -249,8 +402,36 @@ int launch_basket(const tqf_basket_args& a, cudaStream_t s) {
   return reduce_partials(static_cast<const double*>(a.workspace), grid, width, a.out, s);
 }
 
+int launch_paths_tc(const tqf_mvgbm_args& a, cudaStream_t s) {
+  const size_t smem = 1024 + 4 * (size_t)kLzATile + 2 * kLzBTile;
+  // >= 14.3 KB keeps <= 15 CTAs (15 x 32 TMEM columns <= 512) on an SM
+  const size_t smem_alloc = smem < 16 * 1024 ? 16 * 1024 : smem;
+  set_smem_config(mvgbm_paths_tc_kernel, smem_alloc);
+  // Resident CTAs per SM from the register file (256-register warp
+  // granularity), shared memory and the 512 TMEM columns (32 per CTA).
+  cudaFuncAttributes fa{};
+  int occ = 4;
+  if (cudaFuncGetAttributes(&fa, mvgbm_paths_tc_kernel) == cudaSuccess && fa.numRegs > 0) {
+    const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;
+    occ = 65536 / (warp_regs * (kLzThreads / 32));
+    const int by_smem = (int)((227 * 1024) / (smem_alloc + 1024));
+    if (by_smem < occ) occ = by_smem;
+  }
+  if (occ > 12) occ = 12;
+  if (occ < 1) occ = 1;
+  int64_t grid = (a.num_paths + kLzThreads - 1) / kLzThreads;
+  const int64_t cap = (int64_t)num_sms() * occ;
+  if (grid > cap) grid = cap;
+  mvgbm_paths_tc_kernel<<<(unsigned)grid, kLzThreads, smem_alloc, s>>>(a);
+  return check_launch("mvgbm_paths_tc_kernel");
+}
+
 template <typename T>
 int dispatch_paths(const tqf_mvgbm_args& a, cudaStream_t s) {
+  // Tensor-core L z (split BF16) for 16 correlated float32 factors.
+  if (sizeof(T) == 4 && a.dim == 16 && a.chol != nullptr && a.lz_mode != 1 &&
+      (reinterpret_cast<uintptr_t>(a.output.ptr) & 15u) == 0)
+    return launch_paths_tc(a, s);
   if (a.dim <= 1) return launch_paths<T, 1>(a, s);
   if (a.dim <= 2) return launch_paths<T, 2>(a, s);
   if (a.dim <= 4) return launch_paths<T, 4>(a, s);

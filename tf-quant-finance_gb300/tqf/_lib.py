@@ -171,6 +171,8 @@ class MvgbmArgs(ctypes.Structure):
         ("draws", Draws),
         ("output", PathOutput),
         ("dev_status", c_vp),
+        ("lz_mode", c_i32),
+        ("pad0", c_i32),
     ]
 
 

@@ -58,9 +58,22 @@ class MultivariateGeometricBrownianMotion:
         return self._name
 
     def sample_paths(self, times, initial_state=None, num_samples=1, random_type=None, seed=None, skip=0,
-                     normal_draws=None, name=None):
-        """Returns [num_samples, k, dim] (multivariate_geometric_brownian_motion.py:153-227)."""
+                     normal_draws=None, name=None, lz_mode=0):
+        """Returns [num_samples, k, dim] (multivariate_geometric_brownian_motion.py:153-227).
+
+        ``lz_mode`` (extension): 0 computes L z on the tensor cores (split BF16,
+        three products) when there are 16 float32 factors, 1 forces CUDA cores."""
         del name
+        launch, out = self.paths_launcher(times, initial_state, num_samples, random_type, seed, skip,
+                                          normal_draws, lz_mode)
+        launch()
+        return out
+
+    def paths_launcher(self, times, initial_state=None, num_samples=1, random_type=None, seed=None, skip=0,
+                       normal_draws=None, lz_mode=0):
+        """Prepares one sample_paths launch: returns (launch, out), where
+        launch() runs the path kernel into the preallocated ``out`` on the
+        current stream (repeatable, for timing and graph capture)."""
         np_dt = self._np_dtype
         td = utils.torch_dtype(np_dt)
         times_np = utils.to_numpy(times, np_dt).reshape(-1)
@@ -120,8 +133,14 @@ class MultivariateGeometricBrownianMotion:
         a.output.num_slots = k
         a.output.init_slot = -1
         a.dev_status = _lib.status_buffer(device).data_ptr()
-        _lib.call("tqf_mvgbm_paths", a, _lib.stream_ptr(device))
-        return out
+        a.lz_mode = int(lz_mode)  # 0: tensor cores for 16 float32 factors, 1: CUDA cores
+        keep_alive += [x0, table, drift, vol, chol]
+
+        def launch():
+            _ = keep_alive
+            _lib.call("tqf_mvgbm_paths", a, _lib.stream_ptr(device))
+
+        return launch, out
 
 
 __all__ = ["MultivariateGeometricBrownianMotion", "cholesky_f64"]
