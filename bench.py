@@ -393,7 +393,51 @@ def run_neural_cv(pilot_paths=1 << 20, train_steps=2000, eval_paths=1 << 26, bat
     }
 
 
-def run_basket(paths_n=1 << 20, price_paths=1 << 22, n_steps=64, reps=10):
+def run_sobol(dim=1024, total_points=1 << 26, chunk=1 << 20, timed_chunks=8):
+    """Config C2: Sobol dim 1024, 2^26 points (nd = 27 for the whole set),
+    generated in chunks of 2^20 points (4 GiB each) into one reused buffer,
+    for the uint32, float32 and float32 inverse-normal outputs.  Timed chunks
+    are spread over the index range (chunk c * total/(timed*chunk)); each is
+    written once, larger than L2.  Roofline: 4 B written per element against
+    the measured copy bandwidth."""
+    import torch
+    from tqf import _lib
+    from tqf.math.random import sobol
+    dev = torch.device("cuda", torch.cuda.current_device())
+    nd = sobol.num_digits(total_points, 0)
+    v = sobol.device_direction_numbers(dim, dev)
+    out = torch.empty((chunk, dim), dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    spacing = total_points // (timed_chunks * chunk)
+    peaks, peak_src = measured_peaks()
+    peak = peaks.get("hbm_gbs")
+    res = {"config": f"dim {dim}, {total_points} points, nd {nd}, chunks of {chunk} points, "
+                     f"{timed_chunks} chunks timed (every {spacing}th)"}
+    for kind, tag in [(_lib.SOBOL_U32, "u32"), (_lib.SOBOL_F32, "f32"), (_lib.SOBOL_NORMAL_F32, "normal_f32")]:
+        def launch(c):
+            _lib.call("tqf_sobol_sample", v.data_ptr(), dim, chunk, c * chunk, nd, kind, out.data_ptr(),
+                      stream.cuda_stream)
+        for c in range(2):
+            launch(c)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * timed_chunks)]
+        for j in range(timed_chunks):
+            ev[2 * j].record(stream)
+            launch(j * spacing)
+            ev[2 * j + 1].record(stream)
+        torch.cuda.synchronize()
+        ms = [ev[2 * j].elapsed_time(ev[2 * j + 1]) for j in range(timed_chunks)]
+        sec = sum(ms) / 1e3 / timed_chunks
+        gbs = chunk * dim * 4 / sec / 1e9
+        res[tag] = {"seconds_per_chunk": sec, "points_per_s": chunk / sec, "write_gbs": gbs,
+                    "frac_of_hbm": gbs / peak, "peak_source": peak_src,
+                    "full_set_seconds": sec * total_points / chunk}
+    del out
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_basket(paths_n=1 << 22, price_paths=1 << 22, n_steps=64, reps=10):
     """Config C4: 16-asset correlated GBM (FP32, 64 steps, in-kernel Philox).
     (1) sample_paths writing every date, [paths, 64, 16] float32, with L z on
     the tensor cores (split BF16, three products) and on CUDA cores; (2) the
@@ -462,7 +506,10 @@ def main():
     ap.add_argument("--cv-train-steps", type=int, default=2000)
     ap.add_argument("--no-basket", action="store_true")
     ap.add_argument("--basket-only", action="store_true", help="run only the 16-asset basket measurement")
-    ap.add_argument("--basket-paths", type=int, default=1 << 20)
+    ap.add_argument("--basket-paths", type=int, default=1 << 22)
+    ap.add_argument("--no-sobol", action="store_true")
+    ap.add_argument("--sobol-only", action="store_true", help="run only the Sobol dim-1024 measurement")
+    ap.add_argument("--sobol-chunk", type=int, default=1 << 20, help="points per Sobol launch")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "tqf" else args.warmup
     rank = int(os.environ.get("RANK", "0"))
@@ -484,6 +531,9 @@ def main():
         }))
         return
 
+    if args.sobol_only:
+        print(json.dumps({"sobol": run_sobol(chunk=args.sobol_chunk)}))
+        return
     if args.basket_only:
         print(json.dumps({"basket": run_basket(paths_n=args.basket_paths)}))
         return
@@ -506,6 +556,8 @@ def main():
         line["neural_cv"] = run_neural_cv(eval_paths=args.cv_eval_paths, train_steps=args.cv_train_steps)
     if rank == 0 and world == 1 and not args.no_basket:
         line["basket"] = run_basket(paths_n=args.basket_paths)
+    if rank == 0 and world == 1 and not args.no_sobol:
+        line["sobol"] = run_sobol()
     if rank == 0:
         line["cpu_baseline"] = cpu
         print(json.dumps(line))

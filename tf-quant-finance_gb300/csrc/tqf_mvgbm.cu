@@ -120,8 +120,14 @@ struct LzSmem {
   uint64_t bar[2];
   uint32_t tmem_slot;
   uint32_t pad;
-  float drift[16], sigma[16];
+  float drift[16], sigma[16], x0[16];  // drift and sigma pre-scaled by log2(e)
 };
+
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 
 __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_args a) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -139,8 +145,10 @@ __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_ar
     *reinterpret_cast<__nv_bfloat16*>(sB + kLzBTile + tc::kmajor_off(n, k, kLzBLbo, kLzBSbo)) = lo;
   }
   if (tid < 16) {
-    S->drift[tid] = static_cast<const float*>(a.drift)[tid];
-    S->sigma[tid] = static_cast<const float*>(a.vol)[tid];
+    // the log-state is carried in base 2: x0 * 2^(cumsum / ln 2)
+    S->drift[tid] = static_cast<const float*>(a.drift)[tid] * 1.4426950408889634f;
+    S->sigma[tid] = static_cast<const float*>(a.vol)[tid] * 1.4426950408889634f;
+    S->x0[tid] = a.x0_per_path ? 0.f : static_cast<const float*>(a.x0)[tid];
   }
   if (tid == 0) {
     mbar_init(&S->bar[0], 1);
@@ -165,7 +173,7 @@ __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_ar
     const bool valid = path < a.num_paths;
     const int64_t pp = valid ? path : 0;
     DrawSource<float> src(a.draws, pp, 16);
-    const float* x0p = static_cast<const float*>(a.x0) + (a.x0_per_path ? pp * 16 : 0);
+    const float* x0p = a.x0_per_path ? static_cast<const float*>(a.x0) + pp * 16 : S->x0;
     float cs[16];
 #pragma unroll
     for (int j = 0; j < 16; ++j) cs[j] = 0.f;
@@ -208,7 +216,12 @@ __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_ar
         tc::commit(&S->bar[b]);
       }
     };
+    float dt = 0.f, sdt = 0.f;
+    int slot = -1;
     if (steps > 0) {
+      dt = table[0];
+      sdt = table[1];
+      slot = (int)table[2];
       stage(0, 0);
       issue(0);
     }
@@ -228,16 +241,20 @@ __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_ar
       float y[16];
       tc::tmem_ld16(tmem + lane_base + (uint32_t)(16 * b), y);
       tc::fence_before_sync();
-      const float dt = table[i * 4], sdt = table[i * 4 + 1];
-      const int slot = (int)table[i * 4 + 2];
 #pragma unroll
       for (int j = 0; j < 16; ++j) cs[j] += S->drift[j] * dt + sdt * S->sigma[j] * y[j];
       if (valid && slot >= 0) {
         float4* o = reinterpret_cast<float4*>(out + (pp * ns + slot) * 16);
 #pragma unroll
         for (int q = 0; q < 4; ++q)
-          o[q] = make_float4(x0p[4 * q] * expf(cs[4 * q]), x0p[4 * q + 1] * expf(cs[4 * q + 1]),
-                             x0p[4 * q + 2] * expf(cs[4 * q + 2]), x0p[4 * q + 3] * expf(cs[4 * q + 3]));
+          o[q] = make_float4(x0p[4 * q] * ex2_approx(cs[4 * q]), x0p[4 * q + 1] * ex2_approx(cs[4 * q + 1]),
+                             x0p[4 * q + 2] * ex2_approx(cs[4 * q + 2]),
+                             x0p[4 * q + 3] * ex2_approx(cs[4 * q + 3]));
+      }
+      if (i + 1 < steps) {
+        dt = table[(i + 1) * 4];
+        sdt = table[(i + 1) * 4 + 1];
+        slot = (int)table[(i + 1) * 4 + 2];
       }
     }
   }

@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kThreads)
       w.y = bits32(SobolOut<KIND>::conv(x[VEC > 1 ? 1 : 0], scf, scd));
       w.z = bits32(SobolOut<KIND>::conv(x[VEC > 2 ? 2 : 0], scf, scd));
       w.w = bits32(SobolOut<KIND>::conv(x[VEC > 3 ? 3 : 0], scf, scd));
-      *reinterpret_cast<uint4*>(dst) = w;
+      __stcs(reinterpret_cast<uint4*>(dst), w);  // streamed: written once, not re-read by this kernel
     } else {
 #pragma unroll
       for (int e = 0; e < VEC; ++e)
