@@ -42,15 +42,16 @@ N_STEPS = 252
 N_STRIKES = 64
 PARAMS = dict(spot=100.0, variance=0.04, mean_reversion=2.0, theta=0.04, volvol=0.3, rho=-0.7,
               discount_rate=0.02, expiry=1.0)
-# Algorithmic 32-bit lane operations per path-step of the fused kernel (see
-# DESIGN.md, "Roofline accounting"): Philox4x32-10 half block (40: per round
+# Algorithmic 32-bit lane operations per path-step of the fused kernel,
+# counted from the restated math (not from compiled code): Philox4x32-10 half block (40: per round
 # 4 multiplies, 2 three-input XORs, 2 key adds; 10 rounds per 2 steps), one
 # Box–Muller pair (14: two uniform conversions, lg2, scale, sqrt, angle,
 # sin, cos, two products) and the full-truncation step (14: max, sqrt, two
 # dW products, 3 ops log-spot, 7 ops variance).
 ALU_OPS_PER_PATH_STEP = 40 + 14 + 14
-# DRAM bytes per launch measured by ncu on this kernel (2^22 paths x 252 steps):
-# see profiles/heston_ft_f32_2p22x252.md.  None until captured.
+# DRAM bytes (read + write) per launch of the fused kernel, from an ncu capture
+# of full-size launches (2^22 paths x 252 steps, 64 strikes):
+# profiles/heston_ft_f32_pricing.md.  None until captured.
 NCU_TRAFFIC_BYTES = None
 
 
