@@ -504,6 +504,63 @@ TQF_API int tqf_mlp_adam(const tqf_mlp_adam_args* args, void* stream);
 
 /* ---- payoff reduction over stored values ----------------------------------- */
 
+/* ---- Longstaff–Schwartz regression Monte Carlo ------------------------------
+ * Replaces least_square_mc (tff/models/longstaff_schwartz/lsm.py:128-295)
+ * with its loop body (lsm.py:403-436), _expected_exercise_fn (lsm.py:328-383),
+ * make_polynomial_basis (lsm.py:50-125) and make_basket_put_payoff
+ * (payoff_utils.py:27-98).  The caller runs the backward loop over exercise
+ * indices i = E-1 .. 1 as one tqf_lsm_pass (update with the regression of
+ * i+1, accumulate the normal equations of i) and one tqf_lsm_solve per index,
+ * then a final pass; tqf_lsm_means first when the basis is structured.
+ *
+ * Structured mode (degree >= 0, strikes != NULL): exercise values are basket
+ * puts relu(K_b - mean_d S) and the design is the centred tensor-product
+ * polynomial basis of the given degree, both computed in the kernels from the
+ * paths.  Explicit mode (degree < 0): the caller supplies exercise values
+ * [N][B] and the design [Bp][G][N] for the two exercise dates of each pass.
+ * Sums of the masked normal equations X'X, X'y are FP64; the pseudo-inverse
+ * is an FP64 Jacobi eigen-decomposition with tf.linalg.pinv's cutoff
+ * (10 G eps(dtype) x the largest eigenvalue). */
+typedef struct tqf_lsm_args {
+  int32_t dtype;             /* TQF_F32 / TQF_F64: paths, strikes, discounts, payoffs, design, state */
+  int32_t dim;               /* d <= 16 (structured mode) */
+  int64_t num_paths;         /* N */
+  int32_t num_times;         /* T: time axis of the paths */
+  int32_t paths_batch;       /* Bp: 1 for paths [N][T][d], B for [B][N][T][d] */
+  int32_t batch;             /* B: payoff batch (strikes) */
+  int32_t num_basis;         /* G <= 128 basis functions ((degree + 1)^d when structured) */
+  int32_t degree;            /* >= 0: structured polynomial basis; < 0: explicit design */
+  int32_t num_exercise;      /* E */
+  int64_t num_calibration;   /* > 0: regress on paths [0, n), price on [n, N); 0: all paths */
+  const void* paths;         /* [Bp][N][T][d] contiguous (structured mode) */
+  const void* strikes;       /* [B] (structured mode) */
+  const int32_t* exponents;  /* device [G][d] exponent grid (structured mode) */
+  const int32_t* exercise_times; /* device [E] time indices into the paths */
+  const void* discount;      /* D[E+1][Nd][Bd] with D[0] = 1 (lsm.py:258-272) */
+  int64_t disc_stride_e, disc_stride_n, disc_stride_b; /* elements; 0 broadcasts */
+  void* state;               /* [2][B][N]: cashflow, option values (dtype) */
+  int32_t init;              /* 1: cashflow = payoff at exercise E-1, values = 0 */
+  int32_t upd_index;         /* >= 1: apply the regression of this exercise index first */
+  int32_t acc_index;         /* >= 1: accumulate the normal equations of this exercise index */
+  int32_t final_pass;        /* 1: out[b] = sum over priced paths of D[1]/D[0] (cashflow + values) */
+  const void* init_payoff;   /* explicit mode: [N][B] at exercise E-1 */
+  const void* upd_payoff;    /* explicit mode: [N][B] at exercise upd_index - 1 */
+  const void* upd_design;    /* explicit mode: [Bp][G][N] */
+  const void* acc_payoff;
+  const void* acc_design;
+  double* out;               /* [B] (final pass) */
+  void* workspace;
+  size_t workspace_bytes;
+  int32_t* dev_status;
+} tqf_lsm_args;
+
+TQF_API size_t tqf_lsm_workspace_bytes(const tqf_lsm_args* args);
+/* Column means of the paths at every exercise time (basis centring, lsm.py:106-108). */
+TQF_API int tqf_lsm_means(const tqf_lsm_args* args, void* stream);
+TQF_API int tqf_lsm_pass(const tqf_lsm_args* args, void* stream);
+/* Reduces the pass's partial sums and solves beta = pinv(X'X) X'y per batch member. */
+TQF_API int tqf_lsm_solve(const tqf_lsm_args* args, void* stream);
+
 /* FP64 sums of European payoffs over values[p * stride] for p < num_values
  * (level model: S = spot_scale * values, or log model: S = spot_scale *
  * exp(values) when log_values != 0).  Same output layout as tqf_payoff. */

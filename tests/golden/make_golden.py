@@ -1,5 +1,5 @@
 """Extracts the reference's known-answer vectors for the hot path into
-sobol_golden.json / heston_golden.json.
+sobol_golden.json / heston_golden.json / lsm_golden.json.
 
 Run in a checkout that has the reference sources (read as text; TensorFlow is
 not needed):  python tests/golden/make_golden.py /path/to/tf-quant-finance
@@ -69,6 +69,40 @@ def main(ref_root):
     assert "24.822196" in esrc
     with open(os.path.join(here, "heston_golden.json"), "w") as f:
         json.dump(hest, f, indent=1)
+    # Longstaff-Schwartz: the 8-path example of Longstaff & Schwartz (2001) and
+    # the prices the reference's tests assert for it.
+    lsm_path = os.path.join(tff, "models", "longstaff_schwartz", "lsm_test.py")
+    ltree = ast.parse(open(lsm_path).read())
+    samples = None
+    for node in ltree.body:
+        if isinstance(node, ast.Assign) and getattr(node.targets[0], "id", "") == "_SAMPLES":
+            samples = ast.literal_eval(node.value)
+    lsrc = open(lsm_path).read()
+    for needle in ("[0.0564]", "[0.1144]", "[0.174226]", "[0.1144, 0.199]", "[0.1144, 0.1157]",
+                   "[0.06, 0.06, 0.06]", "[0.05, 0.05, 0.05]", "make_polynomial_basis(10)"):
+        assert needle in lsrc, needle
+    lsm = {
+        "source": "tf_quant_finance/models/longstaff_schwartz/lsm_test.py:26-224",
+        "samples": samples,
+        "rates": [0.06, 0.06, 0.06],
+        "batch_rates": [[0.06, 0.06, 0.06], [0.05, 0.05, 0.05]],
+        "cases": {
+            "european_put": {"exercise_times": [3], "strikes": [1.1], "degree": 2, "discount": "last",
+                             "price": [0.0564]},
+            "american_put": {"exercise_times": [1, 2, 3], "strikes": [1.1], "degree": 2, "price": [0.1144]},
+            "american_put_calibration": {"exercise_times": [1, 2, 3], "strikes": [1.1], "degree": 2,
+                                         "num_calibration_samples": 4, "price": [0.174226]},
+            "american_put_batch_payoff": {"exercise_times": [1, 2, 3], "strikes": [1.1, 1.2], "degree": 2,
+                                          "discount": "batch", "price": [0.1144, 0.199]},
+            "american_put_batch_samples": {"exercise_times": [1, 2, 3], "strikes": [1.1, 1.2], "degree": 2,
+                                           "discount": "batch", "paths_shift": 0.1, "price": [0.1144, 0.1157]},
+            "american_basket_put_2d": {"exercise_times": [1, 2, 3], "strikes": [1.1, 1.2, 1.3], "degree": 10,
+                                       "note": "2-d paths (the sample path twice) price as the 1-d paths"},
+        },
+        "tolerance": {"rtol": 1e-4, "atol": 1e-4},
+    }
+    with open(os.path.join(here, "lsm_golden.json"), "w") as f:
+        json.dump(lsm, f, indent=1)
 
 
 if __name__ == "__main__":

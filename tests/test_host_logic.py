@@ -104,3 +104,22 @@ def test_seed_conventions():
     assert philox_key(RandomType.PSEUDO, 42) == (42, 0)
     with pytest.raises(ValueError):
         philox_key(RandomType.STATELESS, None)
+
+
+def test_lsm_host_basis_and_payoff_match_oracle():
+    """The drop-in basis and payoff callables (torch, any device) equal the
+    oracle's restatement; the exponent grid keeps the reference's order."""
+    import torch
+    from oracle import lsm as olsm
+    from tqf.models.longstaff_schwartz import make_basket_put_payoff, make_polynomial_basis
+    from tqf.models.longstaff_schwartz.lsm import _discount_table, polynomial_exponents
+    for deg, dim in [(2, 1), (3, 2), (1, 4)]:
+        np.testing.assert_array_equal(polynomial_exponents(deg, dim), olsm.polynomial_exponents(deg, dim))
+    rng = np.random.default_rng(0)
+    x = rng.uniform(0.5, 1.5, (2, 50, 4, 2))
+    got = make_polynomial_basis(3)(torch.as_tensor(x), 2).numpy()
+    np.testing.assert_allclose(got, olsm.polynomial_basis(x, 2, 3), rtol=1e-12, atol=1e-14)
+    pay = make_basket_put_payoff([1.0, 1.1], dtype=np.float64)(torch.as_tensor(x), 1).numpy()
+    np.testing.assert_allclose(pay, olsm.basket_put_payoff(x, 1, [1.0, 1.1]), rtol=1e-14)
+    d = _discount_table([0.9, 0.8], 2, np.float64)
+    assert d.shape == (3, 1, 1) and d[0, 0, 0] == 1.0 and d[2, 0, 0] == 0.8

@@ -139,3 +139,46 @@ def test_write_slots():
     keep = np.array([False, True, False, False])
     step_slot, init_slot, n, _ = grids.write_slots(keep, 1, 0)
     assert n == 1 and list(step_slot) == [0]
+
+
+def _lsm_golden():
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "lsm_golden.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_lsm_oracle_matches_reference_known_answers(dtype):
+    """The regression-MC restatement reproduces every price lsm_test.py asserts
+    for the Longstaff & Schwartz (2001) 8-path example."""
+    from oracle import lsm
+    g = _lsm_golden()
+    S = np.array(g["samples"])[..., None]
+    df = np.exp(-np.cumsum(g["rates"]))
+    dfb = np.exp(-np.cumsum(g["batch_rates"], -1))[None]
+    tol = g["tolerance"]
+    c = g["cases"]
+    got = lsm.least_square_mc(S, [3], [1.1], 2, discount_factors=[df[-1]], dtype=dtype)
+    np.testing.assert_allclose(got, c["european_put"]["price"], **tol)
+    got = lsm.least_square_mc(S, [1, 2, 3], [1.1], 2, discount_factors=df, dtype=dtype)
+    np.testing.assert_allclose(got, c["american_put"]["price"], **tol)
+    got = lsm.least_square_mc(S, [1, 2, 3], [1.1], 2, discount_factors=df, num_calibration_samples=4, dtype=dtype)
+    np.testing.assert_allclose(got, c["american_put_calibration"]["price"], **tol)
+    got = lsm.least_square_mc(S, [1, 2, 3], [1.1, 1.2], 2, discount_factors=dfb, dtype=dtype)
+    np.testing.assert_allclose(got, c["american_put_batch_payoff"]["price"], **tol)
+    got = lsm.least_square_mc(np.stack([S, S + 0.1]), [1, 2, 3], [1.1, 1.2], 2, discount_factors=dfb, dtype=dtype)
+    np.testing.assert_allclose(got, c["american_put_batch_samples"]["price"], **tol)
+    two = lsm.least_square_mc(np.concatenate([S, S], -1), [1, 2, 3], [1.1, 1.2, 1.3], 10, discount_factors=df,
+                              dtype=np.float64)
+    one = lsm.least_square_mc(S, [1, 2, 3], [1.1, 1.2, 1.3], 10, discount_factors=df, dtype=np.float64)
+    np.testing.assert_allclose(two, one, **tol)
+    assert two.shape == (3,)
+
+
+def test_lsm_basis_docstring_example():
+    """make_polynomial_basis(2) on [1, 2, 3, 4] (lsm.py:68-77)."""
+    from oracle import lsm
+    x = np.array([[1.0], [2.0], [3.0], [4.0]])[:, None, :]
+    np.testing.assert_allclose(lsm.polynomial_basis(x, 0, 2)[0],
+                               [[1, 1, 1, 1], [-1.5, -0.5, 0.5, 1.5], [2.25, 0.25, 0.25, 2.25]])

@@ -176,6 +176,43 @@ class MvgbmArgs(ctypes.Structure):
     ]
 
 
+class LsmArgs(ctypes.Structure):
+    _fields_ = [
+        ("dtype", c_i32),
+        ("dim", c_i32),
+        ("num_paths", c_i64),
+        ("num_times", c_i32),
+        ("paths_batch", c_i32),
+        ("batch", c_i32),
+        ("num_basis", c_i32),
+        ("degree", c_i32),
+        ("num_exercise", c_i32),
+        ("num_calibration", c_i64),
+        ("paths", c_vp),
+        ("strikes", c_vp),
+        ("exponents", c_vp),
+        ("exercise_times", c_vp),
+        ("discount", c_vp),
+        ("disc_stride_e", c_i64),
+        ("disc_stride_n", c_i64),
+        ("disc_stride_b", c_i64),
+        ("state", c_vp),
+        ("init", c_i32),
+        ("upd_index", c_i32),
+        ("acc_index", c_i32),
+        ("final_pass", c_i32),
+        ("init_payoff", c_vp),
+        ("upd_payoff", c_vp),
+        ("upd_design", c_vp),
+        ("acc_payoff", c_vp),
+        ("acc_design", c_vp),
+        ("out", c_vp),
+        ("workspace", c_vp),
+        ("workspace_bytes", ctypes.c_size_t),
+        ("dev_status", c_vp),
+    ]
+
+
 class BasketArgs(ctypes.Structure):
     _fields_ = [
         ("dtype", c_i32),
@@ -305,6 +342,10 @@ _SIGNATURES = {
     "tqf_heston_adjoint_workspace_bytes": (ctypes.c_size_t, [c_i64]),
     "tqf_cholesky_f64": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp, c_vp]),
     "tqf_mvgbm_paths": (ctypes.c_int, [ctypes.POINTER(MvgbmArgs), c_vp]),
+    "tqf_lsm_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(LsmArgs)]),
+    "tqf_lsm_means": (ctypes.c_int, [ctypes.POINTER(LsmArgs), c_vp]),
+    "tqf_lsm_pass": (ctypes.c_int, [ctypes.POINTER(LsmArgs), c_vp]),
+    "tqf_lsm_solve": (ctypes.c_int, [ctypes.POINTER(LsmArgs), c_vp]),
     "tqf_basket_price": (ctypes.c_int, [ctypes.POINTER(BasketArgs), c_vp]),
     "tqf_basket_workspace_bytes": (ctypes.c_size_t, [c_i32, c_i32, c_i64]),
     "tqf_tc_selftest": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp]),
