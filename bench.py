@@ -438,6 +438,48 @@ def run_sobol(dim=1024, total_points=1 << 26, chunk=1 << 20, timed_chunks=8):
     return res
 
 
+def run_lsm(n_paths=1 << 20, n_dates=50, degree=3, reps=5, cpu_paths=1 << 15):
+    """Longstaff–Schwartz American put (K = 1.1, r = 6 %, sigma = 0.2, T = 1)
+    on GBM paths from this engine's sampler: N paths x 50 exercise dates,
+    float32, centred cubic basis.  Device time of least_square_mc (all
+    passes, reductions and solves, paths resident) from CUDA events; the
+    oracle's NumPy restatement timed on a path sample beside it."""
+    import torch
+    from tqf.math.random import RandomType
+    from tqf.models import MultivariateGeometricBrownianMotion
+    from tqf.models import longstaff_schwartz as L
+    from oracle import lsm as olsm  # CPU baseline only
+    proc = MultivariateGeometricBrownianMotion(1, means=0.06, volatilities=[0.2], dtype=np.float32)
+    times = np.linspace(1.0 / n_dates, 1.0, n_dates)
+    paths = proc.sample_paths(times, initial_state=[1.0], num_samples=n_paths, random_type=RandomType.STATELESS,
+                              seed=[7, 8])
+    ex = list(range(n_dates))
+    df = np.exp(-0.06 * times)
+    pay, basis = L.make_basket_put_payoff([1.1], dtype=np.float32), L.make_polynomial_basis(degree)
+    price = None
+    for _ in range(2):
+        price = L.least_square_mc(paths, ex, pay, basis, discount_factors=df, dtype=np.float32)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        price = L.least_square_mc(paths, ex, pay, basis, discount_factors=df, dtype=np.float32)
+    e1.record()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / reps / 1e3
+    sample = paths[:cpu_paths].cpu().numpy()
+    t0 = time.perf_counter()
+    cpu_price = olsm.least_square_mc(sample, ex, [1.1], degree, discount_factors=df, dtype=np.float32)
+    cpu_sec = time.perf_counter() - t0
+    return {"config": f"American put K=1.1 on GBM (r 0.06, vol 0.2, T 1), {n_paths} paths x {n_dates} exercise dates, "
+                      f"float32, degree-{degree} basis",
+            "price": float(price.cpu().numpy()[0]), "seconds": sec,
+            "path_dates_per_s": n_paths * n_dates / sec,
+            "launches_per_call": 3 * (n_dates - 1) + 4,
+            "cpu_baseline": {"path_dates_per_s": cpu_paths * n_dates / cpu_sec, "cores": 1, "kind": "port",
+                             "sample": f"oracle NumPy restatement, {cpu_paths} paths, price {float(cpu_price[0]):.5f}"}}
+
+
 def run_basket(paths_n=1 << 22, price_paths=1 << 22, n_steps=64, reps=10):
     """Config C4: 16-asset correlated GBM (FP32, 64 steps, in-kernel Philox).
     (1) sample_paths writing every date, [paths, 64, 16] float32, with L z on
@@ -509,6 +551,9 @@ def main():
     ap.add_argument("--basket-only", action="store_true", help="run only the 16-asset basket measurement")
     ap.add_argument("--basket-paths", type=int, default=1 << 22)
     ap.add_argument("--no-sobol", action="store_true")
+    ap.add_argument("--no-lsm", action="store_true")
+    ap.add_argument("--lsm-only", action="store_true", help="run only the Longstaff-Schwartz measurement")
+    ap.add_argument("--lsm-paths", type=int, default=1 << 20)
     ap.add_argument("--sobol-only", action="store_true", help="run only the Sobol dim-1024 measurement")
     ap.add_argument("--sobol-chunk", type=int, default=1 << 20, help="points per Sobol launch")
     args = ap.parse_args()
@@ -532,6 +577,9 @@ def main():
         }))
         return
 
+    if args.lsm_only:
+        print(json.dumps({"lsm": run_lsm(n_paths=args.lsm_paths)}))
+        return
     if args.sobol_only:
         print(json.dumps({"sobol": run_sobol(chunk=args.sobol_chunk)}))
         return
@@ -559,6 +607,8 @@ def main():
         line["basket"] = run_basket(paths_n=args.basket_paths)
     if rank == 0 and world == 1 and not args.no_sobol:
         line["sobol"] = run_sobol()
+    if rank == 0 and world == 1 and not args.no_lsm:
+        line["lsm"] = run_lsm(n_paths=args.lsm_paths)
     if rank == 0:
         line["cpu_baseline"] = cpu
         print(json.dumps(line))

@@ -511,7 +511,8 @@ TQF_API int tqf_mlp_adam(const tqf_mlp_adam_args* args, void* stream);
  * (payoff_utils.py:27-98).  The caller runs the backward loop over exercise
  * indices i = E-1 .. 1 as one tqf_lsm_pass (update with the regression of
  * i+1, accumulate the normal equations of i) and one tqf_lsm_solve per index,
- * then a final pass; tqf_lsm_means first when the basis is structured.
+ * then a final pass; tqf_lsm_gather first when the basis is structured.
+ * tqf_lsm_price runs that whole sequence (structured mode) in one call.
  *
  * Structured mode (degree >= 0, strikes != NULL): exercise values are basket
  * puts relu(K_b - mean_d S) and the design is the centred tensor-product
@@ -554,12 +555,18 @@ typedef struct tqf_lsm_args {
   int32_t* dev_status;
 } tqf_lsm_args;
 
+/* Workspace for a given argument block (needs the CUDA device: sized by occupancy). */
 TQF_API size_t tqf_lsm_workspace_bytes(const tqf_lsm_args* args);
-/* Column means of the paths at every exercise time (basis centring, lsm.py:106-108). */
-TQF_API int tqf_lsm_means(const tqf_lsm_args* args, void* stream);
+/* Structured mode: copies the states at the exercise times into the workspace
+ * ([Bp][E][N][d], one coalesced pass) and their column means (basis centring,
+ * lsm.py:106-108). */
+TQF_API int tqf_lsm_gather(const tqf_lsm_args* args, void* stream);
 TQF_API int tqf_lsm_pass(const tqf_lsm_args* args, void* stream);
-/* Reduces the pass's partial sums and solves beta = pinv(X'X) X'y per batch member. */
+/* Solves beta = pinv(X'X) X'y per batch member from the last pass's sums. */
 TQF_API int tqf_lsm_solve(const tqf_lsm_args* args, void* stream);
+/* Structured mode, whole algorithm: out[b] = least_square_mc price of payoff b
+ * (lsm.py:128-295).  The per-pass fields of args are ignored. */
+TQF_API int tqf_lsm_price(const tqf_lsm_args* args, void* stream);
 
 /* FP64 sums of European payoffs over values[p * stride] for p < num_values
  * (level model: S = spot_scale * values, or log model: S = spot_scale *

@@ -3,18 +3,24 @@
 //
 // The reference loops backwards over exercise dates; each iteration builds a
 // [batch, N, G] design, masks it by "in the money", forms X'X and X'y with two
-// matmuls, takes tf.linalg.pinv (SVD) and re-projects every path.  Here each
-// iteration is:
-//   lsm_pass_kernel   one pass over the paths: applies the previous date's
-//                     regression (continuation value, exercise decision,
-//                     cashflow/value update, discounting) and accumulates this
-//                     date's masked normal equations in FP64 — the design is
-//                     built per path in registers/shared memory, never stored;
-//   reduce_partials   fixed-order sum of the per-CTA partials;
-//   lsm_solve_kernel  one CTA per batch member: cyclic Jacobi eigen-
-//                     decomposition of X'X in FP64 (parallel round-robin
-//                     rotations), pinv with tf.linalg.pinv's cutoff, beta.
-// Per-path arithmetic runs in the dtype of the paths, as in the reference.
+// matmuls, takes tf.linalg.pinv (SVD) and re-projects every path.  Here:
+//   lsm_gather_kernel  one coalesced pass over the paths: copies the states at
+//                      the exercise times into [Bp][E][N][d] (so every later
+//                      pass reads contiguous rows) and sums their columns in
+//                      FP64 (the basis centring means, lsm.py:106-108);
+//   lsm_pass_kernel    per date: applies the previous date's regression
+//                      (continuation value, exercise decision, cashflow and
+//                      value update, discounting) and accumulates this date's
+//                      masked normal equations — the design is built per path
+//                      in shared memory, never stored.  Products are summed in
+//                      the paths' dtype over at most 16 paths, then in FP64;
+//   reduce_partials    fixed-order sum of the per-CTA partials;
+//   lsm_solve_kernel   one CTA per batch member: Jacobi eigen-decomposition of
+//                      X'X in FP64 (serial for <= 16 basis functions, parallel
+//                      round-robin rotations above), pinv with tf.linalg.pinv's
+//                      cutoff, beta.
+// tqf_lsm_price runs the whole backward loop for the structured basis and
+// payoff without returning to the caller.
 #include <math.h>
 
 #include "tqf_internal.cuh"
@@ -26,43 +32,118 @@ constexpr int kMaxBasis = 128;
 constexpr int kMaxDimLsm = 16;
 constexpr int kSolveThreads = 256;
 constexpr int kMaxJacobiSweeps = 40;
+constexpr int kGatherThreads = 256;
+constexpr size_t kGatherTileBytes = 96 * 1024;
+constexpr int kSubSum = 16;  // products summed in the paths' dtype before FP64
 
 __host__ __device__ inline int lsm_entries(int G) { return G * (G + 1) / 2 + G; }
 
-// Chunk of paths per CTA iteration (= threads per CTA), chosen so that the
-// design tile [C][G+1], the accumulators and the beta row fit in 200 KB.
-__host__ inline int lsm_chunk(int G) {
+// Design-tile row stride (elements): odd, so that threads reading one column
+// of consecutive rows hit distinct banks.
+__host__ __device__ inline int lsm_row_stride(int G) { return (G + 1) | 1; }
+
+// Shared memory of the pass kernel: design tile [C][W] (dtype), accumulators
+// [max(En, C)] (FP64), entry -> (j, k) table [max(En, C)], beta [G] and the
+// two centring means [2][16] in the dtype, block-sum scratch, exponents [G][16].
+template <typename T>
+__host__ __device__ inline size_t lsm_pass_smem(int G, int C) {
   const int En = lsm_entries(G);
-  for (int C = 256; C >= 64; C >>= 1) {
-    const int W = (G + 1) | 1;
-    const size_t bytes = (size_t)C * W * 8 + (size_t)(En > C ? En : C) * 8 + (size_t)G * 8 + 64 * 8 +
-                         (size_t)G * kMaxDimLsm;
-    if (bytes <= 200 * 1024) return C;
-  }
+  const size_t items = (size_t)(En > C ? En : C);
+  const size_t tile = ((size_t)C * lsm_row_stride(G) * sizeof(T) + 15) & ~(size_t)15;
+  return tile + items * 8 + items * 4 + ((G + 2 * kMaxDimLsm) * sizeof(T) + 15) / 16 * 16 + 64 * 8 +
+         (size_t)G * kMaxDimLsm;
+}
+
+// Paths per CTA iteration (= threads per CTA): the largest of 256/128/64
+// whose tiles fit in 200 KB.
+template <typename T>
+__host__ inline int lsm_chunk(int G) {
+  for (int C = 256; C >= 64; C >>= 1)
+    if (lsm_pass_smem<T>(G, C) <= 200 * 1024) return C;
   return 64;
 }
 
-__host__ inline size_t lsm_pass_smem(int G, int C) {
-  const int En = lsm_entries(G);
-  const int W = (G + 1) | 1;
-  return (size_t)C * W * 8 + (size_t)(En > C ? En : C) * 8 + (size_t)G * 8 + 64 * 8 + (size_t)G * kMaxDimLsm;
+template <typename T, int DM, int GR>
+__global__ void lsm_pass_kernel(tqf_lsm_args a, const T* __restrict__ xt, void* __restrict__ partials_raw,
+                                const double* __restrict__ beta, const double* __restrict__ means, int C);
+
+// The instantiation for a call: path-state registers for the dimension bucket
+// (1, 2, 4, 16); GR = number of basis functions when it is 2..5 and d <= 2
+// (per-thread register accumulation), else 0 (shared-memory design tile).
+template <typename T>
+__host__ inline void* pass_kernel_for(int d, int G);
+
+template <typename T>
+__host__ inline int lsm_pass_grid(const tqf_lsm_args& a, int* chunk_out, size_t* smem_out) {
+  const int G = a.num_basis;
+  const int C = lsm_chunk<T>(G);
+  const size_t smem = lsm_pass_smem<T>(G, C);
+  const void* k = pass_kernel_for<T>(a.degree >= 0 ? a.dim : 1, G);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+  int occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, C, smem) != cudaSuccess || occ < 1) occ = 1;
+  if (occ > 8) occ = 8;
+  const int64_t chunks = (a.num_paths + C - 1) / C;
+  int64_t g = (int64_t)num_sms() * occ;
+  if (g > chunks) g = chunks;
+  if (chunk_out) *chunk_out = C;
+  if (smem_out) *smem_out = smem;
+  return (int)(g < 1 ? 1 : g);
 }
 
-__host__ inline int lsm_grid_x(const tqf_lsm_args& a, int C) {
-  const int64_t chunks = (a.num_paths + C - 1) / C;
-  int64_t g = (int64_t)num_sms() * (C >= 256 ? 2 : 1);
-  if (g > chunks) g = chunks;
+// Gather tile: whole path rows [Cn][T*d] when at least 8 fit in 96 KB
+// (full = 1, Cn a multiple of 4 so chunk starts stay 16-byte aligned), else
+// the exercise columns [Cn][E*d].  Returns Cn (0: does not fit, rejected).
+__host__ inline int lsm_gather_chunk(const tqf_lsm_args& a, int* full_out = nullptr) {
+  const size_t es = a.dtype == TQF_F32 ? 4 : 8;
+  const size_t Ed = (size_t)a.num_exercise * a.dim;
+  const size_t R = Ed >= kGatherThreads ? 1 : kGatherThreads / Ed;
+  const size_t fixed = ((Ed * R + 1) & ~(size_t)1) * 8 + 2 * ((Ed + 3) & ~(size_t)3) * 4;
+  if (fixed >= 200 * 1024) return 0;
+  size_t room = 200 * 1024 - fixed;
+  if (room > kGatherTileBytes) room = kGatherTileBytes;
+  const size_t full_row = (size_t)a.num_times * a.dim * es;
+  size_t c = room / full_row;
+  int full = 1;
+  if (c >= 8) {
+    c &= ~(size_t)3;
+  } else {
+    full = 0;
+    c = room / ((Ed | 1) * es);
+  }
+  if (c > 256) c = 256;
+  if (full_out) *full_out = full;
+  return (int)c;
+}
+
+__host__ inline size_t lsm_gather_smem(const tqf_lsm_args& a, int Cn, int full) {
+  const size_t es = a.dtype == TQF_F32 ? 4 : 8;
+  const size_t Ed = (size_t)a.num_exercise * a.dim;
+  const size_t R = Ed >= kGatherThreads ? 1 : kGatherThreads / Ed;
+  const size_t row = full ? (size_t)a.num_times * a.dim : (Ed | 1);
+  return ((Ed * R + 1) & ~(size_t)1) * 8 + 2 * ((Ed + 3) & ~(size_t)3) * 4 + (size_t)Cn * row * es;
+}
+
+__host__ inline int lsm_gather_grid(const tqf_lsm_args& a) {
+  const int Cn = lsm_gather_chunk(a);
+  if (Cn < 1) return 1;
+  int64_t g = (a.num_paths + Cn - 1) / Cn;
+  if (g > num_sms() * 2) g = num_sms() * 2;
   return (int)(g < 1 ? 1 : g);
 }
 
 struct WsLayout {
-  size_t partials, sums, beta, means, mean_partials, eig_v, total;
+  size_t partials, sums, beta, means, mean_partials, eig_v, xt, total;
 };
 
 __host__ inline WsLayout lsm_layout(const tqf_lsm_args& a) {
   const int G = a.num_basis, B = a.batch, E = a.num_exercise;
   const int En = lsm_entries(G);
-  const int gx = num_sms() * 2;
+  const int gx = a.dtype == TQF_F32 ? lsm_pass_grid<float>(a, nullptr, nullptr)
+                                    : lsm_pass_grid<double>(a, nullptr, nullptr);
+  const int gg = lsm_gather_grid(a);
+  const size_t es = a.dtype == TQF_F32 ? 4 : 8;
   auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
   WsLayout w{};
   size_t off = 0;
@@ -75,9 +156,11 @@ __host__ inline WsLayout lsm_layout(const tqf_lsm_args& a) {
   w.means = off;
   off += up((size_t)E * a.paths_batch * kMaxDimLsm * 8);
   w.mean_partials = off;
-  off += up((size_t)gx * E * a.paths_batch * kMaxDimLsm * 8);
+  off += up((size_t)gg * E * a.paths_batch * kMaxDimLsm * 8);
   w.eig_v = off;
   off += up((size_t)B * G * G * 8);
+  w.xt = off;
+  if (a.degree >= 0) off += up((size_t)a.paths_batch * E * a.num_paths * a.dim * es);
   w.total = off;
   return w;
 }
@@ -89,20 +172,154 @@ __device__ __forceinline__ T ipow(T x, int e) {
   return r;
 }
 
-// Packed upper triangle, row-major: entry e <-> (j, k), j <= k < G.
-__device__ __forceinline__ void sym_pair(int e, int G, int& j, int& k) {
-  const double g2 = 2.0 * G + 1.0;
-  int jj = (int)((g2 - sqrt(g2 * g2 - 8.0 * e)) * 0.5);
-  if (jj < 0) jj = 0;
-  while (jj > 0 && jj * G - jj * (jj - 1) / 2 > e) --jj;
-  while (jj + 1 < G && (jj + 1) * G - (jj + 1) * jj / 2 <= e) ++jj;
-  j = jj;
-  k = jj + (e - (jj * G - jj * (jj - 1) / 2));
+// ---- cross-path accumulators --------------------------------------------------
+// FP64 is a narrow pipe on this GPU, so float paths accumulate in compensated
+// double-float (an unevaluated float pair hi + lo, Knuth TwoSum additions:
+// ~2^-48 relative, FP32 pipe) and convert to double once per entry at the end;
+// double paths accumulate in FP64.
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  const float s = a.x + b.x;
+  const float bb = s - a.x;
+  const float err = (a.x - (s - bb)) + (b.x - bb);
+  const float lo = err + a.y + b.y;
+  const float hi = s + lo;
+  return make_float2(hi, lo - (hi - s));
 }
 
 template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+  using S = double;
+  __device__ static S zero() { return 0.0; }
+  __device__ static S add(S a, double v) { return a + v; }
+  __device__ static S sum(S a, S b) { return a + b; }
+  __device__ static double value(S a) { return a; }
+  __device__ static S shfl_down(S a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
+};
+template <>
+struct Acc<float> {
+  using S = float2;
+  __device__ static S zero() { return make_float2(0.f, 0.f); }
+  __device__ static S add(S a, float v) { return df_add(a, make_float2(v, 0.f)); }
+  __device__ static S sum(S a, S b) { return df_add(a, b); }
+  __device__ static double value(S a) { return (double)a.x + (double)a.y; }
+  __device__ static S shfl_down(S a, int o) {
+    return make_float2(__shfl_down_sync(0xffffffffu, a.x, o), __shfl_down_sync(0xffffffffu, a.y, o));
+  }
+};
+static_assert(sizeof(Acc<float>::S) == 8 && sizeof(Acc<double>::S) == 8, "8-byte accumulators");
+
+// Fixed-order reduction of per-CTA accumulator rows [rows][width] -> double out[width].
+template <typename T>
+__global__ void __launch_bounds__(1024)
+    lsm_reduce_kernel(const typename Acc<T>::S* __restrict__ part, int rows, int width, double* __restrict__ out) {
+  using A = Acc<T>;
+  __shared__ typename A::S s[32][33];
+  const int c = threadIdx.x % 32, r = threadIdx.x / 32;
+  const int w = blockIdx.x * 32 + c;
+  typename A::S acc = A::zero();
+  if (w < width)
+    for (int i = r; i < rows; i += 32) acc = A::sum(acc, part[(size_t)i * width + w]);
+  s[r][c] = acc;
+  __syncthreads();
+  for (int st = 16; st > 0; st >>= 1) {
+    if (r < st) s[r][c] = A::sum(s[r][c], s[r + st][c]);
+    __syncthreads();
+  }
+  if (r == 0 && w < width) out[w] = A::value(s[0][c]);
+}
+
+
+// ---- gather the exercise-time states, column sums -------------------------------
+// CTA (x, pb): chunks of Cn consecutive paths.  When whole path rows fit
+// (full = 1) the chunk [Cn][T*d] is one contiguous range, copied with 16-byte
+// loads; otherwise only the exercise columns are loaded.  Column sums use R
+// replicas per column, combined in a fixed order at the end.
+template <typename T>
+__global__ void __launch_bounds__(kGatherThreads)
+    lsm_gather_kernel(tqf_lsm_args a, T* __restrict__ xt, typename Acc<T>::S* __restrict__ partials, int Cn,
+                      int full) {
+  using A = Acc<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int d = a.dim, E = a.num_exercise;
+  const int Ed = E * d;
+  const int64_t Td = (int64_t)a.num_times * d;
+  const int Wt = full ? (int)Td : (Ed | 1);
+  const int R = Ed >= kGatherThreads ? 1 : kGatherThreads / Ed;
+  const int nacc = Ed * R;
+  typename A::S* acc = reinterpret_cast<typename A::S*>(smem);  // [nacc]
+  int* col = reinterpret_cast<int*>(acc + ((nacc + 1) & ~1));   // [Ed] column of each exercise state in a tile row
+  int* src = col + ((Ed + 3) & ~3);                              // [Ed] column within a path row
+  T* tile = reinterpret_cast<T*>(src + ((Ed + 3) & ~3));         // [Cn][Wt]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int pb = blockIdx.y;
+  const int64_t N = a.num_paths;
+  const T* P = static_cast<const T*>(a.paths) + (int64_t)pb * N * Td;
+  T* X = xt + (int64_t)pb * E * N * d;
+  for (int j = tid; j < nacc; j += kGatherThreads) acc[j] = A::zero();
+  for (int j = tid; j < Ed; j += kGatherThreads) {
+    src[j] = a.exercise_times[j / d] * d + j % d;
+    col[j] = full ? src[j] : j;
+  }
+  const int64_t nchunks = (N + Cn - 1) / Cn;
+  for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    const int64_t n0 = ch * Cn;
+    const int cn = (int)((N - n0) < Cn ? (N - n0) : Cn);
+    __syncthreads();
+    if (full) {
+      const T* base = P + n0 * Td;
+      const int64_t count = (int64_t)cn * Td;
+      constexpr int V = 16 / sizeof(T);
+      if ((reinterpret_cast<uintptr_t>(base) & 15u) == 0 && count % V == 0) {
+        const uint4* b4 = reinterpret_cast<const uint4*>(base);
+        uint4* t4 = reinterpret_cast<uint4*>(tile);
+        const int64_t n4 = count / V;
+#pragma unroll 4
+        for (int64_t q = tid; q < n4; q += kGatherThreads) t4[q] = __ldg(b4 + q);
+      } else {
+        for (int64_t q = tid; q < count; q += kGatherThreads) tile[q] = base[q];
+      }
+    } else {
+      // one warp per path row, lanes over the exercise columns
+      for (int nl = warp; nl < cn; nl += kGatherThreads / 32) {
+        const T* row = P + (n0 + nl) * Td;
+        for (int r = lane; r < Ed; r += 32) tile[nl * Wt + r] = row[src[r]];
+      }
+    }
+    __syncthreads();
+    // store [E][N][d]: one warp per exercise date, lanes over (path, component)
+    for (int e = warp; e < E; e += kGatherThreads / 32) {
+      T* dst = X + ((int64_t)e * N + n0) * d;
+      for (int q = lane; q < cn * d; q += 32) {
+        const int nl = q / d, c = q - nl * d;
+        dst[q] = tile[(int64_t)nl * Wt + col[e * d + c]];
+      }
+    }
+    // column sums: replica r sums paths r, r + R, ... in the dtype
+    for (int it = tid; it < nacc; it += kGatherThreads) {
+      const int j = it % Ed, r = it / Ed;
+      const int cj = col[j];
+      T sum = T(0);
+      for (int nl = r; nl < cn; nl += R) sum += tile[(int64_t)nl * Wt + cj];
+      acc[it] = A::add(acc[it], sum);
+    }
+  }
+  __syncthreads();
+  typename A::S* out = partials + ((size_t)blockIdx.x * gridDim.y + pb) * E * kMaxDimLsm;
+  for (int j = tid; j < E * kMaxDimLsm; j += kGatherThreads) {
+    const int e = j / kMaxDimLsm, c = j % kMaxDimLsm;
+    typename A::S v = A::zero();
+    if (c < d)
+      for (int r = 0; r < R; ++r) v = A::sum(v, acc[r * Ed + e * d + c]);
+    out[j] = v;
+  }
+}
+
+template <typename T, int DM>
 struct LsmCtx {
   const tqf_lsm_args& a;
+  const T* xt;
   int b, pb, G, d;
   const int8_t* exps;  // [G][16] in shared memory (structured)
   __device__ T ratio(int i, int64_t n) const {
@@ -110,72 +327,139 @@ struct LsmCtx {
     const int64_t o = n * a.disc_stride_n + (int64_t)b * a.disc_stride_b;
     return D[(int64_t)(i + 1) * a.disc_stride_e + o] / D[(int64_t)i * a.disc_stride_e + o];
   }
-  // Exercise value at path time t (basket put) or from the caller's [N][B] array.
-  __device__ T payoff(const void* expl, int t, int64_t n, T* x) const {
+  // D[i+1]/D[i] for this path: hoisted value when the discounts do not vary by path.
+  __device__ __forceinline__ T ratio_at(int i, int64_t n, T hoisted) const {
+    return a.disc_stride_n == 0 ? hoisted : ratio(i, n);
+  }
+  // Exercise value at exercise index e (basket put on the gathered states) or
+  // from the caller's [N][B] array; x receives the states.
+  __device__ T payoff(const void* expl, int e, int64_t n, T* x) const {
     if (a.degree < 0) return static_cast<const T*>(expl)[n * a.batch + b];
-    const T* S = static_cast<const T*>(a.paths) + (((int64_t)pb * a.num_paths + n) * a.num_times + t) * d;
+    const T* S = xt + (((int64_t)pb * a.num_exercise + e) * a.num_paths + n) * d;
     T s = T(0);
-    for (int c = 0; c < d; ++c) {
-      x[c] = S[c];
-      s += x[c];
-    }
+#pragma unroll
+    for (int c = 0; c < DM; ++c)
+      if (c < d) {
+        x[c] = S[c];
+        s += x[c];
+      }
     const T K = static_cast<const T*>(a.strikes)[b];
-    const T v = K - s / (T)d;
+    const T v = K - (d == 1 ? s : s / (T)d);
     return v > T(0) ? v : T(0);
   }
   // Basis function g at the path (structured: centred powers of x).
   __device__ T basis(const void* expl, int g, int64_t n, const T* xc) const {
     if (a.degree < 0) return static_cast<const T*>(expl)[((int64_t)pb * G + g) * a.num_paths + n];
     T p = T(1);
-    for (int c = 0; c < d; ++c) p *= ipow(xc[c], (int)exps[g * kMaxDimLsm + c]);
+#pragma unroll
+    for (int c = 0; c < DM; ++c)
+      if (c < d) p *= ipow(xc[c], (int)exps[g * kMaxDimLsm + c]);
     return p;
+  }
+  // All NG basis functions (compile-time count).  One dimension: the powers
+  // 1, x, x^2, ... by repeated multiplication (the same products as ipow).
+  template <int NG>
+  __device__ __forceinline__ void basis_all(const void* expl, int64_t n, const T* xc, T* phi) const {
+    if (DM == 1 && a.degree >= 0) {
+      phi[0] = T(1);
+#pragma unroll
+      for (int g = 1; g < NG; ++g) phi[g] = phi[g - 1] * xc[0];
+    } else {
+#pragma unroll
+      for (int g = 0; g < NG; ++g) phi[g] = basis(expl, g, n, xc);
+    }
   }
 };
 
-template <typename T>
-__global__ void lsm_pass_kernel(tqf_lsm_args a, double* __restrict__ partials, const double* __restrict__ beta,
-                                const double* __restrict__ means, int C, double* __restrict__ final_partials) {
+template <typename T, int DM, int GR>
+__global__ void lsm_pass_kernel(tqf_lsm_args a, const T* __restrict__ xt, void* __restrict__ partials_raw,
+                                const double* __restrict__ beta, const double* __restrict__ means, int C) {
+  using A = Acc<T>;
+  using S = typename A::S;
+  constexpr int GN = GR > 0 ? GR : 1;                    // compile-time basis size (register mode)
+  constexpr int EN = GN * (GN + 1) / 2 + GN;              // its accumulator entries
+  S* partials = static_cast<S*>(partials_raw);
   extern __shared__ __align__(16) unsigned char smem[];
-  const int G = a.num_basis, d = a.dim, B = a.batch;
+  const int G = GR > 0 ? GR : a.num_basis, d = a.dim, B = a.batch;
   const int En = lsm_entries(G);
-  const int W = (G + 1) | 1;
-  double* phi_s = reinterpret_cast<double*>(smem);                 // [C][W]
-  double* acc_s = phi_s + (size_t)C * W;                            // [max(En, C)]
-  double* beta_s = acc_s + (En > C ? En : C);                       // [G]
-  double* red_s = beta_s + G;                                       // [64]
-  int8_t* exps_s = reinterpret_cast<int8_t*>(red_s + 64);           // [G][16]
+  const int W = lsm_row_stride(G);
+  const int nitems = En > C ? En : C;
+  T* phi_s = reinterpret_cast<T*>(smem);  // [C][W]
+  S* acc_s = reinterpret_cast<S*>(smem + (((size_t)C * W * sizeof(T) + 15) & ~(size_t)15));  // [nitems]
+  uint32_t* pair_s = reinterpret_cast<uint32_t*>(acc_s + nitems);                          // [nitems]
+  T* beta_s = reinterpret_cast<T*>(pair_s + nitems);                                       // [G]
+  T* mu_s = beta_s + G;                                                                    // [2][16]
+  double* red_s = reinterpret_cast<double*>(
+      reinterpret_cast<unsigned char*>(beta_s) + ((G + 2 * kMaxDimLsm) * sizeof(T) + 15) / 16 * 16);  // [64]
+  int8_t* exps_s = reinterpret_cast<int8_t*>(red_s + 64);  // [G][16]
   const int tid = threadIdx.x;
   const int b = blockIdx.y;
   const int pb = a.paths_batch > 1 ? b : 0;
   const int R = En >= C ? 1 : C / En;  // replicas of each accumulator entry
   const int items = En * R;
-  for (int i = tid; i < items; i += C) acc_s[i] = 0.0;
+  const int tri = G * (G + 1) / 2;
+  for (int i = tid; i < items; i += C) {
+    acc_s[i] = A::zero();
+    // entry -> (j, k): packed upper triangle row-major, then the X'y column (k = G)
+    const int e = i % En;
+    int j = 0, k = G;
+    if (e < tri) {
+      int rem = e;
+      while (rem >= G - j) {
+        rem -= G - j;
+        ++j;
+      }
+      k = j + rem;
+    } else {
+      j = e - tri;
+    }
+    pair_s[i] = (uint32_t)j | ((uint32_t)k << 16);
+  }
   if (a.upd_index >= 1)
-    for (int g = tid; g < G; g += C) beta_s[g] = beta[(size_t)b * G + g];
-  if (a.degree >= 0)
+    for (int g = tid; g < G; g += C) beta_s[g] = (T)beta[(size_t)b * G + g];
+  if (a.degree >= 0) {
     for (int i = tid; i < G * kMaxDimLsm; i += C) {
       const int g = i / kMaxDimLsm, c = i % kMaxDimLsm;
       exps_s[i] = c < d ? (int8_t)a.exponents[g * d + c] : (int8_t)0;
     }
+    const int E0 = a.num_exercise;
+    for (int i = tid; i < 2 * kMaxDimLsm; i += C) {
+      const int which = i / kMaxDimLsm, c = i % kMaxDimLsm;
+      const int idx = which == 0 ? a.upd_index : a.acc_index;
+      mu_s[i] = idx >= 1 ? (T)means[((size_t)pb * E0 + (idx - 1)) * kMaxDimLsm + c] : T(0);
+    }
+  }
   __syncthreads();
-  LsmCtx<T> ctx{a, b, pb, G, d, exps_s};
+  LsmCtx<T, DM> ctx{a, xt, b, pb, G, d, exps_s};
+  // discount ratios that do not depend on the path
+  const T r_upd = a.upd_index >= 1 && a.disc_stride_n == 0 ? ctx.ratio(a.upd_index, 0) : T(0);
+  const T r_acc = a.acc_index >= 1 && a.disc_stride_n == 0 ? ctx.ratio(a.acc_index, 0) : T(0);
+  const T r_fin = a.final_pass && a.disc_stride_n == 0 ? ctx.ratio(0, 0) : T(0);
+  // register mode: per-thread products summed in the dtype over <= kSubSum paths
+  T part[EN];
+  S acc2[EN];
+  int cnt = 0;
+#pragma unroll
+  for (int e = 0; e < EN; ++e) {
+    part[e] = T(0);
+    acc2[e] = A::zero();
+  }
   const int E = a.num_exercise;
-  const int* ex = a.exercise_times;
   T* state = static_cast<T*>(a.state);
   T* cash = state + (size_t)b * a.num_paths;
   T* vals = state + ((size_t)B + b) * a.num_paths;
   const int64_t n_cal = a.num_calibration > 0 ? a.num_calibration : a.num_paths;
   const int64_t price_from = a.num_calibration > 0 ? a.num_calibration : 0;
-  double final_acc = 0.0;
+  S final_acc = A::zero();
   const int64_t nchunks = (a.num_paths + C - 1) / C;
   for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
     const int64_t n = ch * C + tid;
     const bool valid = n < a.num_paths;
-    T x[kMaxDimLsm], xc[kMaxDimLsm];
+    T x[DM], xc[DM];
     T c = T(0), v = T(0);
     if (valid) {
       if (a.init) {
-        c = ctx.payoff(a.init_payoff, ex[E - 1], n, x);
+        c = ctx.payoff(a.init_payoff, E - 1, n, x);
         v = T(0);
       } else {
         c = cash[n];
@@ -184,113 +468,155 @@ __global__ void lsm_pass_kernel(tqf_lsm_args a, double* __restrict__ partials, c
       if (a.upd_index >= 1) {
         // continuation = relu(design . beta), exercise where payoff > continuation (lsm.py:380-400)
         const int iu = a.upd_index;
-        const int t = ex[iu - 1];
-        const T evu = ctx.payoff(a.upd_payoff, t, n, x);
+        const T evu = ctx.payoff(a.upd_payoff, iu - 1, n, x);
         if (a.degree >= 0) {
-          const double* mu = means + ((size_t)pb * E + (iu - 1)) * kMaxDimLsm;
-          for (int q = 0; q < d; ++q) xc[q] = x[q] - (T)mu[q];
+#pragma unroll
+          for (int q = 0; q < DM; ++q) xc[q] = q < d ? x[q] - mu_s[q] : T(0);
         }
         T cont = T(0);
-        for (int g = 0; g < G; ++g) cont += ctx.basis(a.upd_design, g, n, xc) * (T)beta_s[g];
+        if (GR > 0) {
+          T phi[GN];
+          ctx.template basis_all<GN>(a.upd_design, n, xc, phi);
+#pragma unroll
+          for (int g = 0; g < GN; ++g) cont += phi[g] * beta_s[g];
+        } else {
+          for (int g = 0; g < G; ++g) cont += ctx.basis(a.upd_design, g, n, xc) * beta_s[g];
+        }
         cont = cont > T(0) ? cont : T(0);
         const bool ex_now = evu > cont;
         const T vn = ex_now ? T(0) : c + v;
         c = ex_now ? evu : T(0);
-        v = ctx.ratio(iu, n) * vn;
+        v = ctx.ratio_at(iu, n, r_upd) * vn;
       }
       if (a.final_pass) {
-        if (n >= price_from) final_acc += (double)(ctx.ratio(0, n) * (c + v));
+        if (n >= price_from) final_acc = A::add(final_acc, ctx.ratio_at(0, n, r_fin) * (c + v));
       } else {
         cash[n] = c;
         vals[n] = v;
       }
     }
-    if (a.acc_index >= 1) {
+    if (GR > 0 && a.acc_index >= 1) {
+      // masked normal equations of exercise index ia (lsm.py:355-379), in registers
+      const int ia = a.acc_index;
+      if (valid && n < n_cal) {
+        const T cv = ctx.ratio_at(ia, n, r_acc) * (v + c);
+        const T eva = ctx.payoff(a.acc_payoff, ia - 1, n, x);
+        if (a.degree >= 0) {
+#pragma unroll
+          for (int q = 0; q < DM; ++q) xc[q] = q < d ? x[q] - mu_s[kMaxDimLsm + q] : T(0);
+        }
+        T phi[GN];
+        ctx.template basis_all<GN>(a.acc_design, n, xc, phi);
+        const bool use = eva > T(0);
+#pragma unroll
+        for (int g = 0; g < GN; ++g) phi[g] = use ? phi[g] : T(0);
+        int e = 0;
+#pragma unroll
+        for (int j = 0; j < GN; ++j)
+#pragma unroll
+          for (int k = j; k < GN; ++k) part[e++] += phi[j] * phi[k];
+#pragma unroll
+        for (int j = 0; j < GN; ++j) part[e++] += phi[j] * cv;
+        if (++cnt == kSubSum) {
+#pragma unroll
+          for (int q = 0; q < EN; ++q) {
+            acc2[q] = A::add(acc2[q], part[q]);
+            part[q] = T(0);
+          }
+          cnt = 0;
+        }
+      }
+    } else if (a.acc_index >= 1) {
       // masked normal equations of exercise index ia (lsm.py:355-379)
       const int ia = a.acc_index;
-      double* row = phi_s + (size_t)tid * W;
+      T* row = phi_s + (size_t)tid * W;
       if (valid) {
-        const int t = ex[ia - 1];
-        const T cv = ctx.ratio(ia, n) * (v + c);
-        const T eva = ctx.payoff(a.acc_payoff, t, n, x);
+        const T cv = ctx.ratio_at(ia, n, r_acc) * (v + c);
+        const T eva = ctx.payoff(a.acc_payoff, ia - 1, n, x);
         const bool use = eva > T(0) && n < n_cal;
         if (a.degree >= 0) {
-          const double* mu = means + ((size_t)pb * E + (ia - 1)) * kMaxDimLsm;
-          for (int q = 0; q < d; ++q) xc[q] = x[q] - (T)mu[q];
+#pragma unroll
+          for (int q = 0; q < DM; ++q) xc[q] = q < d ? x[q] - mu_s[kMaxDimLsm + q] : T(0);
         }
-        for (int g = 0; g < G; ++g) row[g] = use ? (double)ctx.basis(a.acc_design, g, n, xc) : 0.0;
-        row[G] = n < n_cal ? (double)cv : 0.0;
+        for (int g = 0; g < G; ++g) row[g] = use ? ctx.basis(a.acc_design, g, n, xc) : T(0);
+        row[G] = n < n_cal ? cv : T(0);
       } else {
-        for (int g = 0; g <= G; ++g) row[g] = 0.0;
+        for (int g = 0; g <= G; ++g) row[g] = T(0);
       }
       __syncthreads();
       for (int it = tid; it < items; it += C) {
-        const int e = it % En, r = it / En;
-        int j, k;
-        if (e < G * (G + 1) / 2) {
-          sym_pair(e, G, j, k);
-        } else {
-          j = e - G * (G + 1) / 2;
-          k = G;
+        const int r = it / En;
+        const int j = (int)(pair_s[it] & 0xFFFFu), k = (int)(pair_s[it] >> 16);
+        S s = A::zero();
+        int p = r;
+        while (p < C) {
+          T part = T(0);
+          for (int q = 0; q < kSubSum && p < C; ++q, p += R) part += phi_s[(size_t)p * W + j] * phi_s[(size_t)p * W + k];
+          s = A::add(s, part);
         }
-        double s = 0.0;
-        for (int p = r; p < C; p += R) s += phi_s[(size_t)p * W + j] * phi_s[(size_t)p * W + k];
-        acc_s[it] += s;
+        acc_s[it] = A::sum(acc_s[it], s);
       }
       __syncthreads();
     }
   }
-  if (a.acc_index >= 1) {
-    double* out = partials + ((size_t)blockIdx.x * B + b) * En;
+  if (GR > 0 && a.acc_index >= 1) {
+    // flush, then a fixed-order block reduction (warp shuffles, then warps in order)
+    S* red = acc_s;  // [C/32][EN]
+#pragma unroll
+    for (int q = 0; q < EN; ++q) {
+      S t = A::add(acc2[q], part[q]);
+      for (int o = 16; o > 0; o >>= 1) t = A::sum(t, A::shfl_down(t, o));
+      if ((tid & 31) == 0) red[(tid >> 5) * EN + q] = t;
+    }
+    __syncthreads();
+    S* out = partials + ((size_t)blockIdx.x * B + b) * EN;
+    for (int q = tid; q < EN; q += C) {
+      S t = A::zero();
+      for (int w = 0; w < C / 32; ++w) t = A::sum(t, red[w * EN + q]);
+      out[q] = t;
+    }
+  } else if (a.acc_index >= 1) {
+    S* out = partials + ((size_t)blockIdx.x * B + b) * En;
     for (int e = tid; e < En; e += C) {
-      double s = 0.0;
-      for (int r = 0; r < R; ++r) s += acc_s[r * En + e];
+      S s = A::zero();
+      for (int r = 0; r < R; ++r) s = A::sum(s, acc_s[r * En + e]);
       out[e] = s;
     }
   }
   if (a.final_pass) {
     // fixed-order block sum
-    for (int o = 16; o > 0; o >>= 1) final_acc += __shfl_down_sync(0xffffffffu, final_acc, o);
-    if ((tid & 31) == 0) red_s[tid >> 5] = final_acc;
+    for (int o = 16; o > 0; o >>= 1) final_acc = A::sum(final_acc, A::shfl_down(final_acc, o));
+    S* red = reinterpret_cast<S*>(red_s);
+    if ((tid & 31) == 0) red[tid >> 5] = final_acc;
     __syncthreads();
     if (tid == 0) {
-      double s = 0.0;
-      for (int w = 0; w < C / 32; ++w) s += red_s[w];
-      final_partials[(size_t)blockIdx.x * B + b] = s;
+      S s = A::zero();
+      for (int w = 0; w < C / 32; ++w) s = A::sum(s, red[w]);
+      partials[(size_t)blockIdx.x * B + b] = s;
     }
   }
 }
 
-// Column sums of the paths at every exercise time: partial [gx][Bp][E][16].
+template <typename T, int DM>
+__host__ inline void* pass_kernel_dm(int G) {
+  if constexpr (DM <= 2) {
+    switch (G) {
+      case 2: return reinterpret_cast<void*>(&lsm_pass_kernel<T, DM, 2>);
+      case 3: return reinterpret_cast<void*>(&lsm_pass_kernel<T, DM, 3>);
+      case 4: return reinterpret_cast<void*>(&lsm_pass_kernel<T, DM, 4>);
+      case 5: return reinterpret_cast<void*>(&lsm_pass_kernel<T, DM, 5>);
+      default: break;
+    }
+  }
+  return reinterpret_cast<void*>(&lsm_pass_kernel<T, DM, 0>);
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) lsm_means_kernel(tqf_lsm_args a, double* __restrict__ partials) {
-  const int e = blockIdx.y % a.num_exercise;
-  const int pb = blockIdx.y / a.num_exercise;
-  const int d = a.dim;
-  const int t = a.exercise_times[e];
-  __shared__ double red[8][kMaxDimLsm];
-  double s[kMaxDimLsm];
-#pragma unroll
-  for (int c = 0; c < kMaxDimLsm; ++c) s[c] = 0.0;
-  const T* P = static_cast<const T*>(a.paths);
-  for (int64_t n = (int64_t)blockIdx.x * 256 + threadIdx.x; n < a.num_paths; n += (int64_t)gridDim.x * 256) {
-    const T* S = P + (((int64_t)pb * a.num_paths + n) * a.num_times + t) * d;
-#pragma unroll
-    for (int c = 0; c < kMaxDimLsm; ++c)
-      if (c < d) s[c] += (double)S[c];
-  }
-#pragma unroll
-  for (int c = 0; c < kMaxDimLsm; ++c) {
-    double v = s[c];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][c] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < kMaxDimLsm) {
-    double v = 0.0;
-    for (int w = 0; w < 8; ++w) v += red[w][threadIdx.x];
-    partials[((size_t)blockIdx.x * gridDim.y + blockIdx.y) * kMaxDimLsm + threadIdx.x] = v;
-  }
+__host__ inline void* pass_kernel_for(int d, int G) {
+  if (d <= 1) return pass_kernel_dm<T, 1>(G);
+  if (d <= 2) return pass_kernel_dm<T, 2>(G);
+  if (d <= 4) return pass_kernel_dm<T, 4>(G);
+  return pass_kernel_dm<T, 16>(G);
 }
 
 __global__ void lsm_scale_kernel(double* __restrict__ v, int n, double s) {
@@ -298,38 +624,110 @@ __global__ void lsm_scale_kernel(double* __restrict__ v, int n, double s) {
   if (i < n) v[i] *= s;
 }
 
+// Jacobi rotation (c, s) for the symmetric 2x2 block (app, apq; apq, aqq)
+// (Golub & Van Loan, sym.schur2).  The angle only has to shrink apq, so it is
+// computed in FP32 from the entries scaled by sc (a power of two); (c, s) are
+// then renormalised in FP64 to c^2 + s^2 = 1 with a second-order correction
+// (|c^2 + s^2 - 1| ~ 1e-7 before, ~1e-21 after), keeping the rotation
+// orthogonal to FP64 precision without FP64 division or square root.  The
+// residual apq (~1e-7 of its old value) is removed by the following sweeps.
+__device__ __forceinline__ void jacobi_cs(double app, double aqq, double apq, double sc, double& c, double& s) {
+  c = 1.0;
+  s = 0.0;
+  const float fp = (float)(apq * sc);
+  if (fp == 0.f) return;
+  const float fd = (float)((aqq - app) * sc);
+  const float th = fd / (2.f * fp);
+  const float ath = fabsf(th);
+  float t;
+  if (ath > 1e18f)
+    t = 0.5f / th;
+  else
+    t = copysignf(1.f, th) / (ath + sqrtf(fmaf(th, th, 1.f)));
+  const float cf = rsqrtf(fmaf(t, t, 1.f));
+  c = (double)cf;
+  s = (double)(t * cf);
+  const double dl = fma(c, c, s * s) - 1.0;
+  const double f = 1.0 - dl * (0.5 - 0.375 * dl);
+  c *= f;
+  s *= f;
+}
+
 // One CTA per batch member: A = X'X (packed) -> Jacobi eigen-decomposition
 // A = V diag(l) V^T; beta = V diag(l+) V^T (X'y), l+ = 1/l where |l| > cutoff.
+// Parallel cyclic Jacobi: each round applies G/2 disjoint rotations (round-
+// robin pairing), columns then rows.  One warp for <= 16 basis functions
+// (V in shared memory), 256 threads above (V in the workspace).
+template <int GC>
 __global__ void __launch_bounds__(kSolveThreads)
-    lsm_solve_kernel(const double* __restrict__ sums, int G, double rcond, double* __restrict__ beta,
-                     double* __restrict__ Vg) {
+    lsm_solve_kernel(const double* __restrict__ sums, int Gr, double rcond, double* __restrict__ beta,
+                     double* __restrict__ Vg, int warm) {
   extern __shared__ __align__(16) unsigned char smem[];
+  const int G = GC > 0 ? GC : Gr;  // compile-time size for small systems (constant index arithmetic)
   const int P = G + 1;  // row stride of A
+  const int nt = blockDim.x;
   double* A = reinterpret_cast<double*>(smem);  // [G][G+1]
   double* rhs = A + (size_t)G * P;               // [G]
   double* w = rhs + G;                           // [G]
   double* cs = w + G;                            // [2][kMaxBasis/2]
   int* pq = reinterpret_cast<int*>(cs + kMaxBasis);  // [2][kMaxBasis/2]
   double* red = reinterpret_cast<double*>(pq + kMaxBasis);  // [kSolveThreads/32][2]
+  double* Vs = red + kSolveThreads / 32 * 2;                // [G][G] when G <= 16
+  double* Tm = Vs + (G <= 16 ? G * G : 0);                  // [G][G+1] when warm
   const int b = blockIdx.x, tid = threadIdx.x;
   const int En = lsm_entries(G);
   const double* s = sums + (size_t)b * En;
-  double* V = Vg + (size_t)b * G * G;
+  double* Vb = Vg + (size_t)b * G * G;  // eigenvectors kept between exercise dates
+  double* V = G <= 16 ? Vs : Vb;
   const int tri = G * (G + 1) / 2;
-  for (int e = tid; e < tri; e += kSolveThreads) {
-    int j, k;
-    sym_pair(e, G, j, k);
+  for (int e = tid; e < tri; e += nt) {
+    int j = 0, rem = e;
+    while (rem >= G - j) {
+      rem -= G - j;
+      ++j;
+    }
+    const int k = j + rem;
     A[j * P + k] = s[e];
     A[k * P + j] = s[e];
   }
-  for (int j = tid; j < G; j += kSolveThreads) rhs[j] = s[tri + j];
-  for (int i = tid; i < G * G; i += kSolveThreads) V[i] = (i / G == i % G) ? 1.0 : 0.0;
+  for (int j = tid; j < G; j += nt) rhs[j] = s[tri + j];
+  if (warm) {
+    // warm start from the previous exercise date's eigenvectors: A <- V^T A V
+    if (G <= 16)
+      for (int i = tid; i < G * G; i += nt) V[i] = Vb[i];
+    __syncthreads();
+    for (int it = tid; it < G * G; it += nt) {
+      const int i = it / G, j = it % G;
+      double x = 0.0;
+      for (int k = 0; k < G; ++k) x = fma(A[i * P + k], V[k * G + j], x);
+      Tm[i * P + j] = x;
+    }
+    __syncthreads();
+    for (int it = tid; it < G * G; it += nt) {
+      const int i = it / G, j = it % G;
+      double x = 0.0;
+      for (int k = 0; k < G; ++k) x = fma(V[k * G + i], Tm[k * P + j], x);
+      A[i * P + j] = x;
+    }
+    __syncthreads();
+    // exact symmetry
+    for (int it = tid; it < G * G; it += nt) {
+      const int i = it / G, j = it % G;
+      if (i < j) {
+        const double m = 0.5 * (A[i * P + j] + A[j * P + i]);
+        A[i * P + j] = m;
+        A[j * P + i] = m;
+      }
+    }
+  } else {
+    for (int i = tid; i < G * G; i += nt) V[i] = (i / G == i % G) ? 1.0 : 0.0;
+  }
   __syncthreads();
   const int Pe = G + (G & 1);
   const int half = Pe / 2;
   for (int sweep = 0; sweep < kMaxJacobiSweeps && G > 1; ++sweep) {
     double off = 0.0, tot = 0.0;
-    for (int i = tid; i < G * G; i += kSolveThreads) {
+    for (int i = tid; i < G * G; i += nt) {
       const double x = A[(i / G) * P + i % G];
       tot += x * x;
       if (i / G != i % G) off += x * x;
@@ -344,32 +742,24 @@ __global__ void __launch_bounds__(kSolveThreads)
     }
     __syncthreads();
     double OFF = 0.0, TOT = 0.0;
-    for (int q = 0; q < kSolveThreads / 32; ++q) {
+    for (int q = 0; q < nt / 32; ++q) {
       OFF += red[q * 2];
       TOT += red[q * 2 + 1];
     }
     __syncthreads();
     if (OFF <= 1e-30 * TOT || OFF == 0.0) break;
+    int ex2;
+    frexp(TOT, &ex2);
+    const double sc = ldexp(1.0, -(ex2 / 2));  // power of two: entries * sc = O(1)
     for (int r = 0; r < Pe - 1; ++r) {
+      // round-robin pairing: round r pairs (r + k, r - k) mod (Pe - 1), k = 0 with the last index
       if (tid < half) {
         const int k = tid;
-        int i1 = (r + k) % (Pe - 1);
-        int i2 = k == 0 ? Pe - 1 : (Pe - 1 - k + r) % (Pe - 1);
+        const int i1 = (r + k) % (Pe - 1);
+        const int i2 = k == 0 ? Pe - 1 : (Pe - 1 - k + r) % (Pe - 1);
         const int p = i1 < i2 ? i1 : i2, q = i1 < i2 ? i2 : i1;
         double c = 1.0, sn = 0.0;
-        if (q < G) {
-          const double apq = A[p * P + q];
-          if (apq != 0.0) {
-            const double theta = (A[q * P + q] - A[p * P + p]) / (2.0 * apq);
-            double t;
-            if (fabs(theta) > 1e150)
-              t = 0.5 / theta;
-            else
-              t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(1.0 + theta * theta));
-            c = 1.0 / sqrt(1.0 + t * t);
-            sn = t * c;
-          }
-        }
+        if (q < G) jacobi_cs(A[p * P + p], A[q * P + q], A[p * P + q], sc, c, sn);
         cs[2 * k] = c;
         cs[2 * k + 1] = sn;
         pq[2 * k] = p;
@@ -377,7 +767,7 @@ __global__ void __launch_bounds__(kSolveThreads)
       }
       __syncthreads();
       // A <- A J (columns p, q)
-      for (int it = tid; it < G * half; it += kSolveThreads) {
+      for (int it = tid; it < G * half; it += nt) {
         const int i = it / half, k = it % half;
         const int p = pq[2 * k], q = pq[2 * k + 1];
         if (q < 0) continue;
@@ -388,7 +778,7 @@ __global__ void __launch_bounds__(kSolveThreads)
       }
       __syncthreads();
       // A <- J^T A (rows p, q)
-      for (int it = tid; it < G * half; it += kSolveThreads) {
+      for (int it = tid; it < G * half; it += nt) {
         const int k = it / G, j = it % G;
         const int p = pq[2 * k], q = pq[2 * k + 1];
         if (q < 0) continue;
@@ -398,7 +788,7 @@ __global__ void __launch_bounds__(kSolveThreads)
         A[q * P + j] = sn * apj + c * aqj;
       }
       // V <- V J
-      for (int it = tid; it < G * half; it += kSolveThreads) {
+      for (int it = tid; it < G * half; it += nt) {
         const int i = it / half, k = it % half;
         const int p = pq[2 * k], q = pq[2 * k + 1];
         if (q < 0) continue;
@@ -415,22 +805,28 @@ __global__ void __launch_bounds__(kSolveThreads)
   double lmax = 0.0;
   for (int j = 0; j < G; ++j) lmax = fmax(lmax, fabs(A[j * P + j]));
   const double cutoff = rcond * lmax;
-  for (int j = tid; j < G; j += kSolveThreads) {
+  for (int j = tid; j < G; j += nt) {
     double u = 0.0;
     for (int i = 0; i < G; ++i) u += V[i * G + j] * rhs[i];
     const double l = A[j * P + j];
     w[j] = fabs(l) > cutoff && l != 0.0 ? u / l : 0.0;
   }
   __syncthreads();
-  for (int i = tid; i < G; i += kSolveThreads) {
+  for (int i = tid; i < G; i += nt) {
     double x = 0.0;
     for (int j = 0; j < G; ++j) x += V[i * G + j] * w[j];
     beta[(size_t)b * G + i] = x;
   }
+  if (G <= 16)
+    for (int i = tid; i < G * G; i += nt) Vb[i] = V[i];
 }
 
+constexpr int kMaxWarmBasis = 64;  // warm start needs a second [G][G+1] buffer
+
 size_t solve_smem(int G) {
-  return (size_t)G * (G + 1) * 8 + 2 * (size_t)G * 8 + kMaxBasis * 8 + kMaxBasis * 4 + kSolveThreads / 32 * 16;
+  const size_t base =
+      (size_t)G * (G + 1) * 8 + 2 * (size_t)G * 8 + kMaxBasis * 8 + kMaxBasis * 4 + kSolveThreads / 32 * 16;
+  return base + (G <= 16 ? (size_t)G * G * 8 : 0) + (G <= kMaxWarmBasis ? (size_t)G * (G + 1) * 8 : 0);
 }
 
 int check_args(const tqf_lsm_args* a, const char* who) {
@@ -447,7 +843,10 @@ int check_args(const tqf_lsm_args* a, const char* who) {
     TQF_REQUIRE(a->paths && a->strikes && a->exponents, "%s: structured mode needs paths, strikes, exponents",
                 who);
     TQF_REQUIRE(a->degree <= 127, "%s: degree too large", who);
+    TQF_REQUIRE(lsm_gather_chunk(*a) >= 1, "%s: num_exercise * dim too large for one gather tile", who);
+    TQF_REQUIRE(a->paths_batch <= 65535, "%s: paths batch too large", who);
   }
+  TQF_REQUIRE(a->batch <= 65535, "%s: batch too large", who);
   TQF_REQUIRE(a->workspace && a->workspace_bytes >= lsm_layout(*a).total, "%s: workspace too small", who);
   return TQF_OK;
 }
@@ -457,65 +856,88 @@ int launch_pass(const tqf_lsm_args& a, cudaStream_t s) {
   const WsLayout L = lsm_layout(a);
   unsigned char* ws = static_cast<unsigned char*>(a.workspace);
   const int G = a.num_basis;
-  const int C = lsm_chunk(G);
-  const size_t smem = lsm_pass_smem(G, C);
-  set_smem_config(lsm_pass_kernel<T>, smem);
-  const int gx = lsm_grid_x(a, C);
+  int C = 256;
+  size_t smem = 0;
+  const int gx = lsm_pass_grid<T>(a, &C, &smem);
   dim3 grid((unsigned)gx, (unsigned)a.batch);
-  double* partials = reinterpret_cast<double*>(ws + L.partials);
-  lsm_pass_kernel<T><<<grid, C, smem, s>>>(a, partials, reinterpret_cast<const double*>(ws + L.beta),
-                                           reinterpret_cast<const double*>(ws + L.means), C, partials);
-  int rc = check_launch("lsm_pass_kernel");
+  using S = typename Acc<T>::S;
+  S* partials = reinterpret_cast<S*>(ws + L.partials);
+  const T* xt = reinterpret_cast<const T*>(ws + L.xt);
+  const double* beta = reinterpret_cast<const double*>(ws + L.beta);
+  const double* means = reinterpret_cast<const double*>(ws + L.means);
+  const int d = a.degree >= 0 ? a.dim : 1;
+  void* k = pass_kernel_for<T>(d, G);
+  void* params[] = {const_cast<tqf_lsm_args*>(&a), const_cast<T**>(&xt), &partials, const_cast<double**>(&beta),
+                    const_cast<double**>(&means), &C};
+  int rc = check_cuda(cudaLaunchKernel(k, grid, dim3((unsigned)C), params, smem, s), "lsm_pass_kernel launch");
   if (rc) return rc;
-  if (a.final_pass) return reduce_partials(partials, gx, a.batch, a.out, s);
-  if (a.acc_index >= 1)
-    return reduce_partials(partials, gx, a.batch * lsm_entries(G), reinterpret_cast<double*>(ws + L.sums), s);
+  rc = check_launch("lsm_pass_kernel");
+  if (rc) return rc;
+  if (a.final_pass) {
+    lsm_reduce_kernel<T><<<(a.batch + 31) / 32, 1024, 0, s>>>(partials, gx, a.batch, a.out);
+    return check_launch("lsm_reduce_kernel");
+  }
+  if (a.acc_index >= 1) {
+    const int width = a.batch * lsm_entries(G);
+    lsm_reduce_kernel<T><<<(width + 31) / 32, 1024, 0, s>>>(partials, gx, width,
+                                                            reinterpret_cast<double*>(ws + L.sums));
+    return check_launch("lsm_reduce_kernel");
+  }
   return TQF_OK;
 }
 
 template <typename T>
-int launch_means(const tqf_lsm_args& a, cudaStream_t s) {
+int launch_gather(const tqf_lsm_args& a, cudaStream_t s) {
   const WsLayout L = lsm_layout(a);
   unsigned char* ws = static_cast<unsigned char*>(a.workspace);
-  const int rows = a.num_exercise * a.paths_batch;
-  int64_t gx = (a.num_paths + 255) / 256;
-  if (gx > num_sms() * 2) gx = num_sms() * 2;
-  TQF_REQUIRE(rows <= 65535, "tqf_lsm_means: too many exercise times");
-  double* part = reinterpret_cast<double*>(ws + L.mean_partials);
+  int full = 0;
+  const int Cn = lsm_gather_chunk(a, &full);
+  const int gx = lsm_gather_grid(a);
+  const size_t smem = lsm_gather_smem(a, Cn, full);
+  set_smem_config(lsm_gather_kernel<T>, smem);
+  using S = typename Acc<T>::S;
+  S* part = reinterpret_cast<S*>(ws + L.mean_partials);
   double* means = reinterpret_cast<double*>(ws + L.means);
-  lsm_means_kernel<T><<<dim3((unsigned)gx, (unsigned)rows), 256, 0, s>>>(a, part);
-  int rc = check_launch("lsm_means_kernel");
+  lsm_gather_kernel<T><<<dim3((unsigned)gx, (unsigned)a.paths_batch), kGatherThreads, smem, s>>>(
+      a, reinterpret_cast<T*>(ws + L.xt), part, Cn, full);
+  int rc = check_launch("lsm_gather_kernel");
   if (rc) return rc;
-  rc = reduce_partials(part, (int)gx, rows * kMaxDimLsm, means, s);
+  const int width = a.paths_batch * a.num_exercise * kMaxDimLsm;
+  lsm_reduce_kernel<T><<<(width + 31) / 32, 1024, 0, s>>>(part, gx, width, means);
+  rc = check_launch("lsm_reduce_kernel");
   if (rc) return rc;
-  const int n = rows * kMaxDimLsm;
-  lsm_scale_kernel<<<(n + 255) / 256, 256, 0, s>>>(means, n, 1.0 / (double)a.num_paths);
+  lsm_scale_kernel<<<(width + 255) / 256, 256, 0, s>>>(means, width, 1.0 / (double)a.num_paths);
   return check_launch("lsm_scale_kernel");
 }
 
-}  // namespace
-}  // namespace tqf
-
-using namespace tqf;
-
-extern "C" size_t tqf_lsm_workspace_bytes(const tqf_lsm_args* a) {
-  if (!a) return 0;
-  return lsm_layout(*a).total;
+int launch_solve(const tqf_lsm_args& a, cudaStream_t s) {
+  const WsLayout L = lsm_layout(a);
+  unsigned char* ws = static_cast<unsigned char*>(a.workspace);
+  const int G = a.num_basis;
+  const double eps = a.dtype == TQF_F32 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
+  const double rcond = 10.0 * G * eps;
+  const size_t smem = solve_smem(G);
+  // warm start from the previous date's eigenvectors (every solve after the first)
+  const int warm = (G <= kMaxWarmBasis && a.acc_index >= 1 && a.acc_index < a.num_exercise - 1) ? 1 : 0;
+  void (*k)(const double*, int, double, double*, double*, int) = lsm_solve_kernel<0>;
+  switch (G) {
+    case 2: k = lsm_solve_kernel<2>; break;
+    case 3: k = lsm_solve_kernel<3>; break;
+    case 4: k = lsm_solve_kernel<4>; break;
+    case 5: k = lsm_solve_kernel<5>; break;
+    case 6: k = lsm_solve_kernel<6>; break;
+    case 8: k = lsm_solve_kernel<8>; break;
+    case 9: k = lsm_solve_kernel<9>; break;
+    default: break;
+  }
+  set_smem_config(k, smem);
+  k<<<a.batch, G <= 16 ? 32 : kSolveThreads, smem, s>>>(reinterpret_cast<const double*>(ws + L.sums), G, rcond,
+                                                        reinterpret_cast<double*>(ws + L.beta),
+                                                        reinterpret_cast<double*>(ws + L.eig_v), warm);
+  return check_launch("lsm_solve_kernel");
 }
 
-extern "C" int tqf_lsm_means(const tqf_lsm_args* a, void* stream) {
-  clear_error();
-  int rc = check_args(a, "tqf_lsm_means");
-  if (rc) return rc;
-  TQF_REQUIRE(a->degree >= 0, "tqf_lsm_means: structured basis only");
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return a->dtype == TQF_F32 ? launch_means<float>(*a, s) : launch_means<double>(*a, s);
-}
-
-extern "C" int tqf_lsm_pass(const tqf_lsm_args* a, void* stream) {
-  clear_error();
-  int rc = check_args(a, "tqf_lsm_pass");
-  if (rc) return rc;
+int check_pass(const tqf_lsm_args* a) {
   TQF_REQUIRE(a->upd_index < a->num_exercise && a->acc_index < a->num_exercise,
               "tqf_lsm_pass: exercise index out of range");
   TQF_REQUIRE(!a->final_pass || a->out, "tqf_lsm_pass: final pass needs out");
@@ -525,6 +947,34 @@ extern "C" int tqf_lsm_pass(const tqf_lsm_args* a, void* stream) {
     TQF_REQUIRE(a->upd_index < 1 || (a->upd_payoff && a->upd_design), "tqf_lsm_pass: explicit update needs data");
     TQF_REQUIRE(a->acc_index < 1 || (a->acc_payoff && a->acc_design), "tqf_lsm_pass: explicit accumulate needs data");
   }
+  return TQF_OK;
+}
+
+}  // namespace
+}  // namespace tqf
+
+using namespace tqf;
+
+extern "C" size_t tqf_lsm_workspace_bytes(const tqf_lsm_args* a) {
+  if (!a || a->num_basis < 1 || a->num_basis > kMaxBasis) return 0;
+  return lsm_layout(*a).total;
+}
+
+extern "C" int tqf_lsm_gather(const tqf_lsm_args* a, void* stream) {
+  clear_error();
+  int rc = check_args(a, "tqf_lsm_gather");
+  if (rc) return rc;
+  TQF_REQUIRE(a->degree >= 0, "tqf_lsm_gather: structured basis only");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a->dtype == TQF_F32 ? launch_gather<float>(*a, s) : launch_gather<double>(*a, s);
+}
+
+extern "C" int tqf_lsm_pass(const tqf_lsm_args* a, void* stream) {
+  clear_error();
+  int rc = check_args(a, "tqf_lsm_pass");
+  if (rc) return rc;
+  rc = check_pass(a);
+  if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   return a->dtype == TQF_F32 ? launch_pass<float>(*a, s) : launch_pass<double>(*a, s);
 }
@@ -533,16 +983,42 @@ extern "C" int tqf_lsm_solve(const tqf_lsm_args* a, void* stream) {
   clear_error();
   int rc = check_args(a, "tqf_lsm_solve");
   if (rc) return rc;
-  const WsLayout L = lsm_layout(*a);
-  unsigned char* ws = static_cast<unsigned char*>(a->workspace);
-  const int G = a->num_basis;
-  const double eps = a->dtype == TQF_F32 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
-  const double rcond = 10.0 * G * eps;
-  const size_t smem = solve_smem(G);
-  set_smem_config(lsm_solve_kernel, smem);
+  return launch_solve(*a, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tqf_lsm_price(const tqf_lsm_args* args, void* stream) {
+  clear_error();
+  int rc = check_args(args, "tqf_lsm_price");
+  if (rc) return rc;
+  TQF_REQUIRE(args->degree >= 0, "tqf_lsm_price: structured basis and payoff only (explicit mode runs per pass)");
+  TQF_REQUIRE(args->out, "tqf_lsm_price: null out");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  lsm_solve_kernel<<<a->batch, kSolveThreads, smem, s>>>(reinterpret_cast<const double*>(ws + L.sums), G, rcond,
-                                                         reinterpret_cast<double*>(ws + L.beta),
-                                                         reinterpret_cast<double*>(ws + L.eig_v));
-  return check_launch("lsm_solve_kernel");
+  tqf_lsm_args a = *args;
+  const bool f32 = a.dtype == TQF_F32;
+  rc = f32 ? launch_gather<float>(a, s) : launch_gather<double>(a, s);
+  if (rc) return rc;
+  auto pass = [&](int init, int upd, int acc, int fin) {
+    a.init = init;
+    a.upd_index = upd;
+    a.acc_index = acc;
+    a.final_pass = fin;
+    return f32 ? launch_pass<float>(a, s) : launch_pass<double>(a, s);
+  };
+  const int E = a.num_exercise;
+  if (E == 1) {
+    rc = pass(1, 0, 0, 1);
+  } else {
+    rc = pass(1, 0, E - 1, 0);
+    if (!rc) rc = launch_solve(a, s);
+    for (int i = E - 1; i > 1 && !rc; --i) {
+      rc = pass(0, i, i - 1, 0);
+      if (!rc) rc = launch_solve(a, s);
+    }
+    if (!rc) rc = pass(0, 1, 0, 1);
+  }
+  if (rc) return rc;
+  const int64_t count = a.num_calibration > 0 ? a.num_paths - a.num_calibration : a.num_paths;
+  TQF_REQUIRE(count >= 1, "tqf_lsm_price: no paths left to price after calibration");
+  lsm_scale_kernel<<<(a.batch + 255) / 256, 256, 0, s>>>(a.out, a.batch, 1.0 / (double)count);
+  return check_launch("lsm_scale_kernel");
 }

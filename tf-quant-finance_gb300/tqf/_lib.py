@@ -343,7 +343,8 @@ _SIGNATURES = {
     "tqf_cholesky_f64": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp, c_vp]),
     "tqf_mvgbm_paths": (ctypes.c_int, [ctypes.POINTER(MvgbmArgs), c_vp]),
     "tqf_lsm_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(LsmArgs)]),
-    "tqf_lsm_means": (ctypes.c_int, [ctypes.POINTER(LsmArgs), c_vp]),
+    "tqf_lsm_gather": (ctypes.c_int, [ctypes.POINTER(LsmArgs), c_vp]),
+    "tqf_lsm_price": (ctypes.c_int, [ctypes.POINTER(LsmArgs), c_vp]),
     "tqf_lsm_pass": (ctypes.c_int, [ctypes.POINTER(LsmArgs), c_vp]),
     "tqf_lsm_solve": (ctypes.c_int, [ctypes.POINTER(LsmArgs), c_vp]),
     "tqf_basket_price": (ctypes.c_int, [ctypes.POINTER(BasketArgs), c_vp]),

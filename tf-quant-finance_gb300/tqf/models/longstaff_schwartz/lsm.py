@@ -3,12 +3,13 @@
 
 ``least_square_mc`` keeps the reference's signature and backward loop over
 exercise dates.  With the reference's own basis and payoff factories
-(``make_polynomial_basis``, ``make_basket_put_payoff``) every date is one
-fused pass over the paths (``tqf_lsm_pass``: previous date's exercise update
-plus this date's masked FP64 normal equations, the design built per path in
-the kernel) and one pseudo-inverse solve (``tqf_lsm_solve``).  Any other
-callables are evaluated by the caller's torch code once per date and their
-[N, B] payoffs / [B, G, N] designs are fed to the same kernels.
+(``make_polynomial_basis``, ``make_basket_put_payoff``) the whole algorithm is
+one native call (``tqf_lsm_price``): a gather pass, then per date one fused
+pass over the paths (previous date's exercise update plus this date's masked
+FP64 normal equations, the design built per path in the kernel) and one
+pseudo-inverse solve.  Any other callables are evaluated by the caller's torch
+code once per date and their [N, B] payoffs / [B, G, N] designs are fed to the
+same kernels through ``tqf_lsm_pass`` / ``tqf_lsm_solve``.
 """
 
 from __future__ import annotations
@@ -198,7 +199,8 @@ def least_square_mc(sample_paths, exercise_times, payoff_fn, basis_fn, discount_
         _lib.call("tqf_lsm_pass", a, stream)
 
     if structured:
-        _lib.call("tqf_lsm_means", a, stream)
+        _lib.call("tqf_lsm_price", a, stream)  # whole backward loop in one native call
+        return out.to(td)
     if E == 1:
         run_pass(init=1, final=1)
     else:
