@@ -291,9 +291,14 @@ __global__ void __launch_bounds__(kGatherThreads)
     // store [E][N][d]: one warp per exercise date, lanes over (path, component)
     for (int e = warp; e < E; e += kGatherThreads / 32) {
       T* dst = X + ((int64_t)e * N + n0) * d;
-      for (int q = lane; q < cn * d; q += 32) {
-        const int nl = q / d, c = q - nl * d;
-        dst[q] = tile[(int64_t)nl * Wt + col[e * d + c]];
+      if (d == 1) {
+        const int ce = col[e];
+        for (int q = lane; q < cn; q += 32) dst[q] = tile[q * Wt + ce];
+      } else {
+        for (int q = lane; q < cn * d; q += 32) {
+          const int nl = q / d, c = q - nl * d;
+          dst[q] = tile[nl * Wt + col[e * d + c]];
+        }
       }
     }
     // column sums: replica r sums paths r, r + R, ... in the dtype
@@ -561,12 +566,15 @@ __global__ void lsm_pass_kernel(tqf_lsm_args a, const T* __restrict__ xt, void* 
   }
   if (GR > 0 && a.acc_index >= 1) {
     // flush, then a fixed-order block reduction (warp shuffles, then warps in order)
+    // Each thread's value (at most kSubSum products unless it was flushed) is
+    // rounded to the dtype for a pairwise warp tree (32 values); warps and CTAs
+    // are then combined in the compensated / FP64 accumulator.
     S* red = acc_s;  // [C/32][EN]
 #pragma unroll
     for (int q = 0; q < EN; ++q) {
-      S t = A::add(acc2[q], part[q]);
-      for (int o = 16; o > 0; o >>= 1) t = A::sum(t, A::shfl_down(t, o));
-      if ((tid & 31) == 0) red[(tid >> 5) * EN + q] = t;
+      T t = (T)A::value(A::add(acc2[q], part[q]));
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      if ((tid & 31) == 0) red[(tid >> 5) * EN + q] = A::add(A::zero(), t);
     }
     __syncthreads();
     S* out = partials + ((size_t)blockIdx.x * B + b) * EN;
