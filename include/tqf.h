@@ -238,6 +238,64 @@ typedef struct tqf_euler_update_args {
 
 TQF_API int tqf_euler_update(const tqf_euler_update_args* args, void* stream);
 
+/* ---- Milstein scheme (tff/models/milstein_sampling.py) ---------------------
+ * Step of _milstein_1d / _milstein_nd (milstein_sampling.py:565-593) with the
+ * Stratonovich integral approximation of _stratonovich_integral (:481-525) and
+ * the drift correction of _stratonovich_drift_update (:555-562), the grid and
+ * recording of _while_loop (:356-424).  Every step consumes
+ * dim + 3 * dim * order normals (draw dimension k = step * K + c, K that count):
+ * [0, dim) the Wiener increments, then the mu, zeta, eta blocks of dim * order
+ * each, element (component c, term r) at c * order + r.
+ *
+ * tqf_milstein_affine: the whole loop for structured coefficients
+ * a(x) = m + M x, B(x)_kj = (s0_k + s1_k x_k) C_kj (exact dB_kj/dx_i =
+ * delta_ik s1_k C_kj), step table [num_steps][4] = (dt, sqrt dt, slot, 0),
+ * dim <= 8. */
+typedef struct tqf_milstein_affine_args {
+  int32_t dtype;
+  int32_t dim;
+  int64_t num_paths;
+  int32_t num_steps;
+  int32_t x0_per_path;
+  int32_t order;             /* stratonovich_order >= 1 */
+  int32_t pad0;
+  const void* step_table;
+  const void* x0;
+  const void* drift_m;
+  const void* drift_M;
+  const void* vol_s0;
+  const void* vol_s1;
+  const void* vol_C;
+  tqf_draws draws;
+  tqf_path_output output;
+  int32_t* dev_status;
+} tqf_milstein_affine_args;
+
+TQF_API int tqf_milstein_affine(const tqf_milstein_affine_args* args, void* stream);
+
+/* One Milstein step for coefficients the caller evaluated at t_{i+1}:
+ * drift [N][d], vol [N][d][d] = B, grad [N][d(i)][d(k)][d(j)] = dB_kj/dx_i. */
+typedef struct tqf_milstein_update_args {
+  int32_t dtype;
+  int32_t dim;
+  int64_t num_paths;
+  int32_t step;
+  int32_t out_slot;
+  int32_t order;
+  int32_t num_slots;
+  double dt;
+  double sqrt_dt;
+  const void* x;
+  const void* drift;
+  const void* vol;
+  const void* grad;
+  void* x_next;
+  tqf_draws draws;
+  void* paths_out;           /* [N][num_slots][d] or NULL */
+} tqf_milstein_update_args;
+
+TQF_API int tqf_milstein_update(const tqf_milstein_update_args* args, void* stream);
+
 /* Full-truncation Euler for the Heston model in log-spot form, as the
  * reference Euler sampler runs it with drift [r - v+/2, kappa (theta - v+)]
  * and volatility [[sqrt v+, 0], [xi rho sqrt v+, xi sqrt(1-rho^2) sqrt v+]],

@@ -42,3 +42,13 @@ def basket_price_torch(spots, vols, rate, corr, weights, strike, times, draws, i
     pay = torch.clamp(B - strike if is_call else strike - B, min=0)
     T = float(t[-1])
     return torch.exp(-rate * T) * pay.mean()
+
+
+def univariate_with_draws(mean_int, volsq_int, x0, draws, dtype):
+    """Univariate GBM exact scheme (univariate_geometric_brownian_motion.py:261-318):
+    x0 exp(cumsum((int mu - int sigma^2 / 2) + sqrt(int sigma^2) z)); draws [N, k]."""
+    dt_ = np.dtype(dtype).type
+    mean_int = np.asarray(mean_int, dtype)
+    volsq_int = np.asarray(volsq_int, dtype)
+    inc = ((mean_int - volsq_int / dt_(2)) + np.sqrt(volsq_int) * np.asarray(draws, dtype)).astype(dtype)
+    return (dt_(x0) * np.exp(np.cumsum(inc, axis=-1).astype(dtype))).astype(dtype)

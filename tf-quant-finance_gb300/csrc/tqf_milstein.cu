@@ -1,0 +1,319 @@
+// Milstein scheme kernels — the GB300 replacement of
+// tff/models/milstein_sampling.py:258-671.
+//
+// milstein_affine_kernel: the whole time loop for structured coefficients
+//   a(x) = m + M x, B(x)_kj = (s0_k + s1_k x_k) C_kj, whose volatility gradient
+//   is exact (dB_kj/dx_i = delta_ik s1_k C_kj); path state, B and the
+//   Stratonovich integrals J live in registers, the step table is staged in
+//   shared memory by a bulk copy, draws come from memory or in-kernel Philox.
+// milstein_update_kernel: one step for coefficients (drift, B, dB/dx) that the
+//   caller evaluated at t_{i+1}.
+//
+// The update is the reference's, term for term (milstein_sampling.py:565-593):
+//   d = 1: x + dt a + b dW + b b' (dW^2 - dt) / 2
+//   d > 1: x + dt (a - u) + B dW + h, with
+//     u_k = sum_{i,j} dB_kj/dx_i B_ij                 (_stratonovich_drift_update)
+//     h_s = sum_{i,m} (sum_j dB_sj/dx_i B_jm) J_im     (_milstein_hot)
+//     J_ij = dt (dW_i dW_j / 2 + sqrt(rho_p) (mu_i xi_j - xi_i mu_j))
+//          + dt / (2 pi) sum_r (1/r) (zeta_ir (sqrt2 xi_j + eta_jr) - (sqrt2 xi_i + eta_ir) zeta_jr),
+//     J_ii = dW_i^2 / 2, xi = dW / sqrt(dt)             (_stratonovich_integral)
+#include "tqf_internal.cuh"
+
+// Full unrolling for the small dimension buckets only; the 8-wide bucket keeps
+// runtime loops (register arrays there would spill anyway).
+
+namespace tqf {
+namespace {
+
+constexpr int kBlock = 128;
+constexpr int kMaxDimMil = 8;
+
+template <typename T, int DM>
+struct AffineMil {
+  T m[DM], M[DM * DM], s0[DM], s1[DM], C[DM * DM];
+};
+
+// Off-diagonal Stratonovich integrals J (diagonal set to dW^2 / 2).
+template <typename T, int DM>
+__device__ __forceinline__ void stratonovich_J(int d, int order, T dt, T sqrt_dt, T sqrt_rho, const T* dw,
+                                               DrawSource<T>& src, int step, T (&J)[DM][DM]) {
+  T xi[DM], mup[DM];
+  const int p = order - 1;
+#pragma unroll(DM <= 4 ? DM : 1)
+  for (int c = 0; c < DM; ++c) {
+    xi[c] = c < d ? dw[c] / sqrt_dt : T(0);
+    mup[c] = c < d ? src.get(step, d + c * order + p) : T(0);
+  }
+  T acc[DM][DM];
+#pragma unroll(DM <= 4 ? DM : 1)
+  for (int i = 0; i < DM; ++i)
+#pragma unroll(DM <= 4 ? DM : 1)
+    for (int j = 0; j < DM; ++j) {
+      J[i][j] = dt * (dw[i] * dw[j] / T(2) + sqrt_rho * (mup[i] * xi[j] - xi[i] * mup[j]));
+      acc[i][j] = T(0);
+    }
+  const T s2 = (T)1.4142135623730951;
+  for (int r = 0; r < order; ++r) {
+    T z[DM], w[DM];
+#pragma unroll(DM <= 4 ? DM : 1)
+    for (int c = 0; c < DM; ++c) {
+      z[c] = c < d ? src.get(step, d + d * order + c * order + r) : T(0);
+      const T e = c < d ? src.get(step, d + 2 * d * order + c * order + r) : T(0);
+      w[c] = s2 * xi[c] + e;
+    }
+    const T inv = T(1) / T(r + 1);
+#pragma unroll(DM <= 4 ? DM : 1)
+    for (int i = 0; i < DM; ++i)
+#pragma unroll(DM <= 4 ? DM : 1)
+      for (int j = 0; j < DM; ++j) acc[i][j] += (z[i] * w[j] - w[i] * z[j]) * inv;
+  }
+  const T two_pi = (T)6.283185307179586;
+#pragma unroll(DM <= 4 ? DM : 1)
+  for (int i = 0; i < DM; ++i)
+#pragma unroll(DM <= 4 ? DM : 1)
+    for (int j = 0; j < DM; ++j) J[i][j] = i == j ? dw[i] * dw[i] / T(2) : J[i][j] + dt * acc[i][j] / two_pi;
+}
+
+template <typename T, int DM, int SRC>
+__global__ void __launch_bounds__(kBlock) milstein_affine_kernel(tqf_milstein_affine_args a, double rho_c,
+                                                                 int staged) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+  AffineMil<T, DM>* cf = reinterpret_cast<AffineMil<T, DM>*>(smem + 16);
+  unsigned char* tab_raw = smem + ((16 + sizeof(AffineMil<T, DM>) + 15) & ~(size_t)15);
+  const int d = a.dim, order = a.order;
+  for (int i = threadIdx.x; i < DM; i += kBlock) {
+    const bool in = i < d;
+    cf->m[i] = in ? static_cast<const T*>(a.drift_m)[i] : T(0);
+    cf->s0[i] = in ? static_cast<const T*>(a.vol_s0)[i] : T(0);
+    cf->s1[i] = in ? static_cast<const T*>(a.vol_s1)[i] : T(0);
+  }
+  for (int i = threadIdx.x; i < DM * DM; i += kBlock) {
+    const int r = i / DM, c = i % DM;
+    const bool in = r < d && c < d;
+    cf->M[i] = in ? static_cast<const T*>(a.drift_M)[r * d + c] : T(0);
+    cf->C[i] = in ? static_cast<const T*>(a.vol_C)[r * d + c] : T(0);
+  }
+  const T* table = static_cast<const T*>(a.step_table);
+  if (staged) {
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    uint32_t phase = 0;
+    if (!stage_to_smem(tab_raw, a.step_table, (uint32_t)(a.num_steps * 4 * sizeof(T)), bar, phase, a.dev_status))
+      return;
+    table = reinterpret_cast<const T*>(tab_raw);
+  } else {
+    __syncthreads();
+  }
+  const T sqrt_rho = sqrt((T)rho_c);
+  const int K = d + 3 * d * order;  // normals per step
+  T* out = static_cast<T*>(a.output.ptr);
+  const int ns = a.output.num_slots;
+  for (int64_t path = (int64_t)blockIdx.x * kBlock + threadIdx.x; path < a.num_paths;
+       path += (int64_t)gridDim.x * kBlock) {
+    T x[DM];
+    const T* x0 = static_cast<const T*>(a.x0) + (a.x0_per_path ? path * d : 0);
+#pragma unroll(DM <= 4 ? DM : 1)
+    for (int j = 0; j < DM; ++j) x[j] = j < d ? x0[j] : T(0);
+    if (a.output.init_slot >= 0) {
+      T* o = out + (path * ns + a.output.init_slot) * d;
+#pragma unroll(DM <= 4 ? DM : 1)
+      for (int j = 0; j < DM; ++j)
+        if (j < d) o[j] = x[j];
+    }
+    DrawSource<T> src(a.draws, path, K);
+    for (int i = 0; i < a.num_steps; ++i) {
+      const T dt = table[i * 4], sdt = table[i * 4 + 1];
+      const int slot = (int)table[i * 4 + 2];
+      T dw[DM], xn[DM];
+#pragma unroll(DM <= 4 ? DM : 1)
+      for (int c = 0; c < DM; ++c) dw[c] = c < d ? src.get(i, c) * sdt : T(0);
+      T lev[DM];  // s0_k + s1_k x_k
+#pragma unroll(DM <= 4 ? DM : 1)
+      for (int k = 0; k < DM; ++k) lev[k] = cf->s0[k] + cf->s1[k] * x[k];
+      if (DM == 1) {
+        const T b = lev[0] * cf->C[0], g = cf->s1[0] * cf->C[0];
+        const T drift = cf->m[0] + cf->M[0] * x[0];
+        xn[0] = x[0] + dt * drift + b * dw[0] + (b * g) * (dw[0] * dw[0] - dt) / T(2);
+      } else {
+        T J[DM][DM];
+        stratonovich_J<T, DM>(d, order, dt, sdt, sqrt_rho, dw, src, i, J);
+#pragma unroll(DM <= 4 ? DM : 1)
+        for (int k = 0; k < DM; ++k) {
+          if (k >= d) {
+            xn[k] = T(0);
+            continue;
+          }
+          T drift = cf->m[k];
+#pragma unroll(DM <= 4 ? DM : 1)
+          for (int c = 0; c < DM; ++c) drift += cf->M[k * DM + c] * x[c];
+          T u = T(0), dwi = T(0), h = T(0);
+#pragma unroll(DM <= 4 ? DM : 1)
+          for (int j = 0; j < DM; ++j) {
+            const T Bkj = lev[k] * cf->C[k * DM + j];
+            u += cf->s1[k] * cf->C[k * DM + j] * Bkj;
+            dwi += Bkj * dw[j];
+          }
+#pragma unroll(DM <= 4 ? DM : 1)
+          for (int m = 0; m < DM; ++m) {
+            T l = T(0);  // sum_j dB_kj/dx_k B_jm
+#pragma unroll(DM <= 4 ? DM : 1)
+            for (int j = 0; j < DM; ++j) l += cf->s1[k] * cf->C[k * DM + j] * (lev[j] * cf->C[j * DM + m]);
+            h += l * J[k][m];
+          }
+          xn[k] = x[k] + dt * (drift - u) + dwi + h;
+        }
+      }
+#pragma unroll(DM <= 4 ? DM : 1)
+      for (int k = 0; k < DM; ++k) x[k] = xn[k];
+      if (slot >= 0) {
+        T* o = out + (path * ns + slot) * d;
+#pragma unroll(DM <= 4 ? DM : 1)
+        for (int j = 0; j < DM; ++j)
+          if (j < d) o[j] = x[j];
+      }
+    }
+  }
+}
+
+template <typename T, int DM>
+__global__ void __launch_bounds__(kBlock) milstein_update_kernel(tqf_milstein_update_args a, double rho_c) {
+  const int64_t path = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  if (path >= a.num_paths) return;
+  const int d = a.dim, order = a.order;
+  const int K = d + 3 * d * order;
+  const T* x = static_cast<const T*>(a.x) + path * d;
+  const T* A = static_cast<const T*>(a.drift) + path * d;
+  const T* B = static_cast<const T*>(a.vol) + path * d * d;
+  const T* G = static_cast<const T*>(a.grad) + path * d * d * d;  // [i][k][j]
+  DrawSource<T> src(a.draws, path, K);
+  const T dt = (T)a.dt, sdt = (T)a.sqrt_dt;
+  T dw[DM], xn[DM];
+#pragma unroll(DM <= 4 ? DM : 1)
+  for (int c = 0; c < DM; ++c) dw[c] = c < d ? src.get(a.step, c) * sdt : T(0);
+  if (DM == 1) {
+    xn[0] = x[0] + dt * A[0] + B[0] * dw[0] + (B[0] * G[0]) * (dw[0] * dw[0] - dt) / T(2);
+  } else {
+    T J[DM][DM];
+    stratonovich_J<T, DM>(d, order, dt, sdt, sqrt((T)rho_c), dw, src, a.step, J);
+#pragma unroll(DM <= 4 ? DM : 1)
+    for (int k = 0; k < DM; ++k) {
+      if (k >= d) {
+        xn[k] = T(0);
+        continue;
+      }
+      T u = T(0), dwi = T(0), h = T(0);
+      for (int i = 0; i < d; ++i)
+        for (int j = 0; j < d; ++j) u += G[(i * d + k) * d + j] * B[i * d + j];
+      for (int j = 0; j < d; ++j) dwi += B[k * d + j] * dw[j];
+#pragma unroll(DM <= 4 ? DM : 1)
+      for (int i = 0; i < DM; ++i) {
+        if (i >= d) continue;
+#pragma unroll(DM <= 4 ? DM : 1)
+        for (int m = 0; m < DM; ++m) {
+          if (m >= d) continue;
+          T l = T(0);
+          for (int j = 0; j < d; ++j) l += G[(i * d + k) * d + j] * B[j * d + m];
+          h += l * J[i][m];
+        }
+      }
+      xn[k] = x[k] + dt * (A[k] - u) + dwi + h;
+    }
+  }
+  T* xo = static_cast<T*>(a.x_next) + path * d;
+  T* po = a.paths_out && a.out_slot >= 0 ? static_cast<T*>(a.paths_out) + (path * a.num_slots + a.out_slot) * d
+                                          : nullptr;
+#pragma unroll(DM <= 4 ? DM : 1)
+  for (int k = 0; k < DM; ++k)
+    if (k < d) {
+      xo[k] = xn[k];
+      if (po) po[k] = xn[k];
+    }
+}
+
+// 1/12 - sum_{r=1}^{order} r^-2 / (2 pi^2), the variance factor rho_p of the
+// truncated Fourier expansion (milstein_sampling.py:500-503).
+double rho_constant(int order) {
+  double s = 0.0;
+  for (int r = 1; r <= order; ++r) s += 1.0 / ((double)r * r);
+  const double pi = 3.14159265358979323846;
+  return 1.0 / 12.0 - s / 2.0 / (pi * pi);
+}
+
+template <typename T, int DM>
+int launch_affine(const tqf_milstein_affine_args& a, cudaStream_t s) {
+  const size_t tab_bytes = (size_t)a.num_steps * 4 * sizeof(T);
+  const bool staged = tab_bytes > 0 && tab_bytes <= 96 * 1024 && (reinterpret_cast<uintptr_t>(a.step_table) & 15u) == 0;
+  const size_t head = (16 + sizeof(AffineMil<T, DM>) + 15) & ~(size_t)15;
+  const size_t smem = head + (staged ? tab_bytes : 0);
+  void (*k)(tqf_milstein_affine_args, double, int) = a.draws.source == TQF_DRAWS_PHILOX
+                                                         ? milstein_affine_kernel<T, DM, TQF_DRAWS_PHILOX>
+                                                         : milstein_affine_kernel<T, DM, TQF_DRAWS_MEMORY>;
+  if (smem > 48 * 1024) set_smem_config(k, smem);
+  int occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem) != cudaSuccess || occ < 1) occ = 1;
+  int64_t grid = (a.num_paths + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)num_sms() * occ;
+  if (grid > cap) grid = cap;
+  k<<<(unsigned)grid, kBlock, smem, s>>>(a, rho_constant(a.order), staged ? 1 : 0);
+  return check_launch("milstein_affine_kernel");
+}
+
+template <typename T>
+int dispatch_affine(const tqf_milstein_affine_args& a, cudaStream_t s) {
+  if (a.dim == 1) return launch_affine<T, 1>(a, s);
+  if (a.dim <= 2) return launch_affine<T, 2>(a, s);
+  if (a.dim <= 4) return launch_affine<T, 4>(a, s);
+  return launch_affine<T, 8>(a, s);
+}
+
+template <typename T>
+int dispatch_update(const tqf_milstein_update_args& a, cudaStream_t s) {
+  const int64_t grid = (a.num_paths + kBlock - 1) / kBlock;
+  TQF_REQUIRE(grid <= 2147483647LL, "tqf_milstein_update: too many paths");
+  const double rc = rho_constant(a.order);
+  if (a.dim == 1) milstein_update_kernel<T, 1><<<(unsigned)grid, kBlock, 0, s>>>(a, rc);
+  else if (a.dim <= 2) milstein_update_kernel<T, 2><<<(unsigned)grid, kBlock, 0, s>>>(a, rc);
+  else if (a.dim <= 4) milstein_update_kernel<T, 4><<<(unsigned)grid, kBlock, 0, s>>>(a, rc);
+  else milstein_update_kernel<T, 8><<<(unsigned)grid, kBlock, 0, s>>>(a, rc);
+  return check_launch("milstein_update_kernel");
+}
+
+}  // namespace
+}  // namespace tqf
+
+using namespace tqf;
+
+extern "C" int tqf_milstein_affine(const tqf_milstein_affine_args* a, void* stream) {
+  clear_error();
+  TQF_REQUIRE(a != nullptr, "tqf_milstein_affine: null args");
+  TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "tqf_milstein_affine: bad dtype %d", a->dtype);
+  TQF_REQUIRE(a->dim >= 1 && a->dim <= kMaxDimMil, "tqf_milstein_affine: dim must be in [1, 8], got %d", a->dim);
+  TQF_REQUIRE(a->order >= 1 && a->order <= 64, "tqf_milstein_affine: order must be in [1, 64], got %d", a->order);
+  TQF_REQUIRE(a->num_paths >= 1 && a->num_steps >= 0, "tqf_milstein_affine: bad sizes");
+  TQF_REQUIRE(a->x0 && a->drift_m && a->drift_M && a->vol_s0 && a->vol_s1 && a->vol_C,
+              "tqf_milstein_affine: null coefficient pointer");
+  TQF_REQUIRE(a->num_steps == 0 || a->step_table, "tqf_milstein_affine: null step_table");
+  TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.ptr || a->num_steps == 0,
+              "tqf_milstein_affine: memory draws need draws.ptr");
+  TQF_REQUIRE(!a->draws.antithetic || 2 * a->draws.antithetic_half == a->num_paths,
+              "tqf_milstein_affine: antithetic needs num_paths == 2 * antithetic_half");
+  TQF_REQUIRE(a->output.ptr && a->output.num_slots >= 1 && a->output.init_slot < a->output.num_slots,
+              "tqf_milstein_affine: bad output");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a->dtype == TQF_F32 ? dispatch_affine<float>(*a, s) : dispatch_affine<double>(*a, s);
+}
+
+extern "C" int tqf_milstein_update(const tqf_milstein_update_args* a, void* stream) {
+  clear_error();
+  TQF_REQUIRE(a != nullptr, "tqf_milstein_update: null args");
+  TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "tqf_milstein_update: bad dtype %d", a->dtype);
+  TQF_REQUIRE(a->dim >= 1 && a->dim <= kMaxDimMil, "tqf_milstein_update: dim must be in [1, 8], got %d", a->dim);
+  TQF_REQUIRE(a->order >= 1 && a->order <= 64, "tqf_milstein_update: bad order %d", a->order);
+  TQF_REQUIRE(a->num_paths >= 1, "tqf_milstein_update: num_paths must be >= 1");
+  TQF_REQUIRE(a->x && a->drift && a->vol && a->grad && a->x_next, "tqf_milstein_update: null pointer");
+  TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.ptr, "tqf_milstein_update: memory draws need ptr");
+  TQF_REQUIRE(!a->paths_out || a->out_slot < a->num_slots, "tqf_milstein_update: out_slot out of range");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a->dtype == TQF_F32 ? dispatch_update<float>(*a, s) : dispatch_update<double>(*a, s);
+}

@@ -96,6 +96,49 @@ class EulerAffineArgs(ctypes.Structure):
     ]
 
 
+class MilsteinAffineArgs(ctypes.Structure):
+    _fields_ = [
+        ("dtype", c_i32),
+        ("dim", c_i32),
+        ("num_paths", c_i64),
+        ("num_steps", c_i32),
+        ("x0_per_path", c_i32),
+        ("order", c_i32),
+        ("pad0", c_i32),
+        ("step_table", c_vp),
+        ("x0", c_vp),
+        ("drift_m", c_vp),
+        ("drift_M", c_vp),
+        ("vol_s0", c_vp),
+        ("vol_s1", c_vp),
+        ("vol_C", c_vp),
+        ("draws", Draws),
+        ("output", PathOutput),
+        ("dev_status", c_vp),
+    ]
+
+
+class MilsteinUpdateArgs(ctypes.Structure):
+    _fields_ = [
+        ("dtype", c_i32),
+        ("dim", c_i32),
+        ("num_paths", c_i64),
+        ("step", c_i32),
+        ("out_slot", c_i32),
+        ("order", c_i32),
+        ("num_slots", c_i32),
+        ("dt", ctypes.c_double),
+        ("sqrt_dt", ctypes.c_double),
+        ("x", c_vp),
+        ("drift", c_vp),
+        ("vol", c_vp),
+        ("grad", c_vp),
+        ("x_next", c_vp),
+        ("draws", Draws),
+        ("paths_out", c_vp),
+    ]
+
+
 class EulerUpdateArgs(ctypes.Structure):
     _fields_ = [
         ("dtype", c_i32),
@@ -332,6 +375,8 @@ _SIGNATURES = {
     "tqf_philox_normal_draws": (ctypes.c_int, [ctypes.POINTER(Draws), c_i32, c_i32, c_i64, c_i32, c_vp, c_vp]),
     "tqf_euler_affine": (ctypes.c_int, [ctypes.POINTER(EulerAffineArgs), c_vp]),
     "tqf_euler_update": (ctypes.c_int, [ctypes.POINTER(EulerUpdateArgs), c_vp]),
+    "tqf_milstein_affine": (ctypes.c_int, [ctypes.POINTER(MilsteinAffineArgs), c_vp]),
+    "tqf_milstein_update": (ctypes.c_int, [ctypes.POINTER(MilsteinUpdateArgs), c_vp]),
     "tqf_heston_euler": (ctypes.c_int, [ctypes.POINTER(HestonArgs), c_vp]),
     "tqf_heston_qe": (ctypes.c_int, [ctypes.POINTER(HestonArgs), c_vp]),
     "tqf_heston_euler_price_noalloc": (ctypes.c_int, [ctypes.POINTER(HestonArgs), c_vp]),

@@ -44,3 +44,31 @@ class PiecewiseConstantFunc:
         side = "left" if left_continuous else "right"
         idx = np.searchsorted(self._jump_locations, x, side=side)
         return self._values[idx]
+
+    def integrate(self, x1, x2, name=None):
+        """Integral of f over [x1, x2] (piecewise.py:178-208), elementwise."""
+        del name
+        x1 = np.asarray(x1, dtype=self._dtype)
+        x2 = np.asarray(x2, dtype=self._dtype)
+        return (self._primitive(x2) - self._primitive(x1)).astype(self._dtype)
+
+    def _primitive(self, x):
+        """F(x) = integral of f from the first jump location to x."""
+        jl = self._jump_locations.astype(np.float64)
+        v = self._values.astype(np.float64)
+        x = np.asarray(x, dtype=np.float64)
+        # F at each jump location: F(j_0) = 0, F(j_i) = sum_{m=1..i} v_m (j_m - j_{m-1})
+        Fj = np.concatenate([[0.0], np.cumsum(v[1:-1] * np.diff(jl))])
+        idx = np.searchsorted(jl, x, side="left")  # x in (j_{idx-1}, j_idx]
+        below = idx == 0
+        i = np.clip(idx - 1, 0, len(jl) - 1)
+        out = Fj[i] + v[np.clip(idx, 0, len(v) - 1)] * (x - jl[i])
+        return np.where(below, v[0] * (x - jl[0]), out)
+
+
+def convert_to_tensor_or_func(x, dtype=None, name=None):
+    """(x, is_constant): a PiecewiseConstantFunc unchanged, else an array (piecewise.py:421-466)."""
+    del name
+    if isinstance(x, PiecewiseConstantFunc):
+        return x, False
+    return np.asarray(x, dtype=dtype), True
