@@ -238,6 +238,43 @@ typedef struct tqf_euler_update_args {
 
 TQF_API int tqf_euler_update(const tqf_euler_update_args* args, void* stream);
 
+/* ---- Halton sequence (tff/math/random_ops/halton/halton_impl.py) ----------
+ * tqf_halton_sample: out[i][d] (row-major [num_results][dim]) = radical inverse
+ * of index_i + 1 in the d-th prime base over max_sizes[d] digit positions
+ * (halton_impl.py:250-299), index_i = sequence_indices[i] (device int64) or
+ * first_index + i.  With perms (device int32 [num_coeffs * radix_sum]) the
+ * digit at position k is replaced by perms[k * radix_sum + perm_offsets[d] +
+ * digit] and zero_correction[d] (device, out dtype) is added (Owen
+ * scrambling, :282-299).  out_kind: TQF_SOBOL_F32 / _F64 (uniform) or
+ * TQF_SOBOL_NORMAL_F32 / _F64 (sqrt2 erfinv(2u - 1)). */
+typedef struct tqf_halton_args {
+  int32_t dim;
+  int32_t out_kind;
+  int64_t num_results;
+  int64_t first_index;
+  const int64_t* sequence_indices; /* device [num_results] or NULL */
+  const int32_t* primes;           /* device [dim] */
+  const int32_t* max_sizes;        /* device [dim] digit positions per axis */
+  const int32_t* perms;            /* device or NULL (unscrambled) */
+  const int32_t* perm_offsets;     /* device [dim]: sum of the primes before axis d */
+  int32_t radix_sum;               /* sum of the dim primes */
+  int32_t pad0;
+  const void* zero_correction;     /* device [dim] (out dtype) or NULL */
+  void* out;
+} tqf_halton_args;
+
+TQF_API int tqf_halton_sample(const tqf_halton_args* args, void* stream);
+
+/* Independent uniform permutations for the Owen scrambling: for every digit
+ * position k < num_coeffs and axis d a Fisher-Yates shuffle of 0..p_d-1
+ * written at perms[k * radix_sum + perm_offsets[d]], and uniforms[d] in [0, 1)
+ * for the zero correction.  Counter-based (Philox4x32-10, key = seed), so a
+ * seed reproduces the same permutations on any device.  Replaces
+ * _get_permutations (halton_impl.py:321-343) with this engine's own stream. */
+TQF_API int tqf_halton_permutations(int32_t dim, int32_t num_coeffs, const int32_t* primes,
+                                    const int32_t* perm_offsets, int32_t radix_sum, uint64_t seed,
+                                    int32_t* perms, double* uniforms, void* stream);
+
 /* ---- Milstein scheme (tff/models/milstein_sampling.py) ---------------------
  * Step of _milstein_1d / _milstein_nd (milstein_sampling.py:565-593) with the
  * Stratonovich integral approximation of _stratonovich_integral (:481-525) and

@@ -182,3 +182,12 @@ def test_lsm_basis_docstring_example():
     x = np.array([[1.0], [2.0], [3.0], [4.0]])[:, None, :]
     np.testing.assert_allclose(lsm.polynomial_basis(x, 0, 2)[0],
                                [[1, 1, 1, 1], [-1.5, -0.5, 0.5, 1.5], [2.25, 0.25, 0.25, 2.25]])
+
+
+def test_halton_oracle_known_values():
+    """First five unscrambled points in bases 2 and 3 (halton_test.py:30-37)."""
+    from oracle import halton
+    expected = np.array([[1 / 2, 1 / 3], [1 / 4, 2 / 3], [3 / 4, 1 / 9], [1 / 8, 4 / 9], [5 / 8, 7 / 9]], np.float32)
+    np.testing.assert_allclose(halton.sample(2, np.arange(5), np.float32), expected, rtol=1e-6)
+    np.testing.assert_allclose(halton.sample(2, np.arange(5), np.float64), expected.astype(np.float64), rtol=1e-6)
+    assert halton.primes(1000)[-1] == 7919 and list(halton.primes(5)) == [2, 3, 5, 7, 11]

@@ -96,6 +96,24 @@ class EulerAffineArgs(ctypes.Structure):
     ]
 
 
+class HaltonArgs(ctypes.Structure):
+    _fields_ = [
+        ("dim", c_i32),
+        ("out_kind", c_i32),
+        ("num_results", c_i64),
+        ("first_index", c_i64),
+        ("sequence_indices", c_vp),
+        ("primes", c_vp),
+        ("max_sizes", c_vp),
+        ("perms", c_vp),
+        ("perm_offsets", c_vp),
+        ("radix_sum", c_i32),
+        ("pad0", c_i32),
+        ("zero_correction", c_vp),
+        ("out", c_vp),
+    ]
+
+
 class MilsteinAffineArgs(ctypes.Structure):
     _fields_ = [
         ("dtype", c_i32),
@@ -376,6 +394,8 @@ _SIGNATURES = {
     "tqf_euler_affine": (ctypes.c_int, [ctypes.POINTER(EulerAffineArgs), c_vp]),
     "tqf_euler_update": (ctypes.c_int, [ctypes.POINTER(EulerUpdateArgs), c_vp]),
     "tqf_milstein_affine": (ctypes.c_int, [ctypes.POINTER(MilsteinAffineArgs), c_vp]),
+    "tqf_halton_sample": (ctypes.c_int, [ctypes.POINTER(HaltonArgs), c_vp]),
+    "tqf_halton_permutations": (ctypes.c_int, [c_i32, c_i32, c_vp, c_vp, c_i32, ctypes.c_uint64, c_vp, c_vp, c_vp]),
     "tqf_milstein_update": (ctypes.c_int, [ctypes.POINTER(MilsteinUpdateArgs), c_vp]),
     "tqf_heston_euler": (ctypes.c_int, [ctypes.POINTER(HestonArgs), c_vp]),
     "tqf_heston_qe": (ctypes.c_int, [ctypes.POINTER(HestonArgs), c_vp]),

@@ -160,8 +160,15 @@ def multivariate_normal(sample_shape, mean=None, covariance_matrix=None, scale_m
         from tqf.math.random import sobol
         z = sobol.sample_normal(dim, n, skip=skip, dtype=dtype).reshape(sample_shape + (dim,))
     elif random_type in (RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
-        raise NotImplementedError("HALTON random types are not built in this engine (Sobol and "
-                                  "Philox streams are)")
+        if len(batch_shape) != 1:
+            raise NotImplementedError("HALTON draws with a batched mean/scale are not supported")
+        skip = int(kwargs.get("skip", 0) or 0)
+        from tqf.math.random import halton
+        z, _ = halton.sample(dim, sequence_indices=torch.arange(skip, skip + n),
+                             randomized=random_type == RandomType.HALTON_RANDOMIZED,
+                             randomization_params=kwargs.get("randomization_params"), seed=seed, dtype=dtype,
+                             normal=True)
+        z = z.reshape(sample_shape + (dim,))
     else:
         raise NotImplementedError(f"unsupported random_type {random_type}")
     if scale is not None:

@@ -113,14 +113,12 @@ def sample(dim, drift_fn, volatility_fn, times, time_step=None, num_time_steps=N
         draws = mvn.memory_draws(flat, path_axis=0, step_axis=1)
     else:
         rt = RandomType.PSEUDO if random_type is None else random_type
-        if rt == RandomType.SOBOL:
+        if rt in (RandomType.SOBOL, RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
             if batch_shape:
-                raise NotImplementedError("SOBOL draws with a batch_shape are not supported")
-            sob = utils.generate_mc_normal_draws(dim, steps_total, num_samples, rt, skip=skip, dtype=td)
+                raise NotImplementedError("low-discrepancy draws with a batch_shape are not supported")
+            sob = utils.generate_mc_normal_draws(dim, steps_total, num_samples, rt, skip=skip, seed=seed, dtype=td)
             keep_alive.append(sob)
             draws = mvn.memory_draws(sob, path_axis=1, step_axis=0)
-        elif rt in (RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
-            raise NotImplementedError("HALTON random types are not built in this engine")
         else:
             if mvn.is_antithetic(rt) and batch_shape:
                 raise NotImplementedError("antithetic draws with a batch_shape are not supported")

@@ -104,12 +104,10 @@ class GeometricBrownianMotion:
             draws = mvn.memory_draws(dr, path_axis=0, step_axis=1)
         else:
             rt = RandomType.PSEUDO if random_type is None else random_type
-            if rt == RandomType.SOBOL:
-                sob = utils.generate_mc_normal_draws(1, k, int(num_samples), rt, skip=skip, dtype=td)
+            if rt in (RandomType.SOBOL, RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
+                sob = utils.generate_mc_normal_draws(1, k, int(num_samples), rt, skip=skip, seed=seed, dtype=td)
                 keep_alive.append(sob)
                 draws = mvn.memory_draws(sob, path_axis=1, step_axis=0)
-            elif rt in (RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
-                raise NotImplementedError("HALTON random types are not built in this engine")
             else:
                 draws = mvn.philox_draws(rt, seed, int(num_samples))
         N = int(num_samples)

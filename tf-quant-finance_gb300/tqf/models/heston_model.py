@@ -124,12 +124,11 @@ class HestonModel(GenericItoProcess):
                 raise InvalidArgumentError(
                     f"normal_draws cover {draws_t.shape[-2]} time steps, the grid needs {steps_exec}")
             draws = mvn.memory_draws(draws_t, path_axis=0, step_axis=1)
-        elif random_type == RandomType.SOBOL:
-            sob = utils.generate_mc_normal_draws(2, steps_total, int(num_samples), random_type, skip=skip, dtype=td)
+        elif random_type in (RandomType.SOBOL, RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
+            sob = utils.generate_mc_normal_draws(2, steps_total, int(num_samples), random_type, skip=skip, seed=seed,
+                                                 dtype=td)
             keep_alive.append(sob)
             draws = mvn.memory_draws(sob, path_axis=1, step_axis=0)
-        elif random_type in (RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
-            raise NotImplementedError("HALTON random types are not built in this engine")
         else:
             draws = mvn.philox_draws(random_type, seed, int(num_samples))
         num_samples = int(num_samples)

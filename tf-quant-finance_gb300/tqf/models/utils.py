@@ -149,7 +149,12 @@ def generate_mc_normal_draws(num_normal_draws, num_time_steps, num_sample_paths,
         return sobol.normal_draws(int(num_normal_draws), int(num_time_steps), int(num_sample_paths),
                                   skip=int(skip or 0), dtype=dtype)
     if random_type in (RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
-        raise NotImplementedError("HALTON random types are not built in this engine")
+        if batch_shape:
+            raise NotImplementedError("HALTON draws with a batch_shape are not supported")
+        from tqf.math.random import halton
+        return halton.normal_draws(int(num_normal_draws), int(num_time_steps), int(num_sample_paths),
+                                   randomized=random_type == RandomType.HALTON_RANDOMIZED, seed=seed,
+                                   skip=int(skip or 0), dtype=dtype)
     if mvn.is_antithetic(random_type) and batch_shape:
         raise NotImplementedError("antithetic draws with a batch_shape are not supported")
     draws = mvn.philox_normal_draws(random_type, seed, int(num_normal_draws), int(num_time_steps),
