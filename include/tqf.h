@@ -275,6 +275,44 @@ TQF_API int tqf_halton_permutations(int32_t dim, int32_t num_coeffs, const int32
                                     const int32_t* perm_offsets, int32_t radix_sum, uint64_t seed,
                                     int32_t* perms, double* uniforms, void* stream);
 
+/* ---- tff.math.qmc: digital nets and rank-1 lattice rules ------------------
+ * tqf_digital_net_sample: out[i][d] = (shift_d XOR (XOR over set bits b of
+ * index_i of M[d][b])) / 2^num_digits in the output dtype, optionally tent
+ * transformed (digital_net.py:205-419; index_i = sequence_indices[i] or i,
+ * starting at 0).  M: device [dim][log_num_results], int32 or int64 (int_bits).
+ * tqf_lattice_rule_sample: out[i][d] = frac(index_i * frac(g_d / n) + shift_d)
+ * in the output dtype (lattice_rule.py:99-229).  out_kind TQF_SOBOL_F32/_F64. */
+typedef struct tqf_digital_net_args {
+  int32_t dim;
+  int32_t log_num_results;
+  int32_t num_digits;
+  int32_t out_kind;
+  int32_t tent;
+  int32_t int_bits;              /* 32 or 64: element type of matrices / digital_shift */
+  int64_t count;                 /* points produced */
+  const int64_t* sequence_indices; /* device [count] or NULL (0 .. count-1) */
+  const void* matrices;
+  const void* digital_shift;     /* device [dim] or NULL */
+  void* out;
+} tqf_digital_net_args;
+
+TQF_API int tqf_digital_net_sample(const tqf_digital_net_args* args, void* stream);
+
+typedef struct tqf_lattice_args {
+  int32_t dim;
+  int32_t out_kind;
+  int32_t tent;
+  int32_t int_bits;              /* element type of generating_vectors */
+  int64_t num_results;           /* n of the rule */
+  int64_t count;                 /* points produced */
+  const int64_t* sequence_indices; /* device [count] or NULL */
+  const void* generating_vectors;  /* device [>= dim] */
+  const void* additive_shift;      /* device [>= dim] (out dtype) or NULL */
+  void* out;
+} tqf_lattice_args;
+
+TQF_API int tqf_lattice_rule_sample(const tqf_lattice_args* args, void* stream);
+
 /* ---- Milstein scheme (tff/models/milstein_sampling.py) ---------------------
  * Step of _milstein_1d / _milstein_nd (milstein_sampling.py:565-593) with the
  * Stratonovich integral approximation of _stratonovich_integral (:481-525) and

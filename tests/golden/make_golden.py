@@ -1,5 +1,5 @@
 """Extracts the reference's known-answer vectors for the hot path into
-sobol_golden.json / heston_golden.json / lsm_golden.json.
+sobol_golden.json / heston_golden.json / lsm_golden.json / qmc_golden.json.
 
 Run in a checkout that has the reference sources (read as text; TensorFlow is
 not needed):  python tests/golden/make_golden.py /path/to/tf-quant-finance
@@ -103,6 +103,68 @@ def main(ref_root):
     }
     with open(os.path.join(here, "lsm_golden.json"), "w") as f:
         json.dump(lsm, f, indent=1)
+    # tff.math.qmc: the `expected = tf.constant([...])` literal of each test
+    # function, with the call it checks (cross-checked against the source).
+    qmc_dir = os.path.join(tff, "math", "qmc")
+
+    def expected_of(path, func):
+        tree = ast.parse(open(path).read())
+        for node in ast.walk(tree):
+            if isinstance(node, ast.FunctionDef) and node.name == func:
+                for stmt in ast.walk(node):
+                    if (isinstance(stmt, ast.Assign) and getattr(stmt.targets[0], "id", "") == "expected"
+                            and isinstance(stmt.value, ast.Call) and stmt.value.args):
+                        return ast.literal_eval(stmt.value.args[0])
+        raise KeyError(func)
+
+    def class_list(path, name):
+        tree = ast.parse(open(path).read())
+        for node in ast.walk(tree):
+            if isinstance(node, ast.Assign) and getattr(node.targets[0], "id", "") == name:
+                return ast.literal_eval(node.value)
+        raise KeyError(name)
+
+    sob_t = os.path.join(qmc_dir, "sobol_test.py")
+    dn_t = os.path.join(qmc_dir, "digital_net_test.py")
+    lr_t = os.path.join(qmc_dir, "lattice_rule_test.py")
+    src = open(sob_t).read() + open(dn_t).read() + open(lr_t).read()
+    for needle in ("qmc.sobol_sample(5, 29, validate_args=True)", "indices = [1, 3, 10, 15, 19, 24, 28]",
+                   "apply_tent_transform=True", "qmc.sobol_sample(6, 8, validate_args=True, dtype=dtype)",
+                   "indices = [2, 3, 6, 9, 11, 14]"):
+        assert needle in src, needle
+    qmc = {
+        "source": ["tf_quant_finance/math/qmc/sobol_test.py", "tf_quant_finance/math/qmc/digital_net_test.py",
+                   "tf_quant_finance/math/qmc/lattice_rule_test.py"],
+        "sobol_sample": {"dim": 5, "num_results": 29, "expected": expected_of(sob_t, "test_sobol_sample")},
+        "sobol_sample_indices": {"dim": 5, "num_results": 29, "sequence_indices": [1, 3, 10, 15, 19, 24, 28],
+                                 "expected": expected_of(sob_t, "test_sobol_sample_with_sequence_indices")},
+        "sobol_sample_tent": {"dim": 6, "num_results": 8, "tent": True,
+                              "expected": expected_of(sob_t, "test_sobol_sample_with_tent_transform")},
+        "sobol_sample_dtype": {"dim": 6, "num_results": 8,
+                               "expected": expected_of(sob_t, "test_sobol_sample_with_dtype")},
+        "generating_matrices": {"dim": 5, "num_results": 31, "num_digits": 5,
+                                "expected": expected_of(sob_t, "test_sobol_generating_matrices")},
+        "digital_net": {"dim": 5, "num_results": 29, "num_digits": 5,
+                        "expected": expected_of(dn_t, "test_digital_net_sample")},
+        "digital_net_indices": {"dim": 5, "num_results": 29, "num_digits": 5,
+                                "sequence_indices": [1, 3, 10, 15, 19, 24, 28],
+                                "expected": expected_of(dn_t, "test_digital_net_sample_with_sequence_indices")},
+        "digital_net_tent": {"dim": 6, "num_results": 8, "num_digits": 3, "tent": True,
+                             "expected": expected_of(dn_t, "test_sample_sobol_with_tent_transform")},
+        "lattice_generating_vectors": class_list(lr_t, "generating_vectors_values"),
+        "lattice": {"dim": 6, "num_results": 16, "expected": expected_of(lr_t, "test_lattice_rule_sample")},
+        "lattice_indices": {"dim": 6, "num_results": 16, "sequence_indices": [2, 3, 6, 9, 11, 14],
+                            "expected": expected_of(lr_t, "test_lattice_rule_sample_with_sequence_indices")},
+        "lattice_zero_shift": {"dim": 5, "num_results": 8,
+                               "expected": expected_of(lr_t, "test_lattice_rule_sample_with_zero_additive_shift")},
+        "lattice_shift": {"dim": 5, "num_results": 8,
+                          "additive_shift": _literal_assignments(
+                              lr_t, "test_lattice_rule_sample_with_non_zero_additive_shift")["additive_shift"],
+                          "expected": expected_of(lr_t, "test_lattice_rule_sample_with_non_zero_additive_shift")},
+        "tolerance": {"rtol": 1e-6},
+    }
+    with open(os.path.join(here, "qmc_golden.json"), "w") as f:
+        json.dump(qmc, f, indent=1)
 
 
 if __name__ == "__main__":

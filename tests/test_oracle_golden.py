@@ -191,3 +191,34 @@ def test_halton_oracle_known_values():
     np.testing.assert_allclose(halton.sample(2, np.arange(5), np.float32), expected, rtol=1e-6)
     np.testing.assert_allclose(halton.sample(2, np.arange(5), np.float64), expected.astype(np.float64), rtol=1e-6)
     assert halton.primes(1000)[-1] == 7919 and list(halton.primes(5)) == [2, 3, 5, 7, 11]
+
+
+def test_qmc_oracle_matches_reference_known_answers():
+    """Generating matrices, digital-net and lattice points of the reference's
+    qmc tests (sobol_test.py, digital_net_test.py, lattice_rule_test.py)."""
+    from oracle import qmc
+    with open(os.path.join(os.path.dirname(__file__), "golden", "qmc_golden.json")) as f:
+        g = json.load(f)
+    tol = dict(rtol=1e-6, atol=1e-6)  # tf.test assertAllClose defaults
+    c = g["generating_matrices"]
+    np.testing.assert_array_equal(qmc.sobol_generating_matrices(c["dim"], c["num_results"], c["num_digits"]),
+                                  c["expected"])
+    for key in ("sobol_sample", "sobol_sample_indices", "sobol_sample_tent", "sobol_sample_dtype"):
+        c = g[key]
+        got = qmc.sobol_sample(c["dim"], c["num_results"], sequence_indices=c.get("sequence_indices"),
+                               apply_tent_transform=c.get("tent", False))
+        np.testing.assert_allclose(got, c["expected"], **tol)
+    for key in ("digital_net", "digital_net_indices", "digital_net_tent"):
+        c = g[key]
+        gen = qmc.sobol_generating_matrices(c["dim"], c["num_results"], c["num_digits"])
+        got = qmc.digital_net_sample(gen, c["num_results"], c["num_digits"], c.get("sequence_indices"),
+                                     apply_tent_transform=c.get("tent", False))
+        np.testing.assert_allclose(got, c["expected"], **tol)
+    gv = g["lattice_generating_vectors"]
+    for key, shift in (("lattice", None), ("lattice_indices", None), ("lattice_zero_shift", np.zeros(20)),
+                       ("lattice_shift", g["lattice_shift"].get("additive_shift"))):
+        c = g[key]
+        got = qmc.lattice_rule_sample(gv, c["dim"], c["num_results"], c.get("sequence_indices"), shift)
+        np.testing.assert_allclose(got, c["expected"], **tol)
+    gen = qmc.sobol_generating_matrices(6, 8, 3)
+    np.testing.assert_array_equal(qmc.scramble_generating_matrices(gen, np.full(gen.shape, 4), 3), gen)

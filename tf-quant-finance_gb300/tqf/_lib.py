@@ -114,6 +114,37 @@ class HaltonArgs(ctypes.Structure):
     ]
 
 
+class DigitalNetArgs(ctypes.Structure):
+    _fields_ = [
+        ("dim", c_i32),
+        ("log_num_results", c_i32),
+        ("num_digits", c_i32),
+        ("out_kind", c_i32),
+        ("tent", c_i32),
+        ("int_bits", c_i32),
+        ("count", c_i64),
+        ("sequence_indices", c_vp),
+        ("matrices", c_vp),
+        ("digital_shift", c_vp),
+        ("out", c_vp),
+    ]
+
+
+class LatticeArgs(ctypes.Structure):
+    _fields_ = [
+        ("dim", c_i32),
+        ("out_kind", c_i32),
+        ("tent", c_i32),
+        ("int_bits", c_i32),
+        ("num_results", c_i64),
+        ("count", c_i64),
+        ("sequence_indices", c_vp),
+        ("generating_vectors", c_vp),
+        ("additive_shift", c_vp),
+        ("out", c_vp),
+    ]
+
+
 class MilsteinAffineArgs(ctypes.Structure):
     _fields_ = [
         ("dtype", c_i32),
@@ -395,6 +426,8 @@ _SIGNATURES = {
     "tqf_euler_update": (ctypes.c_int, [ctypes.POINTER(EulerUpdateArgs), c_vp]),
     "tqf_milstein_affine": (ctypes.c_int, [ctypes.POINTER(MilsteinAffineArgs), c_vp]),
     "tqf_halton_sample": (ctypes.c_int, [ctypes.POINTER(HaltonArgs), c_vp]),
+    "tqf_digital_net_sample": (ctypes.c_int, [ctypes.POINTER(DigitalNetArgs), c_vp]),
+    "tqf_lattice_rule_sample": (ctypes.c_int, [ctypes.POINTER(LatticeArgs), c_vp]),
     "tqf_halton_permutations": (ctypes.c_int, [c_i32, c_i32, c_vp, c_vp, c_i32, ctypes.c_uint64, c_vp, c_vp, c_vp]),
     "tqf_milstein_update": (ctypes.c_int, [ctypes.POINTER(MilsteinUpdateArgs), c_vp]),
     "tqf_heston_euler": (ctypes.c_int, [ctypes.POINTER(HestonArgs), c_vp]),
