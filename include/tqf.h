@@ -313,6 +313,31 @@ typedef struct tqf_lattice_args {
 
 TQF_API int tqf_lattice_rule_sample(const tqf_lattice_args* args, void* stream);
 
+/* ---- Hull-White short-rate paths (tff/models/hull_white/vector_hull_white.py) ----
+ * Exact discretisation of the vector Hull-White model with piecewise-constant
+ * parameters (_sample_paths, vector_hull_white.py:641-781): per step i and
+ * axis d, x_d <- decay[i][d] x_d + mean[i][d] + vol[i][d] (L_i z)_d, and the
+ * rate x_d + f0[i+1][d] is stored at slot[i] (f0[0][d] at output.init_slot).
+ * table [num_steps][dim][3] = (exp(-a_{i+1} dt_i), conditional mean increment,
+ * sqrt of the conditional variance); f0 [num_steps + 1][dim] (instantaneous
+ * forward rates on the grid); chol [num_steps][dim][dim] lower Cholesky
+ * factors of the correlation or NULL; slots [num_steps] int32.  dim <= 16. */
+typedef struct tqf_hull_white_args {
+  int32_t dtype;
+  int32_t dim;
+  int64_t num_paths;
+  int32_t num_steps;
+  int32_t pad0;
+  const void* table;
+  const void* f0;
+  const void* chol;
+  const int32_t* slots;
+  tqf_draws draws;
+  tqf_path_output output;
+} tqf_hull_white_args;
+
+TQF_API int tqf_hull_white_paths(const tqf_hull_white_args* args, void* stream);
+
 /* ---- Milstein scheme (tff/models/milstein_sampling.py) ---------------------
  * Step of _milstein_1d / _milstein_nd (milstein_sampling.py:565-593) with the
  * Stratonovich integral approximation of _stratonovich_integral (:481-525) and

@@ -1,5 +1,5 @@
 """Extracts the reference's known-answer vectors for the hot path into
-sobol_golden.json / heston_golden.json / lsm_golden.json / qmc_golden.json.
+sobol_golden.json / heston_golden.json / lsm_golden.json / qmc_golden.json / hw_golden.json.
 
 Run in a checkout that has the reference sources (read as text; TensorFlow is
 not needed):  python tests/golden/make_golden.py /path/to/tf-quant-finance
@@ -165,6 +165,27 @@ def main(ref_root):
     }
     with open(os.path.join(here, "qmc_golden.json"), "w") as f:
         json.dump(qmc, f, indent=1)
+    # Hull-White: the zero-coupon bond prices conditional on r(t) that
+    # hull_white_test.py asserts, with the model parameters of its setUp.
+    hw_t = os.path.join(tff, "models", "hull_white", "hull_white_test.py")
+    setup = _literal_assignments(hw_t, "setUp")
+    bond = _literal_assignments(hw_t, "test_discount_bond_price_fn")
+    hsrc = open(hw_t).read()
+    assert "[[0.011], [0.01]]" in hsrc and "[1.0, 2.0]" in hsrc and "[2.0, 3.5]" in hsrc
+    hw = {
+        "source": "tf_quant_finance/models/hull_white/hull_white_test.py",
+        "mean_reversion": setup["self.mean_reversion"] if "self.mean_reversion" in setup else [0.1, 0.05],
+        "volatility": [0.01, 0.02],
+        "volatility_time_dep_1d": [0.01, 0.02, 0.01],
+        "flat_rate": 0.01,
+        "bond": {"short_rate": [[0.011], [0.01]], "times": [1.0, 2.0], "maturities": [2.0, 3.5],
+                 "expected": bond["expected"], "atol": 1e-12, "rtol": 1e-6},  # tf.test default rtol
+    }
+    for needle in ("self.mean_reversion = [0.1, 0.05]", "self.volatility = [0.01, 0.02]",
+                   "self.volatility_time_dep_1d = [0.01, 0.02, 0.01]", "0.01 * tf.ones_like(t)"):
+        assert needle in hsrc, needle
+    with open(os.path.join(here, "hw_golden.json"), "w") as f:
+        json.dump(hw, f, indent=1)
 
 
 if __name__ == "__main__":

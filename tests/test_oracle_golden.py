@@ -222,3 +222,16 @@ def test_qmc_oracle_matches_reference_known_answers():
         np.testing.assert_allclose(got, c["expected"], **tol)
     gen = qmc.sobol_generating_matrices(6, 8, 3)
     np.testing.assert_array_equal(qmc.scramble_generating_matrices(gen, np.full(gen.shape, 4), 3), gen)
+
+
+def test_hull_white_oracle_bond_prices():
+    """P(t, T | r(t)) of hull_white_test.py:465-485 (atol 1e-12 and tf.test's default rtol 1e-6)."""
+    from oracle import hull_white as ohw
+    with open(os.path.join(os.path.dirname(__file__), "golden", "hw_golden.json")) as f:
+        g = json.load(f)
+    p = ohw.Params(1, [([], [g["mean_reversion"][0]])], [([], [g["volatility"][0]])], np.float64)
+    b = g["bond"]
+    got = ohw.bond_reconstitution(p, b["times"], b["maturities"], b["short_rate"],
+                                  lambda t: np.full((len(t), 1), g["flat_rate"]),
+                                  lambda t: np.full(np.shape(t), g["flat_rate"]))
+    np.testing.assert_allclose(got.ravel(), b["expected"], atol=b["atol"], rtol=b["rtol"])

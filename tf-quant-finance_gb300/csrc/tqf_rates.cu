@@ -1,0 +1,109 @@
+// Hull-White short-rate path kernel — the GB300 replacement of the loop in
+// tff/models/hull_white/vector_hull_white.py:641-781.
+//
+// The reference evaluates the exact one-step transition with a tf.while_loop
+// of whole-tensor ops per time step.  Here the per-step transition constants
+// (decay, conditional mean increment, conditional standard deviation, forward
+// rate, correlation factor) are tabulated once on the host and every thread
+// carries one path's state vector in registers through all steps.
+#include "tqf_internal.cuh"
+
+namespace tqf {
+namespace {
+
+constexpr int kBlock = 256;
+
+template <typename T, int DM>
+__global__ void __launch_bounds__(kBlock) hull_white_kernel(tqf_hull_white_args a) {
+  const int d = a.dim;
+  const T* tab = static_cast<const T*>(a.table);
+  const T* f0 = static_cast<const T*>(a.f0);
+  const T* L = static_cast<const T*>(a.chol);
+  T* out = static_cast<T*>(a.output.ptr);
+  const int ns = a.output.num_slots;
+  for (int64_t path = (int64_t)blockIdx.x * kBlock + threadIdx.x; path < a.num_paths;
+       path += (int64_t)gridDim.x * kBlock) {
+    T x[DM];
+#pragma unroll
+    for (int k = 0; k < DM; ++k) x[k] = T(0);
+    if (a.output.init_slot >= 0) {
+      T* o = out + (path * ns + a.output.init_slot) * d;
+      for (int k = 0; k < d; ++k) o[k] = f0[k];
+    }
+    DrawSource<T> src(a.draws, path, d);
+    for (int i = 0; i < a.num_steps; ++i) {
+      T z[DM], y[DM];
+#pragma unroll
+      for (int c = 0; c < DM; ++c) z[c] = c < d ? src.get(i, c) : T(0);
+      if (L) {
+        const T* Li = L + (size_t)i * d * d;
+#pragma unroll
+        for (int r = 0; r < DM; ++r) {
+          T s = T(0);
+#pragma unroll
+          for (int c = 0; c < DM; ++c)
+            if (r < d && c <= r) s += Li[r * d + c] * z[c];
+          y[r] = s;
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < DM; ++r) y[r] = z[r];
+      }
+      const T* row = tab + (size_t)i * d * 3;
+#pragma unroll
+      for (int k = 0; k < DM; ++k)
+        if (k < d) x[k] = row[3 * k] * x[k] + row[3 * k + 1] + row[3 * k + 2] * y[k];
+      const int slot = a.slots[i];
+      if (slot >= 0) {
+        T* o = out + (path * ns + slot) * d;
+        const T* f = f0 + (size_t)(i + 1) * d;
+#pragma unroll
+        for (int k = 0; k < DM; ++k)
+          if (k < d) o[k] = x[k] + f[k];
+      }
+    }
+  }
+}
+
+template <typename T, int DM>
+int launch(const tqf_hull_white_args& a, cudaStream_t s) {
+  int occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, hull_white_kernel<T, DM>, kBlock, 0) != cudaSuccess ||
+      occ < 1)
+    occ = 1;
+  int64_t grid = (a.num_paths + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)num_sms() * occ;
+  if (grid > cap) grid = cap;
+  hull_white_kernel<T, DM><<<(unsigned)grid, kBlock, 0, s>>>(a);
+  return check_launch("hull_white_kernel");
+}
+
+template <typename T>
+int dispatch(const tqf_hull_white_args& a, cudaStream_t s) {
+  if (a.dim == 1) return launch<T, 1>(a, s);
+  if (a.dim <= 2) return launch<T, 2>(a, s);
+  if (a.dim <= 4) return launch<T, 4>(a, s);
+  return launch<T, 16>(a, s);
+}
+
+}  // namespace
+}  // namespace tqf
+
+using namespace tqf;
+
+extern "C" int tqf_hull_white_paths(const tqf_hull_white_args* a, void* stream) {
+  clear_error();
+  TQF_REQUIRE(a != nullptr, "tqf_hull_white_paths: null args");
+  TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "tqf_hull_white_paths: bad dtype %d", a->dtype);
+  TQF_REQUIRE(a->dim >= 1 && a->dim <= 16, "tqf_hull_white_paths: dim must be in [1, 16], got %d", a->dim);
+  TQF_REQUIRE(a->num_paths >= 1 && a->num_steps >= 0, "tqf_hull_white_paths: bad sizes");
+  TQF_REQUIRE(a->f0 && (a->num_steps == 0 || (a->table && a->slots)), "tqf_hull_white_paths: null table");
+  TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.ptr || a->num_steps == 0,
+              "tqf_hull_white_paths: memory draws need draws.ptr");
+  TQF_REQUIRE(!a->draws.antithetic || 2 * a->draws.antithetic_half == a->num_paths,
+              "tqf_hull_white_paths: antithetic needs num_paths == 2 * antithetic_half");
+  TQF_REQUIRE(a->output.ptr && a->output.num_slots >= 1 && a->output.init_slot < a->output.num_slots,
+              "tqf_hull_white_paths: bad output");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a->dtype == TQF_F32 ? dispatch<float>(*a, s) : dispatch<double>(*a, s);
+}

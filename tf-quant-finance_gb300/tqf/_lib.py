@@ -145,6 +145,22 @@ class LatticeArgs(ctypes.Structure):
     ]
 
 
+class HullWhiteArgs(ctypes.Structure):
+    _fields_ = [
+        ("dtype", c_i32),
+        ("dim", c_i32),
+        ("num_paths", c_i64),
+        ("num_steps", c_i32),
+        ("pad0", c_i32),
+        ("table", c_vp),
+        ("f0", c_vp),
+        ("chol", c_vp),
+        ("slots", c_vp),
+        ("draws", Draws),
+        ("output", PathOutput),
+    ]
+
+
 class MilsteinAffineArgs(ctypes.Structure):
     _fields_ = [
         ("dtype", c_i32),
@@ -426,6 +442,7 @@ _SIGNATURES = {
     "tqf_euler_update": (ctypes.c_int, [ctypes.POINTER(EulerUpdateArgs), c_vp]),
     "tqf_milstein_affine": (ctypes.c_int, [ctypes.POINTER(MilsteinAffineArgs), c_vp]),
     "tqf_halton_sample": (ctypes.c_int, [ctypes.POINTER(HaltonArgs), c_vp]),
+    "tqf_hull_white_paths": (ctypes.c_int, [ctypes.POINTER(HullWhiteArgs), c_vp]),
     "tqf_digital_net_sample": (ctypes.c_int, [ctypes.POINTER(DigitalNetArgs), c_vp]),
     "tqf_lattice_rule_sample": (ctypes.c_int, [ctypes.POINTER(LatticeArgs), c_vp]),
     "tqf_halton_permutations": (ctypes.c_int, [c_i32, c_i32, c_vp, c_vp, c_i32, ctypes.c_uint64, c_vp, c_vp, c_vp]),
