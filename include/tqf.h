@@ -338,6 +338,32 @@ typedef struct tqf_hull_white_args {
 
 TQF_API int tqf_hull_white_paths(const tqf_hull_white_args* args, void* stream);
 
+/* ---- Gaussian HJM factor paths (tff/models/hjm/gaussian_hjm.py) -----------
+ * Euler on the grid for the factors x (gaussian_hjm.py:209-227, 404-457):
+ * x <- x + dt_i (c_i - k x) + B_i (z sqrt(dt_i)), c_i = sum_j y_.j(t_{i+1}),
+ * B_i = chol(rho) scaled by row by sigma(t_{i+1}); along the way the short
+ * rate r_g = sum_k x_k + f0[g] and the discount factor D_{g+1} = D_g exp(-r_g dt_g)
+ * (D_0 = 1).  table [num_steps][2 + dim + dim*dim] = (dt, sqrt dt, c, B);
+ * grid_slot [num_steps + 1]: output slot of each grid point or -1.
+ * rate_out, df_out [N][num_slots]; x_out [N][num_slots][dim] or NULL. */
+typedef struct tqf_hjm_args {
+  int32_t dtype;
+  int32_t dim;
+  int64_t num_paths;
+  int32_t num_steps;
+  int32_t num_slots;
+  const void* table;
+  const void* mean_reversion;  /* [dim] */
+  const void* f0;              /* [num_steps + 1] */
+  const int32_t* grid_slot;    /* [num_steps + 1] */
+  tqf_draws draws;
+  void* rate_out;
+  void* df_out;
+  void* x_out;
+} tqf_hjm_args;
+
+TQF_API int tqf_hjm_paths(const tqf_hjm_args* args, void* stream);
+
 /* ---- Milstein scheme (tff/models/milstein_sampling.py) ---------------------
  * Step of _milstein_1d / _milstein_nd (milstein_sampling.py:565-593) with the
  * Stratonovich integral approximation of _stratonovich_integral (:481-525) and

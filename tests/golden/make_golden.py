@@ -1,5 +1,5 @@
 """Extracts the reference's known-answer vectors for the hot path into
-sobol_golden.json / heston_golden.json / lsm_golden.json / qmc_golden.json / hw_golden.json.
+sobol_golden.json / heston_golden.json / lsm_golden.json / qmc_golden.json / hw_golden.json / hjm_golden.json.
 
 Run in a checkout that has the reference sources (read as text; TensorFlow is
 not needed):  python tests/golden/make_golden.py /path/to/tf-quant-finance
@@ -186,6 +186,24 @@ def main(ref_root):
         assert needle in hsrc, needle
     with open(os.path.join(here, "hw_golden.json"), "w") as f:
         json.dump(hw, f, indent=1)
+    # Gaussian HJM: discount_bond_price known values (gaussian_hjm_test.py:224-282).
+    hjm_t = os.path.join(tff, "models", "hjm", "gaussian_hjm_test.py")
+    jsrc = open(hjm_t).read()
+    one = [0.9803327113840525, 0.9803218405347454, 0.9803116028646381]
+    two = [0.9707109604475661, 0.9706894322583266, 0.9706691582097785]
+    for v in one + two:
+        assert repr(v) in jsrc, v
+    hjm = {
+        "source": "tf_quant_finance/models/hjm/gaussian_hjm_test.py:224-282",
+        "flat_rate": 0.01,
+        "cases": [
+            {"dim": 1, "mr": [0.03], "vol": [0.005], "times": [1.0, 2.0, 3.0], "expected": one},
+            {"dim": 2, "mr": [0.03, 0.03], "vol": [0.005, 0.005], "times": [1.0, 2.0, 3.0], "expected": two},
+        ],
+        "state": 0.01, "maturity_offset": 1.0, "rtol": 1e-8, "atol": 1e-8,
+    }
+    with open(os.path.join(here, "hjm_golden.json"), "w") as f:
+        json.dump(hjm, f, indent=1)
 
 
 if __name__ == "__main__":

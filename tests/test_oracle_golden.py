@@ -235,3 +235,16 @@ def test_hull_white_oracle_bond_prices():
                                   lambda t: np.full((len(t), 1), g["flat_rate"]),
                                   lambda t: np.full(np.shape(t), g["flat_rate"]))
     np.testing.assert_allclose(got.ravel(), b["expected"], atol=b["atol"], rtol=b["rtol"])
+
+
+def test_hjm_oracle_bond_prices():
+    """Gaussian HJM P(t, t + 1 | x = 0.01) of gaussian_hjm_test.py:224-282."""
+    from oracle import hjm
+    with open(os.path.join(os.path.dirname(__file__), "golden", "hjm_golden.json")) as f:
+        g = json.load(f)
+    for c in g["cases"]:
+        m = hjm.Model(c["dim"], c["mr"], None, np.asarray(c["vol"])[:, None], None, np.float64)
+        t = np.asarray(c["times"])
+        got = m.bond(g["state"] * np.ones((len(t), c["dim"])), t, t + g["maturity_offset"],
+                     lambda x: np.full(np.shape(x), g["flat_rate"]))
+        np.testing.assert_allclose(got, c["expected"], rtol=g["rtol"], atol=g["atol"])

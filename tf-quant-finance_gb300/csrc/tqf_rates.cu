@@ -1,5 +1,6 @@
-// Hull-White short-rate path kernel — the GB300 replacement of the loop in
-// tff/models/hull_white/vector_hull_white.py:641-781.
+// Short-rate model path kernels — the GB300 replacement of the loops in
+// tff/models/hull_white/vector_hull_white.py:641-781 (exact Hull-White
+// transition) and tff/models/hjm/gaussian_hjm.py:404-457 (Gaussian HJM Euler).
 //
 // The reference evaluates the exact one-step transition with a tf.while_loop
 // of whole-tensor ops per time step.  Here the per-step transition constants
@@ -86,10 +87,115 @@ int dispatch(const tqf_hull_white_args& a, cudaStream_t s) {
   return launch<T, 16>(a, s);
 }
 
+// Gaussian HJM: Euler for the factors with the short rate and discount factor
+// accumulated in registers (the reference stores every grid point and takes a
+// cumulative product afterwards).
+template <typename T, int DM>
+__global__ void __launch_bounds__(kBlock) hjm_kernel(tqf_hjm_args a) {
+  const int d = a.dim;
+  const int W = 2 + d + d * d;
+  const T* tab = static_cast<const T*>(a.table);
+  const T* f0 = static_cast<const T*>(a.f0);
+  const T* kk = static_cast<const T*>(a.mean_reversion);
+  T* rate_out = static_cast<T*>(a.rate_out);
+  T* df_out = static_cast<T*>(a.df_out);
+  T* x_out = static_cast<T*>(a.x_out);
+  const int ns = a.num_slots;
+  T k[DM];
+#pragma unroll
+  for (int c = 0; c < DM; ++c) k[c] = c < d ? kk[c] : T(0);
+  for (int64_t path = (int64_t)blockIdx.x * kBlock + threadIdx.x; path < a.num_paths;
+       path += (int64_t)gridDim.x * kBlock) {
+    T x[DM];
+#pragma unroll
+    for (int c = 0; c < DM; ++c) x[c] = T(0);
+    T df = T(1);
+    T rate = f0[0];  // sum of zero factors + f0(t_0)
+    int slot = a.grid_slot[0];
+    if (slot >= 0) {
+      rate_out[path * ns + slot] = rate;
+      df_out[path * ns + slot] = df;
+      if (x_out)
+        for (int c = 0; c < d; ++c) x_out[(path * ns + slot) * d + c] = T(0);
+    }
+    DrawSource<T> src(a.draws, path, d);
+    for (int i = 0; i < a.num_steps; ++i) {
+      const T* row = tab + (size_t)i * W;
+      const T dt = row[0], sdt = row[1];
+      df = df * exp(-rate * dt);
+      T dw[DM], xn[DM];
+#pragma unroll
+      for (int c = 0; c < DM; ++c) dw[c] = c < d ? src.get(i, c) * sdt : T(0);
+#pragma unroll
+      for (int r = 0; r < DM; ++r) {
+        if (r >= d) {
+          xn[r] = T(0);
+          continue;
+        }
+        T bw = T(0);
+#pragma unroll
+        for (int c = 0; c < DM; ++c)
+          if (c < d) bw += row[2 + d + r * d + c] * dw[c];
+        xn[r] = x[r] + dt * (row[2 + r] - k[r] * x[r]) + bw;
+      }
+      T s = T(0);
+#pragma unroll
+      for (int c = 0; c < DM; ++c) {
+        x[c] = xn[c];
+        s += x[c];
+      }
+      rate = s + f0[i + 1];
+      slot = a.grid_slot[i + 1];
+      if (slot >= 0) {
+        rate_out[path * ns + slot] = rate;
+        df_out[path * ns + slot] = df;
+        if (x_out)
+          for (int c = 0; c < d; ++c) x_out[(path * ns + slot) * d + c] = x[c];
+      }
+    }
+  }
+}
+
+template <typename T, int DM>
+int launch_hjm(const tqf_hjm_args& a, cudaStream_t s) {
+  int occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, hjm_kernel<T, DM>, kBlock, 0) != cudaSuccess || occ < 1)
+    occ = 1;
+  int64_t grid = (a.num_paths + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)num_sms() * occ;
+  if (grid > cap) grid = cap;
+  hjm_kernel<T, DM><<<(unsigned)grid, kBlock, 0, s>>>(a);
+  return check_launch("hjm_kernel");
+}
+
+template <typename T>
+int dispatch_hjm(const tqf_hjm_args& a, cudaStream_t s) {
+  if (a.dim == 1) return launch_hjm<T, 1>(a, s);
+  if (a.dim <= 2) return launch_hjm<T, 2>(a, s);
+  if (a.dim <= 4) return launch_hjm<T, 4>(a, s);
+  return launch_hjm<T, 16>(a, s);
+}
+
 }  // namespace
 }  // namespace tqf
 
 using namespace tqf;
+
+extern "C" int tqf_hjm_paths(const tqf_hjm_args* a, void* stream) {
+  clear_error();
+  TQF_REQUIRE(a != nullptr, "tqf_hjm_paths: null args");
+  TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "tqf_hjm_paths: bad dtype %d", a->dtype);
+  TQF_REQUIRE(a->dim >= 1 && a->dim <= 16, "tqf_hjm_paths: dim must be in [1, 16], got %d", a->dim);
+  TQF_REQUIRE(a->num_paths >= 1 && a->num_steps >= 0 && a->num_slots >= 1, "tqf_hjm_paths: bad sizes");
+  TQF_REQUIRE(a->table && a->mean_reversion && a->f0 && a->grid_slot && a->rate_out && a->df_out,
+              "tqf_hjm_paths: null pointer");
+  TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.ptr || a->num_steps == 0,
+              "tqf_hjm_paths: memory draws need draws.ptr");
+  TQF_REQUIRE(!a->draws.antithetic || 2 * a->draws.antithetic_half == a->num_paths,
+              "tqf_hjm_paths: antithetic needs num_paths == 2 * antithetic_half");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return a->dtype == TQF_F32 ? dispatch_hjm<float>(*a, s) : dispatch_hjm<double>(*a, s);
+}
 
 extern "C" int tqf_hull_white_paths(const tqf_hull_white_args* a, void* stream) {
   clear_error();

@@ -161,6 +161,24 @@ class HullWhiteArgs(ctypes.Structure):
     ]
 
 
+class HjmArgs(ctypes.Structure):
+    _fields_ = [
+        ("dtype", c_i32),
+        ("dim", c_i32),
+        ("num_paths", c_i64),
+        ("num_steps", c_i32),
+        ("num_slots", c_i32),
+        ("table", c_vp),
+        ("mean_reversion", c_vp),
+        ("f0", c_vp),
+        ("grid_slot", c_vp),
+        ("draws", Draws),
+        ("rate_out", c_vp),
+        ("df_out", c_vp),
+        ("x_out", c_vp),
+    ]
+
+
 class MilsteinAffineArgs(ctypes.Structure):
     _fields_ = [
         ("dtype", c_i32),
@@ -443,6 +461,7 @@ _SIGNATURES = {
     "tqf_milstein_affine": (ctypes.c_int, [ctypes.POINTER(MilsteinAffineArgs), c_vp]),
     "tqf_halton_sample": (ctypes.c_int, [ctypes.POINTER(HaltonArgs), c_vp]),
     "tqf_hull_white_paths": (ctypes.c_int, [ctypes.POINTER(HullWhiteArgs), c_vp]),
+    "tqf_hjm_paths": (ctypes.c_int, [ctypes.POINTER(HjmArgs), c_vp]),
     "tqf_digital_net_sample": (ctypes.c_int, [ctypes.POINTER(DigitalNetArgs), c_vp]),
     "tqf_lattice_rule_sample": (ctypes.c_int, [ctypes.POINTER(LatticeArgs), c_vp]),
     "tqf_halton_permutations": (ctypes.c_int, [c_i32, c_i32, c_vp, c_vp, c_i32, ctypes.c_uint64, c_vp, c_vp, c_vp]),

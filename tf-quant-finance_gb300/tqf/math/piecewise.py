@@ -20,9 +20,20 @@ class PiecewiseConstantFunc:
         self._dtype = dtype or (jl.dtype if jl.dtype.kind == "f" else np.dtype(np.float32))
         self._jump_locations = jl.astype(self._dtype)
         self._values = np.asarray(values, dtype=self._dtype)
-        if self._jump_locations.ndim != 1:
-            raise NotImplementedError("batched PiecewiseConstantFunc is not supported")
-        if self._values.shape[0] - 1 != self._jump_locations.shape[-1]:
+        if self._jump_locations.size == 0 and self._jump_locations.ndim == 1 and self._values.ndim == 2 \
+                and self._values.shape[-1] == 1 and self._values.shape[0] > 1:
+            # [[]] * batch style with values [batch, 1]
+            self._jump_locations = np.zeros((self._values.shape[0], 0), self._dtype)
+        self._batch_rank = self._jump_locations.ndim - 1
+        if self._batch_rank > 1:
+            raise NotImplementedError("PiecewiseConstantFunc with batch rank > 1 is not supported")
+        if self._batch_rank == 1:
+            # batch of functions: jump_locations [B, n], values [B, n + 1] (piecewise.py:19-176)
+            if self._values.shape[:1] != self._jump_locations.shape[:1] or \
+                    self._values.shape[1] - 1 != self._jump_locations.shape[1]:
+                raise ValueError("Batch shapes of `values` and `jump_locations` should be the same and `values` "
+                                 "should have one more element per batch member")
+        elif self._values.shape[0] - 1 != self._jump_locations.shape[-1]:
             raise ValueError(
                 "Event shape of `values` should have one more element than the event shape of "
                 f"`jump_locations` but are {self._values.shape[0]} and {self._jump_locations.shape[-1]}")
@@ -42,6 +53,11 @@ class PiecewiseConstantFunc:
     def __call__(self, x, left_continuous=True, name=None):
         x = np.asarray(x, dtype=self._dtype)
         side = "left" if left_continuous else "right"
+        if self._batch_rank == 1:
+            B = self._jump_locations.shape[0]
+            xb = np.broadcast_to(x, (B,) + x.shape[-1:]) if x.ndim <= 1 else x
+            idx = np.stack([np.searchsorted(self._jump_locations[b], xb[b], side=side) for b in range(B)])
+            return np.take_along_axis(self._values, idx.reshape(B, -1), axis=1).reshape(xb.shape)
         idx = np.searchsorted(self._jump_locations, x, side=side)
         return self._values[idx]
 

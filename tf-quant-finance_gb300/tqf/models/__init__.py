@@ -2,6 +2,7 @@
 
 from tqf.models import coefficients  # noqa: F401
 from tqf.models import euler_sampling  # noqa: F401
+from tqf.models import hjm  # noqa: F401
 from tqf.models import hull_white  # noqa: F401
 from tqf.models import longstaff_schwartz  # noqa: F401
 from tqf.models import milstein_sampling  # noqa: F401
@@ -12,5 +13,5 @@ from tqf.models.heston_model import HestonModel  # noqa: F401
 from tqf.models.ito_process import ItoProcess  # noqa: F401
 from tqf.models.multivariate_gbm import MultivariateGeometricBrownianMotion  # noqa: F401
 
-__all__ = ["coefficients", "euler_sampling", "hull_white", "longstaff_schwartz", "milstein_sampling", "GeometricBrownianMotion", "utils", "GenericItoProcess", "HestonModel", "ItoProcess",
+__all__ = ["coefficients", "euler_sampling", "hjm", "hull_white", "longstaff_schwartz", "milstein_sampling", "GeometricBrownianMotion", "utils", "GenericItoProcess", "HestonModel", "ItoProcess",
            "MultivariateGeometricBrownianMotion"]
