@@ -49,10 +49,12 @@ PARAMS = dict(spot=100.0, variance=0.04, mean_reversion=2.0, theta=0.04, volvol=
 # sin, cos, two products) and the full-truncation step (14: max, sqrt, two
 # dW products, 3 ops log-spot, 7 ops variance).
 ALU_OPS_PER_PATH_STEP = 40 + 14 + 14
-# DRAM bytes (read + write) per launch of the fused kernel, from an ncu capture
-# of full-size launches (2^22 paths x 252 steps, 64 strikes):
-# profiles/heston_ft_f32_pricing.md.  None until captured.
-NCU_TRAFFIC_BYTES = None
+# DRAM bytes (read + write) per launch of the fused kernel: mean of two
+# full-size launches (2^22 paths x 252 steps, 64 strikes) captured with
+# `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum` (47,616 + 0 and
+# 39,936 + 0 bytes): the step table, strikes and parameters; the per-CTA FP64
+# partial sums stay in L2.  profiles/heston_ft_f32_pricing.md.
+NCU_TRAFFIC_BYTES = 43776
 
 
 def strikes():
