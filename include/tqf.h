@@ -644,16 +644,17 @@ TQF_API int tqf_mlp_num_params(void);
 
 /* Gradient of loss = mean_p (Y_p - c - sum_k g(feats_pk) dS_pk)^2 over the
  * paths [path_begin, path_begin + batch_paths) of the pilot data, one CTA per
- * paths_per_cta paths; grad_partials [batch_paths/paths_per_cta][num_params + 1] receives each CTA's
- * gradient and (last column) its share of the loss.  Forward and backward
+ * paths_per_cta paths; grad_partials [batch_paths/paths_per_cta][num_params + 2]
+ * (16-byte aligned) receives each CTA's gradient, in column num_params its
+ * share of the loss, and a zero in the last column.  Forward and backward
  * GEMMs run on tcgen05 tensor cores (BF16 operands, FP32 accumulation). */
 typedef struct tqf_mlp_train_args {
   int32_t num_dates;
   int32_t batch_paths;
-  int32_t paths_per_cta; /* 1..32; one CTA handles paths_per_cta x num_dates rows */
+  int32_t paths_per_cta; /* paths_per_cta x num_dates <= 128: one CTA = one 128-row tile */
   int32_t pad0;
   int64_t path_begin;
-  const float* feats; /* [N][num_dates][4] */
+  const float* feats; /* [N][num_dates][4], 16-byte aligned */
   const float* dS;    /* [N][num_dates] */
   const float* Y;     /* [N] */
   const float* params;

@@ -23,12 +23,11 @@
 //   Modes 0/2 accumulate (Y, Y^2, C, C^2, Y C) in FP64 (fixed order).
 //   Under the log-Euler step E[S~_{i+1} | F_i] = S~_i, so E[C] = 0 exactly.
 // mlp_train_step_kernel: one Adam step's gradient for a minibatch of paths,
-//   loss = mean_p (Y_p - c - sum_k g_pk dS~_pk)^2: per CTA 32 paths x
-//   num_dates rows in 128-row tiles — forward on tensor cores, per-path
-//   residuals, backward with dW2 = d2^T H1, db2 = d2^T 1, dW1 = d1^T X and
-//   d1 = d2 W2 as tcgen05 MMAs accumulated in TMEM across tiles.
-// mlp_adam_kernel: fixed-order reduction of the per-CTA gradients and the
-//   Adam update of the FP32 master parameters and their BF16 copies.
+//   loss = mean_p (Y_p - c - sum_k g_pk dS~_pk)^2: per CTA one 128-row tile
+//   of whole paths — forward on tensor cores, per-path residuals, backward
+//   with d1 = d2 W2, dW2 = d2^T H1, db2, dw3 and dW1 = d1^T X as tcgen05 MMAs.
+// mlp_adam_kernel: fixed-order parallel reduction of the per-CTA gradients
+//   and the Adam update of the FP32 master parameters and their BF16 copies.
 #include <cuda_bf16.h>
 #include <string.h>
 
@@ -42,7 +41,6 @@ constexpr int kIn = 16;           // padded input width (K of layer 1)
 constexpr int kMaxDates = 64;
 constexpr int kPathThreads = 256;  // two warpgroups
 constexpr int kTrainThreads = 128;
-constexpr int kTrainPaths = 32;    // paths per training CTA
 // parameter vector layout (FP32 master copy)
 constexpr int kOffW1 = 0;
 constexpr int kOffW2 = kOffW1 + kH * kIn;   // 1024
@@ -51,7 +49,7 @@ constexpr int kOffW3 = kOffB2 + kH;         // 5184
 constexpr int kOffB3 = kOffW3 + kH;         // 5248
 constexpr int kOffC = kOffB3 + 1;           // 5249
 constexpr int kNumParams = kOffC + 1;       // 5250
-constexpr int kGradWidth = kNumParams + 1;  // + loss sum
+constexpr int kGradWidth = kNumParams + 2;  // + loss sum + one zero pad (16-byte rows)
 
 // Canonical no-swizzle K-major tiles with the 8-row groups contiguous
 // (SBO = 128 B) and the 8-column groups R/8 x 128 B apart (LBO): a K-slice of
@@ -64,22 +62,6 @@ constexpr uint32_t kOnesLbo = 128, kOnesSbo = 2048;  // [16 x 128] read MN-major
 constexpr int kXBytes = 128 * kIn * 2;
 constexpr int kHBytes = 128 * kH * 2;
 constexpr int kW2Bytes = kH * kH * 2;
-
-__device__ __forceinline__ float tanh_approx(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-// x * sigmoid(x) = h (1 + tanh h), h = x / 2
-__device__ __forceinline__ float silu_fast(float x) {
-  const float h = 0.5f * x;
-  return fmaf(h, tanh_approx(h), h);
-}
-// d/dx [x sigmoid(x)] = s + x s (1 - s), s = (1 + tanh(x/2)) / 2
-__device__ __forceinline__ float dsilu_fast(float x) {
-  const float s = fmaf(0.5f, tanh_approx(0.5f * x), 0.5f);
-  return fmaf(x * s, 1.f - s, s);
-}
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
@@ -98,6 +80,29 @@ __device__ __forceinline__ uint32_t silu_bf16x2(float a, float b) {
   asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t2) : "r"(h2));
   asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(s2) : "r"(h2), "r"(t2), "r"(h2));
   return s2;
+}
+
+__device__ __forceinline__ uint32_t bf2_mul(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+__device__ __forceinline__ uint32_t bf2_fma(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+constexpr uint32_t kBf2Half = 0x3F003F00u, kBf2One = 0x3F803F80u, kBf2MinusOne = 0xBF80BF80u;
+
+// SiLU'(x) = s (1 + x (1 - s)), s = sigmoid(x) = (1 + tanh(x/2)) / 2, for a
+// packed BF16 pair (one SFU op for the pair).
+__device__ __forceinline__ uint32_t dsilu_bf16x2(uint32_t x2) {
+  uint32_t h2, t2;
+  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(h2) : "r"(x2), "r"(kBf2Half));
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t2) : "r"(h2));
+  const uint32_t sg = bf2_fma(t2, kBf2Half, kBf2Half);
+  const uint32_t om = bf2_fma(sg, kBf2MinusOne, kBf2One);  // 1 - s
+  return bf2_mul(sg, bf2_fma(x2, om, kBf2One));
 }
 
 // Layer 1 on the CUDA cores (K = 3 is not GEMM-shaped): a1_j = w1_j . (f0,
@@ -123,21 +128,6 @@ __device__ __forceinline__ void layer1_row(const float4* __restrict__ s_l1, floa
       pk[q] = silu_bf16x2(aa, ab);
     }
     *reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, 8 * jc, kHLbo, kHSbo)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-  }
-}
-
-// Writes 8*nlines values of row r of a K-major BF16 tile (16-byte lines).
-__device__ __forceinline__ void write_row_kmajor(unsigned char* tile, int r, const float* v, int nlines,
-                                                 uint32_t lbo, uint32_t sbo) {
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    if (j >= nlines) break;
-    uint4 w;
-    w.x = pack_bf16x2(v[8 * j + 0], v[8 * j + 1]);
-    w.y = pack_bf16x2(v[8 * j + 2], v[8 * j + 3]);
-    w.z = pack_bf16x2(v[8 * j + 4], v[8 * j + 5]);
-    w.w = pack_bf16x2(v[8 * j + 6], v[8 * j + 7]);
-    *reinterpret_cast<uint4*>(tile + tc::kmajor_off(r, 8 * j, lbo, sbo)) = w;
   }
 }
 
@@ -250,19 +240,6 @@ __device__ __forceinline__ float mlp_collect(int tid, const W& ms, uint32_t tmem
   return g;
 }
 
-// Loads W2 (BF16 [64][64] row-major) into its K-major tile and the layer-1
-// weights (BF16-rounded) into ms.l1.
-__device__ __forceinline__ void load_network(MlpScalars* ms, unsigned char* sW2, const uint16_t* w1_bf16,
-                                             const uint16_t* w2_bf16) {
-  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x)
-    *reinterpret_cast<uint16_t*>(sW2 + tc::kmajor_off(i / kH, i % kH, kW2Lbo, kW2Sbo)) = w2_bf16[i];
-  for (int j = threadIdx.x; j < kH; j += blockDim.x) {
-    const uint16_t* w = w1_bf16 + j * kIn;
-    ms->l1[j] = make_float4(__uint_as_float((uint32_t)w[0] << 16), __uint_as_float((uint32_t)w[1] << 16),
-                            __uint_as_float((uint32_t)w[2] << 16), __uint_as_float((uint32_t)w[3] << 16));
-  }
-}
-
 // ---- path kernel -----------------------------------------------------------------
 struct AsianSmem {
   uint64_t bar[2];
@@ -295,9 +272,9 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? 4 : 1)
   for (int i = threadIdx.x; i < (kPathThreads / 32) * 5; i += blockDim.x) (&S->acc[0][0])[i] = 0.0;
   for (int i = threadIdx.x; i < a.num_steps * 8; i += blockDim.x) table[i] = a.step_table[i];
   if (MODE == 2) {
-    const uint16_t* w2 = static_cast<const uint16_t*>(a.mlp.w2_bf16);
-    for (int i = threadIdx.x; i < kH * kH; i += blockDim.x)
-      *reinterpret_cast<uint16_t*>(sW2 + tc::kmajor_off(i / kH, i % kH, kW2Lbo, kW2Sbo)) = w2[i];
+    const uint4* w2 = static_cast<const uint4*>(a.mlp.w2_bf16);
+    for (int i = threadIdx.x; i < kH * kH / 8; i += blockDim.x)
+      *reinterpret_cast<uint4*>(sW2 + tc::kmajor_off(i >> 3, 8 * (i & 7), kW2Lbo, kW2Sbo)) = w2[i];
     if (threadIdx.x == 0) {
       mbar_init(&S->bar[0], 1);
       mbar_init(&S->bar[1], 1);
@@ -424,17 +401,36 @@ int asian_grid(int64_t n, size_t smem) {
 }
 
 // ---- training step ---------------------------------------------------------------------
+// One CTA = one warpgroup = one 128-row tile holding all num_dates rows of
+// paths_per_cta paths (paths_per_cta x num_dates <= 128), so the forward pass
+// runs once and the per-path residual never crosses CTAs.  With
+// q2 = w3 (.) SiLU'(a2) (known after the forward pass) and the per-row output
+// gradient d3 = -2 r_p dS_pk / B (known after the residual):
+//   d2 = d3 q2,  d1 = d3 (Q2 W2) (.) SiLU'(a1),
+//   dW2 = Q2^T (d3 H1),  db2 = Q2^T d3,  dw3 = H2^T d3,  dW1 = D1^T X,
+// so the Q2 W2 product is issued before the residual is known and overlaps
+// it.  Layer 1 runs on the tensor cores here (X [128 x 16] x W1^T, bias in
+// input column 3) and its pre-activations stay in TMEM for the backward
+// pass.  The backward elementwise work (SiLU', the d3 scaling) runs in
+// packed BF16, two values per instruction; its operands are BF16 anyway.
+// TMEM (128 columns): [64, 128) a1, then dW2; [0, 64) the layer-2
+// accumulator, then Q2 W2, then db2 | dw3 | dW1 (16 columns each).
+constexpr uint32_t kW1Lbo = 1024, kW1Sbo = 128;  // W1 [64 x 16] K-major
+constexpr int kW1Bytes = kH * kIn * 2;
+
 struct TrainSmem {
   uint64_t bar;
   uint32_t tmem_slot;
   uint32_t pad;
-  MlpScalars ms;
-  float c;
-  float resid[kTrainPaths];
-  float Y[kTrainPaths];
-  float b3acc[4];
-  float lossacc;
-  float cacc;
+  float b2[kH];
+  float w3[kH];
+  uint32_t w3p[kH / 2];  // w3 as BF16 pairs
+  float4 fs;             // feature scale (x, y, z)
+  float4 fo;             // feature shift
+  float b3, c;
+  float gds[128];     // g x dS~ per row
+  float resid[128];   // per path
+  float wloss[4], wsum[4], wb3[4];
 };
 
 __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_train_args a) {
@@ -442,181 +438,230 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
   TrainSmem* S = reinterpret_cast<TrainSmem*>(smem);
   unsigned char* t0 = smem + ((sizeof(TrainSmem) + 1023) & ~(size_t)1023);
   unsigned char* sW2 = t0;
-  unsigned char* sX = sW2 + kW2Bytes;
-  unsigned char* sH = sX + kXBytes;
+  unsigned char* sW1 = sW2 + kW2Bytes;
+  unsigned char* sX = sW1 + kW1Bytes;
+  unsigned char* sH = sX + kXBytes;   // H1, scaled by d3 in place before dW2
   unsigned char* sH2 = sH + kHBytes;
-  unsigned char* sD2 = sH2 + kHBytes;
-  unsigned char* sD1 = sD2 + kHBytes;
-  unsigned char* sOnes = sD1 + kHBytes;  // [16 x 128] MN-major, all ones
-  unsigned char* sT3 = sOnes + 16 * 128 * 2;  // [16 x 128] MN-major, column 0 = d3
-  float* g_rows = reinterpret_cast<float*>(sT3 + 16 * 128 * 2);
+  unsigned char* sQ2 = sH2 + kHBytes;
+  unsigned char* sD1 = sQ2 + kHBytes;
+  unsigned char* sT3 = sD1 + kHBytes;  // [16 x 128] MN-major, column 0 = d3
   const int D = a.num_dates;
   const int P = a.paths_per_cta;
   const int rows = P * D;
-  float* ds_rows = g_rows + rows;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t p0 = a.path_begin + (int64_t)blockIdx.x * P;
   const float inv_B = 1.f / (float)a.batch_paths;
-  load_network(&S->ms, sW2, static_cast<const uint16_t*>(a.w1_bf16), static_cast<const uint16_t*>(a.w2_bf16));
+  {
+    // W2 (BF16 [64][64] row-major) and W1 (BF16 [64][16]) into K-major tiles
+    const uint4* w2 = static_cast<const uint4*>(a.w2_bf16);
+    for (int i = tid; i < kH * kH / 8; i += kTrainThreads)
+      *reinterpret_cast<uint4*>(sW2 + tc::kmajor_off(i >> 3, 8 * (i & 7), kW2Lbo, kW2Sbo)) = w2[i];
+    const uint4* w1 = static_cast<const uint4*>(a.w1_bf16);
+    for (int i = tid; i < kH * kIn / 8; i += kTrainThreads)
+      *reinterpret_cast<uint4*>(sW1 + tc::kmajor_off(i >> 1, 8 * (i & 1), kW1Lbo, kW1Sbo)) = w1[i];
+  }
   const float* Pm = a.params;
   for (int i = tid; i < kH; i += kTrainThreads) {
-    S->ms.b2[i] = Pm[kOffB2 + i];
-    S->ms.w3[i] = Pm[kOffW3 + i];
+    S->b2[i] = Pm[kOffB2 + i];
+    S->w3[i] = Pm[kOffW3 + i];
   }
-  for (int i = tid; i < 16 * 128; i += kTrainThreads) {
-    *reinterpret_cast<uint16_t*>(sOnes + 2 * i) = (uint16_t)0x3F80u;  // bf16 1.0
-    *reinterpret_cast<uint16_t*>(sT3 + 2 * i) = (uint16_t)0u;
-  }
-  if (tid < P) S->Y[tid] = a.Y[p0 + tid];
+  for (int i = tid; i < kH / 2; i += kTrainThreads) S->w3p[i] = pack_bf16x2(Pm[kOffW3 + 2 * i], Pm[kOffW3 + 2 * i + 1]);
+  for (int i = tid; i < 16 * 128 * 2 / 16; i += kTrainThreads)
+    reinterpret_cast<uint4*>(sT3)[i] = make_uint4(0u, 0u, 0u, 0u);
   if (tid == 0) {
-    S->ms.b3 = Pm[kOffB3];
+    S->b3 = Pm[kOffB3];
     S->c = Pm[kOffC];
-    for (int j = 0; j < 3; ++j) {
-      S->ms.fscale[j] = a.feat_scale[j];
-      S->ms.fshift[j] = a.feat_shift[j];
-    }
-    for (int w = 0; w < 4; ++w) S->b3acc[w] = 0.f;
-    S->lossacc = 0.f;
-    S->cacc = 0.f;
+    S->fs = make_float4(a.feat_scale[0], a.feat_scale[1], a.feat_scale[2], 0.f);
+    S->fo = make_float4(a.feat_shift[0], a.feat_shift[1], a.feat_shift[2], 0.f);
     mbar_init(&S->bar, 1);
   }
-  if (warp == 0) tc::tmem_alloc(&S->tmem_slot, 256);
-  tc::fence_smem_to_async();
+  if (warp == 0) tc::tmem_alloc(&S->tmem_slot, 128);
+  // this row's inputs
+  const int r = tid;
+  const bool in = r < rows;
+  const int pl = in ? r / D : 0, dd = in ? r % D : 0;
+  const int64_t gi = (p0 + pl) * D + dd;
+  const float4 f = in ? reinterpret_cast<const float4*>(a.feats)[gi] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float dsv = in ? a.dS[gi] : 0.f;
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tm = S->tmem_slot;
-  const uint32_t t_d2 = tm, t_d3 = tm + 64, t_dw2 = tm + 128, t_db2 = tm + 192, t_dw1 = tm + 208, t_dw3 = tm + 224;
+  const uint32_t t_fwd = tm, t_a1 = tm + 64, t_db2 = tm, t_dw3 = tm + 16, t_dw1 = tm + 32, t_dw2 = tm + 64;
+  const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
   uint32_t phase = 0;
-  const int tiles = (rows + 127) / 128;
-  const float4* feats = reinterpret_cast<const float4*>(a.feats);
-  // ---- phase A: forward over every row, keep g
-  for (int t = 0; t < tiles; ++t) {
-    const int r = t * 128 + tid;
-    const bool in = r < rows;
-    const int pl = in ? r / D : 0, d = in ? r % D : 0;
-    const float4 f = in ? feats[(p0 + pl) * D + d] : make_float4(0.f, 0.f, 0.f, 0.f);
-    mlp_issue(0, tid, S->ms, sH, sW2, t_d2, &S->bar, f.x, f.y, f.z);
-    const float gg = mlp_collect(tid, S->ms, t_d2, &S->bar, phase, a.dev_status);
-    if (in) {
-      g_rows[r] = gg;
-      ds_rows[r] = a.dS[(p0 + pl) * D + d];
+  // ---- forward.  Layer 1: X row = (BF16 features, 1, 0...) -> a1 in TMEM
+  {
+    const float4 fs = S->fs, fo = S->fo;
+    const float f0 = round_bf16((f.x - fo.x) * fs.x), f1 = round_bf16((f.y - fo.y) * fs.y),
+                f2 = round_bf16((f.z - fo.z) * fs.z);
+    *reinterpret_cast<uint4*>(sX + tc::kmajor_off(r, 0, kXLbo, kXSbo)) =
+        make_uint4(pack_bf16x2(f0, f1), pack_bf16x2(f2, 1.f), 0u, 0u);
+    *reinterpret_cast<uint4*>(sX + tc::kmajor_off(r, 8, kXLbo, kXSbo)) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  tc::fence_smem_to_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (tid == 0) {
+    tc::mma_bf16(t_a1, tc::smem_desc(smem_addr(sX), kXLbo, kXSbo), tc::smem_desc(smem_addr(sW1), kW1Lbo, kW1Sbo),
+                 tc::idesc_bf16(128, kH, false, false), 0u);
+    tc::commit(&S->bar);
+  }
+  mma_wait(&S->bar, phase, a.dev_status);
+#pragma unroll
+  for (int c = 0; c < kH; c += 16) {
+    float acc[16];
+    tc::tmem_ld16(t_a1 + lane_base + (uint32_t)c, acc);
+#pragma unroll
+    for (int h = 0; h < 16; h += 8)
+      *reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, c + h, kHLbo, kHSbo)) =
+          make_uint4(silu_bf16x2(acc[h], acc[h + 1]), silu_bf16x2(acc[h + 2], acc[h + 3]),
+                     silu_bf16x2(acc[h + 4], acc[h + 5]), silu_bf16x2(acc[h + 6], acc[h + 7]));
+  }
+  tc::fence_smem_to_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  // Layer 2 on the tensor cores
+  if (tid == 0) {
+    const uint32_t idesc = tc::idesc_bf16(128, kH, false, false);
+#pragma unroll
+    for (int s = 0; s < kH / 16; ++s)
+      tc::mma_bf16(t_fwd, tc::smem_desc(smem_addr(sH) + 2u * s * kHLbo, kHLbo, kHSbo),
+                   tc::smem_desc(smem_addr(sW2) + 2u * s * kW2Lbo, kW2Lbo, kW2Sbo), idesc, s > 0 ? 1u : 0u);
+    tc::commit(&S->bar);
+  }
+  mma_wait(&S->bar, phase, a.dev_status);
+  // bias, SiLU (H2), layer 3 (g, FP32) and q2 = w3 SiLU'(a2) (Q2)
+  float g = S->b3;
+  const uint32_t keep = in ? 0xFFFFFFFFu : 0u;
+#pragma unroll
+  for (int c = 0; c < kH; c += 16) {
+    float acc[16];
+    tc::tmem_ld16(t_fwd + lane_base + (uint32_t)c, acc);
+#pragma unroll
+    for (int h = 0; h < 16; h += 8) {
+      const float4 ba = *reinterpret_cast<const float4*>(&S->b2[c + h]);
+      const float4 bb = *reinterpret_cast<const float4*>(&S->b2[c + h + 4]);
+      const float4 wa = *reinterpret_cast<const float4*>(&S->w3[c + h]);
+      const float4 wb = *reinterpret_cast<const float4*>(&S->w3[c + h + 4]);
+      const uint4 wp = *reinterpret_cast<const uint4*>(&S->w3p[(c + h) / 2]);
+      const float bias[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
+      const float w3v[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+      const uint32_t w3pv[4] = {wp.x, wp.y, wp.z, wp.w};
+      uint32_t hp[4], qp[4];
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) {
+        const float aa = acc[h + j] + bias[j], ab = acc[h + j + 1] + bias[j + 1];
+        const uint32_t sp = silu_bf16x2(aa, ab);
+        g = fmaf(w3v[j], bf16_lo(sp), fmaf(w3v[j + 1], bf16_hi(sp), g));
+        hp[j >> 1] = sp;
+        qp[j >> 1] = bf2_mul(w3pv[j >> 1], dsilu_bf16x2(pack_bf16x2(aa, ab))) & keep;
+      }
+      *reinterpret_cast<uint4*>(sH2 + tc::kmajor_off(r, c + h, kHLbo, kHSbo)) = make_uint4(hp[0], hp[1], hp[2], hp[3]);
+      *reinterpret_cast<uint4*>(sQ2 + tc::kmajor_off(r, c + h, kHLbo, kHSbo)) = make_uint4(qp[0], qp[1], qp[2], qp[3]);
     }
   }
+  S->gds[r] = in ? g * dsv : 0.f;
+  tc::fence_smem_to_async();
+  tc::fence_before_sync();
   __syncthreads();
-  // ---- phase B: per-path residuals r_p = Y_p - c - sum_k g_pk dS_pk
-  if (tid < P) {
-    float s = 0.f;
-    for (int d = 0; d < D; ++d) s = fmaf(g_rows[tid * D + d], ds_rows[tid * D + d], s);
-    S->resid[tid] = S->Y[tid] - S->c - s;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    const float rr = lane < P ? S->resid[lane] : 0.f;
-    float l = rr * rr, cc = rr;
+  tc::fence_after_sync();
+  if (tid == 0) {
+    // Q2 W2: A = Q2 [128 x 64] K-major, B = W2 read MN-major (N = in, K = out)
+    const uint32_t id_b1 = tc::idesc_bf16(128, kH, false, true);
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      l += __shfl_xor_sync(0xffffffffu, l, off);
-      cc += __shfl_xor_sync(0xffffffffu, cc, off);
+    for (int s = 0; s < 4; ++s)
+      tc::mma_bf16(t_fwd, tc::smem_desc(smem_addr(sQ2) + 2u * s * kHLbo, kHLbo, kHSbo),
+                   tc::smem_desc(smem_addr(sW2) + 2u * s * kW2Sbo, kW2Sbo, kW2Lbo), id_b1, s > 0 ? 1u : 0u);
+    tc::commit(&S->bar);
+  }
+  // ---- per-path residuals r_p = Y_p - c - sum_k g_pk dS~_pk (one warp per path)
+  {
+    float wl = 0.f, ws = 0.f;
+    for (int p = warp; p < P; p += 4) {
+      float sum = 0.f;
+      for (int k = lane; k < D; k += 32) sum += S->gds[p * D + k];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+      const float rr = a.Y[p0 + p] - S->c - sum;
+      if (lane == 0) S->resid[p] = rr;
+      wl = fmaf(rr, rr, wl);
+      ws += rr;
     }
     if (lane == 0) {
-      S->lossacc = l * inv_B;
-      S->cacc = -2.f * cc * inv_B;
+      S->wloss[warp] = wl;
+      S->wsum[warp] = ws;
     }
   }
-  // ---- phase C: backward, weight gradients accumulated in TMEM across tiles
-  const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
-  for (int t = 0; t < tiles; ++t) {
-    const int r = t * 128 + tid;
-    const bool in = r < rows;
-    const int pl = in ? r / D : 0, d = in ? r % D : 0;
-    const float4 f = in ? feats[(p0 + pl) * D + d] : make_float4(0.f, 0.f, 0.f, 0.f);
-    // forward again, keeping pre-activations; X row (with the bias 1) for dW1
-    float f0, f1, f2;
-    features(S->ms, f.x, f.y, f.z, f0, f1, f2);
-    float xin[16] = {f0, f1, f2, 1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    write_row_kmajor(sX, tid, xin, 2, kXLbo, kXSbo);
-    float a1[kH], a2[kH], h2[kH];
-    layer1_row(S->ms.l1, f0, f1, f2, sH, tid, a1);
-    tc::fence_smem_to_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (tid == 0) {
-      const uint32_t idesc = tc::idesc_bf16(128, kH, false, false);
-#pragma unroll
-      for (int s = 0; s < 4; ++s)
-        tc::mma_bf16(t_d2, tc::smem_desc(smem_addr(sH) + 2u * s * kHLbo, kHLbo, kHSbo),
-                     tc::smem_desc(smem_addr(sW2) + 2u * s * kW2Lbo, kW2Lbo, kW2Sbo), idesc, s > 0 ? 1u : 0u);
-      tc::commit(&S->bar);
-    }
-    mlp_collect(tid, S->ms, t_d2, &S->bar, phase, a.dev_status, a2, h2);
-    const float d3 = in ? -2.f * S->resid[pl] * ds_rows[r] * inv_B : 0.f;
-    float d2[kH];
-#pragma unroll
-    for (int j = 0; j < kH; ++j) d2[j] = d3 * S->ms.w3[j] * dsilu_fast(a2[j]);
+  __syncthreads();
+  const float d3 = in ? -2.f * S->resid[pl] * dsv * inv_B : 0.f;
+  {
     float b3p = d3;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) b3p += __shfl_xor_sync(0xffffffffu, b3p, off);
-    if (lane == 0) S->b3acc[warp] += b3p;
-    write_row_kmajor(sD2, tid, d2, 8, kHLbo, kHSbo);
-    write_row_kmajor(sH2, tid, h2, 8, kHLbo, kHSbo);
-    // d3 into column 0 of the [16 x 128] MN-major operand (line of row r: n = 0..7)
-    *reinterpret_cast<uint4*>(sT3 + tc::mnmajor_off(0, tid, kOnesLbo, kOnesSbo)) =
-        make_uint4(pack_bf16x2(d3, 0.f), 0u, 0u, 0u);
-    tc::fence_smem_to_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (tid == 0) {
-      // d1pre = d2 W2: A = d2 [128 x 64] K-major, B = W2 read MN-major (N = in, K = out)
-      const uint32_t id_b1 = tc::idesc_bf16(128, kH, false, true);
-#pragma unroll
-      for (int s = 0; s < 4; ++s)
-        tc::mma_bf16(t_d3, tc::smem_desc(smem_addr(sD2) + 2u * s * kHLbo, kHLbo, kHSbo),
-                     tc::smem_desc(smem_addr(sW2) + 2u * s * kW2Sbo, kW2Sbo, kW2Lbo), id_b1, s > 0 ? 1u : 0u);
-      // dW2 += d2^T H1, db2 += d2^T 1, dw3 += h2^T d3 (A read MN-major with M = 64, K = rows)
-      const uint32_t id_w2 = tc::idesc_bf16(64, kH, true, true);
-      const uint32_t id_n16 = tc::idesc_bf16(64, 16, true, true);
-#pragma unroll
-      for (int s = 0; s < 8; ++s) {
-        const uint32_t acc = (t > 0 || s > 0) ? 1u : 0u;
-        const uint64_t dd2 = tc::smem_desc(smem_addr(sD2) + 2u * s * kHSbo, kHSbo, kHLbo);
-        tc::mma_bf16(t_dw2, dd2, tc::smem_desc(smem_addr(sH) + 2u * s * kHSbo, kHSbo, kHLbo), id_w2, acc);
-        tc::mma_bf16(t_db2, dd2, tc::smem_desc(smem_addr(sOnes) + 2u * s * kOnesLbo, kOnesLbo, kOnesSbo), id_n16,
-                     acc);
-        tc::mma_bf16(t_dw3, tc::smem_desc(smem_addr(sH2) + 2u * s * kHSbo, kHSbo, kHLbo),
-                     tc::smem_desc(smem_addr(sT3) + 2u * s * kOnesLbo, kOnesLbo, kOnesSbo), id_n16, acc);
-      }
-      tc::commit(&S->bar);
-    }
-    mma_wait(&S->bar, phase, a.dev_status);
-    float d1[kH];
-#pragma unroll
-    for (int c = 0; c < kH; c += 16) tc::tmem_ld16(t_d3 + lane_base + (uint32_t)c, d1 + c);
-#pragma unroll
-    for (int j = 0; j < kH; ++j) d1[j] = in ? d1[j] * dsilu_fast(a1[j]) : 0.f;
-    write_row_kmajor(sD1, tid, d1, 8, kHLbo, kHSbo);
-    tc::fence_smem_to_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (tid == 0) {
-      // dW1 += d1^T X: A = d1 read MN-major (M = hidden), B = X read MN-major (N = feature), K = rows
-      const uint32_t id_w1 = tc::idesc_bf16(64, 16, true, true);
-#pragma unroll
-      for (int s = 0; s < 8; ++s)
-        tc::mma_bf16(t_dw1, tc::smem_desc(smem_addr(sD1) + 2u * s * kHSbo, kHSbo, kHLbo),
-                     tc::smem_desc(smem_addr(sX) + 2u * s * kXSbo, kXSbo, kXLbo), id_w1,
-                     (t > 0 || s > 0) ? 1u : 0u);
-      tc::commit(&S->bar);
-    }
-    mma_wait(&S->bar, phase, a.dev_status);
+    if (lane == 0) S->wb3[warp] = b3p;
   }
-  // ---- write this CTA's gradient partials
+  *reinterpret_cast<uint4*>(sT3 + tc::mnmajor_off(0, r, kOnesLbo, kOnesSbo)) =
+      make_uint4(pack_bf16x2(d3, 0.f), 0u, 0u, 0u);
+  // H1 row scaled by d3 (the B operand of dW2)
+  {
+    const uint32_t d3p = pack_bf16x2(d3, d3);
+#pragma unroll
+    for (int jc = 0; jc < 8; ++jc) {
+      uint4* line = reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, 8 * jc, kHLbo, kHSbo));
+      uint4 w = *line;
+      w.x = bf2_mul(w.x, d3p);
+      w.y = bf2_mul(w.y, d3p);
+      w.z = bf2_mul(w.z, d3p);
+      w.w = bf2_mul(w.w, d3p);
+      *line = w;
+    }
+  }
+  // d1 = d3 (Q2 W2) (.) SiLU'(a1)
+  mma_wait(&S->bar, phase, a.dev_status);
+#pragma unroll
+  for (int c = 0; c < kH; c += 16) {
+    float p2[16], a1[16];
+    tc::tmem_ld16(t_fwd + lane_base + (uint32_t)c, p2);
+    tc::tmem_ld16(t_a1 + lane_base + (uint32_t)c, a1);
+#pragma unroll
+    for (int h = 0; h < 16; h += 8) {
+      uint32_t dp[4];
+#pragma unroll
+      for (int j = 0; j < 8; j += 2)
+        dp[j >> 1] = bf2_mul(pack_bf16x2(d3 * p2[h + j], d3 * p2[h + j + 1]),
+                             dsilu_bf16x2(pack_bf16x2(a1[h + j], a1[h + j + 1])));
+      *reinterpret_cast<uint4*>(sD1 + tc::kmajor_off(r, c + h, kHLbo, kHSbo)) = make_uint4(dp[0], dp[1], dp[2], dp[3]);
+    }
+  }
+  tc::fence_smem_to_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (tid == 0) {
+    // weight gradients, K = rows: A read MN-major with M = 64 (hidden)
+    const uint32_t id_w2 = tc::idesc_bf16(64, kH, true, true);
+    const uint32_t id_n16 = tc::idesc_bf16(64, 16, true, true);
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      const uint32_t acc = s > 0 ? 1u : 0u;
+      const uint64_t dq2 = tc::smem_desc(smem_addr(sQ2) + 2u * s * kHSbo, kHSbo, kHLbo);
+      const uint64_t dt3 = tc::smem_desc(smem_addr(sT3) + 2u * s * kOnesLbo, kOnesLbo, kOnesSbo);
+      tc::mma_bf16(t_dw2, dq2, tc::smem_desc(smem_addr(sH) + 2u * s * kHSbo, kHSbo, kHLbo), id_w2, acc);
+      tc::mma_bf16(t_db2, dq2, dt3, id_n16, acc);
+      tc::mma_bf16(t_dw3, tc::smem_desc(smem_addr(sH2) + 2u * s * kHSbo, kHSbo, kHLbo), dt3, id_n16, acc);
+      tc::mma_bf16(t_dw1, tc::smem_desc(smem_addr(sD1) + 2u * s * kHSbo, kHSbo, kHLbo),
+                   tc::smem_desc(smem_addr(sX) + 2u * s * kXSbo, kXSbo, kXLbo), id_n16, acc);
+    }
+    tc::commit(&S->bar);
+  }
+  mma_wait(&S->bar, phase, a.dev_status);
+  // ---- this CTA's gradient partials.  M = 64 accumulators: row m lives in
+  // lane 32 (m / 16) + m % 16.
   float* G = a.grad_partials + (size_t)blockIdx.x * kGradWidth;
   {
-    // M = 64 accumulators: row m lives in lane 32 (m / 16) + m % 16.
     float v[kH];
 #pragma unroll
     for (int c = 0; c < kH; c += 16) tc::tmem_ld16(t_dw2 + lane_base + (uint32_t)c, v + c);
@@ -626,45 +671,64 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
     tc::tmem_ld16(t_dw3 + lane_base, vw3);
     if (lane < 16) {
       const int m = 16 * warp + lane;
+      float4* gw2 = reinterpret_cast<float4*>(G + kOffW2 + m * kH);
 #pragma unroll
-      for (int j = 0; j < kH; ++j) G[kOffW2 + m * kH + j] = v[j];
+      for (int j = 0; j < kH / 4; ++j) gw2[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
       G[kOffB2 + m] = vb[0];
       G[kOffW3 + m] = vw3[0];
+      float4* gw1 = reinterpret_cast<float4*>(G + kOffW1 + m * kIn);
+      gw1[0] = make_float4(vw1[0], vw1[1], vw1[2], vw1[3]);
 #pragma unroll
-      for (int j = 0; j < kIn; ++j) G[kOffW1 + m * kIn + j] = j < 4 ? vw1[j] : 0.f;
+      for (int j = 1; j < kIn / 4; ++j) gw1[j] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
   }
-  __syncthreads();
   if (tid == 0) {
-    float s = 0.f;
-    for (int w = 0; w < 4; ++w) s += S->b3acc[w];
-    G[kOffB3] = s;
-    G[kOffC] = S->cacc;
-    G[kNumParams] = S->lossacc;
+    float l = 0.f, cs = 0.f, b3 = 0.f;
+    for (int w = 0; w < 4; ++w) {
+      l += S->wloss[w];
+      cs += S->wsum[w];
+      b3 += S->wb3[w];
+    }
+    G[kOffB3] = b3;
+    G[kOffC] = -2.f * cs * inv_B;
+    G[kNumParams] = l * inv_B;
+    G[kNumParams + 1] = 0.f;
   }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(tm, 256);
+    tc::tmem_dealloc(tm, 128);
   }
 }
 
-// 256 TMEM columns per training CTA; >= 76 KB of shared memory keeps at most
-// two such CTAs on an SM (2 x 256 = 512 columns).
-size_t train_smem_bytes(int dates, int paths) {
-  size_t total = ((sizeof(TrainSmem) + 1023) & ~(size_t)1023) + kW2Bytes + kXBytes + 4 * kHBytes + 2 * 16 * 128 * 2 +
-                 (size_t)2 * paths * dates * sizeof(float);
-  if (total < 76 * 1024) total = 76 * 1024;
-  return total;
+// 128 TMEM columns and ~86 KB of shared memory per training CTA: two CTAs
+// share an SM.
+size_t train_smem_bytes() {
+  return ((sizeof(TrainSmem) + 1023) & ~(size_t)1023) + kW2Bytes + kW1Bytes + kXBytes + 4 * kHBytes + 16 * 128 * 2;
 }
 
 // ---- Adam ------------------------------------------------------------------------------
-__global__ void mlp_adam_kernel(tqf_mlp_adam_args a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > kNumParams) return;
+// Block b owns parameters [32 b, 32 b + 32): thread (slice, lane) sums the
+// partials slice, slice + 32, ... of parameter 32 b + lane in order, then the
+// 32 slice sums are added in slice order (a fixed order for any launch).
+constexpr int kAdamSlices = 32;
+__global__ void __launch_bounds__(32 * kAdamSlices) mlp_adam_kernel(tqf_mlp_adam_args a) {
+  __shared__ float part[kAdamSlices][33];
+  const int lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
   float g = 0.f;
-  for (int b = 0; b < a.num_partials; ++b) g += a.grad_partials[(size_t)b * kGradWidth + i];
+  if (i <= kNumParams) {
+    const float* src = a.grad_partials + i;
+#pragma unroll 8
+    for (int b = slice; b < a.num_partials; b += kAdamSlices) g += src[(size_t)b * kGradWidth];
+  }
+  part[slice][lane] = g;
+  __syncthreads();
+  if (slice != 0 || i > kNumParams) return;
+  g = 0.f;
+#pragma unroll
+  for (int s2 = 0; s2 < kAdamSlices; ++s2) g += part[s2][lane];
   if (i == kNumParams) {
     if (a.loss_out) a.loss_out[0] = g;
     return;
@@ -719,6 +783,8 @@ extern "C" int tqf_heston_asian(const tqf_heston_asian_args* a, void* stream) {
     TQF_REQUIRE(a->pilot_feats && a->pilot_dS && a->pilot_Y, "tqf_heston_asian: pilot outputs required");
   if (a->mode == 2)
     TQF_REQUIRE(a->mlp.w2_bf16 && a->mlp.host, "tqf_heston_asian: network weights required (w2_bf16, host)");
+  if (a->mode == 2)
+    TQF_REQUIRE((reinterpret_cast<uintptr_t>(a->mlp.w2_bf16) & 15u) == 0, "tqf_heston_asian: w2_bf16 must be 16-byte aligned");
   const size_t smem = asian_smem_bytes(a->mode, a->num_steps);
   TQF_REQUIRE(smem <= 227 * 1024, "tqf_heston_asian: step table too large for shared memory");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -778,15 +844,18 @@ extern "C" int tqf_mlp_train_step(const tqf_mlp_train_args* a, void* stream) {
   clear_error();
   TQF_REQUIRE(a != nullptr, "tqf_mlp_train_step: null args");
   TQF_REQUIRE(a->num_dates >= 1 && a->num_dates <= kMaxDates, "tqf_mlp_train_step: bad num_dates");
-  TQF_REQUIRE(a->paths_per_cta >= 1 && a->paths_per_cta <= kTrainPaths,
-              "tqf_mlp_train_step: paths_per_cta must be in [1, %d]", kTrainPaths);
+  TQF_REQUIRE(a->paths_per_cta >= 1 && a->paths_per_cta * a->num_dates <= 128,
+              "tqf_mlp_train_step: paths_per_cta x num_dates must be in [1, 128]");
   TQF_REQUIRE(a->batch_paths >= a->paths_per_cta && a->batch_paths % a->paths_per_cta == 0,
               "tqf_mlp_train_step: batch_paths must be a positive multiple of paths_per_cta");
   TQF_REQUIRE(a->feats && a->dS && a->Y && a->params && a->w1_bf16 && a->w2_bf16 && a->grad_partials,
               "tqf_mlp_train_step: null pointer");
+  TQF_REQUIRE((reinterpret_cast<uintptr_t>(a->feats) & 15u) == 0 && (reinterpret_cast<uintptr_t>(a->w2_bf16) & 15u) == 0 &&
+                  (reinterpret_cast<uintptr_t>(a->grad_partials) & 15u) == 0 &&
+                  (reinterpret_cast<uintptr_t>(a->w1_bf16) & 7u) == 0,
+              "tqf_mlp_train_step: feats, w2_bf16 and grad_partials must be 16-byte aligned, w1_bf16 8-byte aligned");
   const int grid = a->batch_paths / a->paths_per_cta;
-  const size_t smem = train_smem_bytes(a->num_dates, a->paths_per_cta);
-  TQF_REQUIRE(smem <= 227 * 1024, "tqf_mlp_train_step: too many dates");
+  const size_t smem = train_smem_bytes();
   set_smem_config(mlp_train_step_kernel, smem);
   mlp_train_step_kernel<<<grid, kTrainThreads, smem, static_cast<cudaStream_t>(stream)>>>(*a);
   return check_launch("mlp_train_step_kernel");
@@ -797,8 +866,7 @@ extern "C" int tqf_mlp_adam(const tqf_mlp_adam_args* a, void* stream) {
   TQF_REQUIRE(a && a->params && a->m && a->v && a->grad_partials && a->w1_bf16 && a->w2_bf16,
               "tqf_mlp_adam: null pointer");
   TQF_REQUIRE(a->num_partials >= 1, "tqf_mlp_adam: num_partials must be >= 1");
-  const int threads = 256;
-  const int blocks = (kNumParams + 1 + threads - 1) / threads;
-  mlp_adam_kernel<<<blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(*a);
+  const int blocks = (kNumParams + 1 + 31) / 32;
+  mlp_adam_kernel<<<blocks, 32 * kAdamSlices, 0, static_cast<cudaStream_t>(stream)>>>(*a);
   return check_launch("mlp_adam_kernel");
 }

@@ -43,7 +43,6 @@ OFF_W3 = OFF_B2 + 64
 OFF_B3 = OFF_W3 + 64
 OFF_C = OFF_B3 + 1
 NUM_PARAMS = OFF_C + 1
-TRAIN_PATHS_PER_CTA = 8
 
 
 @dataclasses.dataclass
@@ -99,6 +98,8 @@ class HestonAsianCV:
         self.feat_shift = [0.0, math.log(spot), theta]
         self.feat_scale = [1.0 / expiry, 1.0 / math.sqrt(theta * expiry),
                            1.0 / max(volvol * math.sqrt(theta / (2 * mean_reversion)), 1e-6)]
+        # one training CTA holds whole paths in one 128-row tile
+        self.train_paths_per_cta = max(1, 128 // self.num_dates)
         self._init_params(init_seed)
         self.loss_history: list[float] = []
         self.train_seconds = 0.0
@@ -186,7 +187,7 @@ class HestonAsianCV:
         t = _lib.MlpTrainArgs()
         t.num_dates = self.num_dates
         t.batch_paths = int(batch_paths)
-        t.paths_per_cta = TRAIN_PATHS_PER_CTA
+        t.paths_per_cta = self.train_paths_per_cta
         t.path_begin = int(path_begin)
         t.feats, t.dS, t.Y = self.feats.data_ptr(), self.dS.data_ptr(), self.Y.data_ptr()
         t.params = self.params.data_ptr()
@@ -200,22 +201,29 @@ class HestonAsianCV:
 
     def gradient(self, path_begin, batch_paths):
         """(grad [NUM_PARAMS], loss) of one minibatch (for tests)."""
-        n_cta = batch_paths // TRAIN_PATHS_PER_CTA
-        partials = torch.zeros((n_cta, NUM_PARAMS + 1), dtype=torch.float32, device=self.device)
+        if batch_paths % self.train_paths_per_cta:
+            raise ValueError(f"batch_paths must be a multiple of {self.train_paths_per_cta}")
+        n_cta = batch_paths // self.train_paths_per_cta
+        partials = torch.zeros((n_cta, NUM_PARAMS + 2), dtype=torch.float32, device=self.device)
         _lib.call("tqf_mlp_train_step", self._train_args(path_begin, batch_paths, partials), _lib.stream_ptr())
         s = partials.sum(0)
         return s[:NUM_PARAMS], float(s[NUM_PARAMS])
 
-    def train(self, steps=2000, batch_paths=1024, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, graph=True):
+    def train(self, steps=2000, batch_paths=1024, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, graph=True,
+              init_intercept=True):
         """Adam on minibatches of pilot paths taken in order (wrapping).  The
         2 x steps kernel launches are captured once into a CUDA graph and
         replayed (graph=True) so that host launch overhead stays out of the
-        loop; ``train_seconds`` is the GPU time of the replay."""
-        if batch_paths % TRAIN_PATHS_PER_CTA:
-            raise ValueError(f"batch_paths must be a multiple of {TRAIN_PATHS_PER_CTA}")
+        loop; ``train_seconds`` is the GPU time of the replay.  Before the
+        first step the loss offset c starts at the pilot mean of Y
+        (init_intercept), so that the residuals start centred."""
+        if batch_paths % self.train_paths_per_cta:
+            raise ValueError(f"batch_paths must be a multiple of {self.train_paths_per_cta}")
         d = self.device
-        n_cta = batch_paths // TRAIN_PATHS_PER_CTA
-        partials = torch.zeros((n_cta, NUM_PARAMS + 1), dtype=torch.float32, device=d)
+        if init_intercept and self.adam_t == 0:
+            self.params[OFF_C] = self.Y[: self.num_pilot].double().mean().float()
+        n_cta = batch_paths // self.train_paths_per_cta
+        partials = torch.zeros((n_cta, NUM_PARAMS + 2), dtype=torch.float32, device=d)
         losses = torch.zeros(steps, dtype=torch.float32, device=d)
         lib = _lib.load()
         span = self.num_pilot - batch_paths
