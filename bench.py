@@ -360,7 +360,7 @@ def run_gpu(args, rank, world, local_rank):
     return line
 
 
-def run_neural_cv(pilot_paths=1 << 20, train_steps=2000, eval_paths=1 << 26, batch_paths=1024):
+def run_neural_cv(pilot_paths=1 << 20, train_steps=2000, eval_paths=1 << 26, batch_paths=512):
     """Config C5: Heston arithmetic-Asian call (52 dates, K=100) — pilot paths,
     2,000 Adam steps (lr 1e-3) on the tcgen05 training kernels, then fused CV
     pricing vs plain MC on the same evaluation paths; time to a 1e-4 relative
@@ -549,6 +549,7 @@ def main():
     ap.add_argument("--cv-only", action="store_true", help="run only the neural-CV measurement (small sizes ok)")
     ap.add_argument("--cv-eval-paths", type=int, default=1 << 26)
     ap.add_argument("--cv-train-steps", type=int, default=2000)
+    ap.add_argument("--cv-batch", type=int, default=512, help="pilot paths per Adam step")
     ap.add_argument("--no-basket", action="store_true")
     ap.add_argument("--basket-only", action="store_true", help="run only the 16-asset basket measurement")
     ap.add_argument("--basket-paths", type=int, default=1 << 22)
@@ -589,7 +590,8 @@ def main():
         print(json.dumps({"basket": run_basket(paths_n=args.basket_paths)}))
         return
     if args.cv_only:
-        print(json.dumps({"neural_cv": run_neural_cv(eval_paths=args.cv_eval_paths, train_steps=args.cv_train_steps)}))
+        print(json.dumps({"neural_cv": run_neural_cv(eval_paths=args.cv_eval_paths, train_steps=args.cv_train_steps,
+                                                  batch_paths=args.cv_batch)}))
         return
     if world > 1:
         import torch
@@ -604,7 +606,8 @@ def main():
                "sample": f"oracle full-truncation Euler (numpy f32), {cores} procs x {ppc} paths x {N_STEPS} steps, 2 timed rounds, incl. RNG + 64-strike payoff"}
     line = run_gpu(args, rank, world, local_rank)
     if rank == 0 and world == 1 and not args.no_neural_cv:
-        line["neural_cv"] = run_neural_cv(eval_paths=args.cv_eval_paths, train_steps=args.cv_train_steps)
+        line["neural_cv"] = run_neural_cv(eval_paths=args.cv_eval_paths, train_steps=args.cv_train_steps,
+                                                  batch_paths=args.cv_batch)
     if rank == 0 and world == 1 and not args.no_basket:
         line["basket"] = run_basket(paths_n=args.basket_paths)
     if rank == 0 and world == 1 and not args.no_sobol:

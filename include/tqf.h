@@ -599,12 +599,16 @@ typedef struct tqf_mlp_weights {
 /* Full-truncation Euler Heston paths (Philox in-kernel, FP32) with an
  * arithmetic-Asian payoff Y = discount_T max(mean_k S(t_k) - strike, 0) over
  * num_dates monitoring dates marked in the step table's slot column (date
- * index, -1 otherwise; table layout of tqf_heston_euler).  date_table
+ * index, -1 otherwise; table layout of tqf_heston_euler).  Mode 2 also reads
+ * slot -2 as "advance the network pipeline one stage here"; two such steps
+ * between consecutive dates let the tensor-core work overlap the stepping
+ * (without them every stage runs at the date).  date_table
  * [num_dates][4] = (t_k, exp(-r t_k), 0, 0).
  *  mode 0: out[5] (device, FP64) = sums of (Y, Y^2, 0, 0, 0);
- *  mode 1: pilot data: pilot_feats [N][num_dates][4] = (t, log S, v, 0) at
- *          each interval start, pilot_dS [N][num_dates] discounted-spot
- *          increments, pilot_Y [N];
+ *  mode 1: pilot data, date-major so that the stores coalesce:
+ *          pilot_feats [num_dates][N][4] = (t, log S, v, 0) at each interval
+ *          start, pilot_dS [num_dates][N] discounted-spot increments,
+ *          pilot_Y [N];
  *  mode 2: out[5] = sums of (Y, Y^2, C, C^2, Y C), C = sum_k g_k dS~_k the
  *          martingale control variate with the network evaluated on the
  *          tensor cores at every interval start.
@@ -654,8 +658,9 @@ typedef struct tqf_mlp_train_args {
   int32_t paths_per_cta; /* paths_per_cta x num_dates <= 128: one CTA = one 128-row tile */
   int32_t pad0;
   int64_t path_begin;
-  const float* feats; /* [N][num_dates][4], 16-byte aligned */
-  const float* dS;    /* [N][num_dates] */
+  int64_t pilot_paths; /* N: the pilot data's path count (its date stride) */
+  const float* feats;  /* [num_dates][N][4] (tqf_heston_asian mode 1), 16-byte aligned */
+  const float* dS;     /* [num_dates][N] */
   const float* Y;     /* [N] */
   const float* params;
   const void* w1_bf16;

@@ -114,3 +114,15 @@ def test_trained_control_variate_is_unbiased_and_reduces_variance(cuda):
     assert abs(est.mean_control) < 5 * est.se_control  # E[C] = 0
     assert est.vrf > 5.0, est.vrf
     assert abs(est.price - est.plain_price) < 5 * est.plain_standard_error
+
+
+def test_fused_inference_pipeline_staging_is_exact(cuda):
+    """The inference pipeline stages run at marked steps or all at the date:
+    the same arithmetic either way, so the five sums agree bit for bit."""
+    from tqf.pricing import HestonAsianCV
+    a = HestonAsianCV(**KW, init_seed=5)
+    b = HestonAsianCV(**KW, init_seed=5, pipeline_stages=False)
+    ea = a.price(1 << 15, control_variate=True, seed=(4, 4))
+    eb = b.price(1 << 15, control_variate=True, seed=(4, 4))
+    assert (ea.price, ea.mean_control, ea.var_cv) == (eb.price, eb.mean_control, eb.var_cv)
+    assert ea.mean_control != 0.0

@@ -123,3 +123,17 @@ def test_lsm_host_basis_and_payoff_match_oracle():
     np.testing.assert_allclose(pay, olsm.basket_put_payoff(x, 1, [1.0, 1.1]), rtol=1e-14)
     d = _discount_table([0.9, 0.8], 2, np.float64)
     assert d.shape == (3, 1, 1) and d[0, 0, 0] == 1.0 and d[2, 0, 0] == 0.8
+
+
+def test_cv_pipeline_stage_marks():
+    """Two pipeline steps strictly inside every interval of at least three
+    steps, one for two, none for one; never on a date."""
+    from tqf.pricing.neural_cv import stage_marks
+    dates = np.array([4, 9, 13, 14, 16, 19])
+    m = stage_marks(dates)
+    assert m.tolist() == [1, 2, 6, 7, 10, 12, 15, 17, 18]
+    assert not set(m.tolist()) & set(dates.tolist())
+    # the Asian configuration: 52 dates on 252 steps
+    ti = np.round(np.arange(1, 53) * 252 / 52).astype(int)
+    m = stage_marks(ti - 1)
+    assert len(m) == 2 * 52 and np.all(np.diff(m) > 0)

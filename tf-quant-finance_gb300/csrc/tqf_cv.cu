@@ -40,7 +40,8 @@ constexpr int kH = 64;            // hidden width
 constexpr int kIn = 16;           // padded input width (K of layer 1)
 constexpr int kMaxDates = 64;
 constexpr int kPathThreads = 256;  // two warpgroups
-constexpr int kTrainThreads = 128;
+constexpr int kCvCtasPerSm = 4;    // fused-inference CTAs per SM (4 x 128 TMEM columns = 512)
+constexpr int kTrainThreads = 256;  // two threads per tile row
 // parameter vector layout (FP32 master copy)
 constexpr int kOffW1 = 0;
 constexpr int kOffW2 = kOffW1 + kH * kIn;   // 1024
@@ -105,30 +106,14 @@ __device__ __forceinline__ uint32_t dsilu_bf16x2(uint32_t x2) {
   return bf2_mul(sg, bf2_fma(x2, om, kBf2One));
 }
 
-// Layer 1 on the CUDA cores (K = 3 is not GEMM-shaped): a1_j = w1_j . (f0,
-// f1, f2) + b1_j with BF16-rounded operands (exact products, FP32 sums, as
-// the tensor cores would form them), SiLU in packed BF16, written as row r of
-// the K-major H tile.  s_l1[j] = (w_j0, w_j1, w_j2, b1_j).  If a1 is given,
-// the FP32 pre-activations are also returned.
-__device__ __forceinline__ void layer1_row(const float4* __restrict__ s_l1, float f0, float f1, float f2,
-                                           unsigned char* sH, int r, float* a1 = nullptr) {
-#pragma unroll
-  for (int jc = 0; jc < 8; ++jc) {
-    uint32_t pk[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const float4 wa = s_l1[8 * jc + 2 * q];
-      const float4 wb = s_l1[8 * jc + 2 * q + 1];
-      const float aa = fmaf(wa.x, f0, fmaf(wa.y, f1, fmaf(wa.z, f2, wa.w)));
-      const float ab = fmaf(wb.x, f0, fmaf(wb.y, f1, fmaf(wb.z, f2, wb.w)));
-      if (a1) {
-        a1[8 * jc + 2 * q] = aa;
-        a1[8 * jc + 2 * q + 1] = ab;
-      }
-      pk[q] = silu_bf16x2(aa, ab);
-    }
-    *reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, 8 * jc, kHLbo, kHSbo)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-  }
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start before the previous kernel in the stream has
+// finished; grid_dependency_wait() blocks until that kernel has completed and
+// its memory is visible (a no-op for an ordinary launch), and
+// allow_dependent_launch() lets the next such kernel start launching.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void allow_dependent_launch() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 // Warpgroup barrier (named barrier 1 or 2, 128 threads).  Immediate barrier
@@ -144,23 +129,15 @@ __device__ __forceinline__ void wg_sync(int wg) {
 // Bounded wait on an MMA-completion mbarrier; on time-out records the status
 // and waits once more (bounded) so that no MMA is in flight afterwards.
 __device__ __forceinline__ bool mma_wait(uint64_t* bar, uint32_t& phase, int32_t* status) {
-  bool ok = mbar_wait_bounded(bar, phase);
+  bool ok = mbar_wait_suspend(bar, phase);
   if (!ok) {
     if (status) atomicExch(status, TQF_E_TIMEOUT);
-    ok = mbar_wait_bounded(bar, phase);
+    ok = mbar_wait_suspend(bar, phase);
   }
   phase ^= 1u;
   tc::fence_after_sync();
   return ok;
 }
-
-struct MlpScalars {
-  float4 l1[kH];  // (w_j0, w_j1, w_j2, b1_j), BF16-rounded
-  float b2[kH];
-  float w3[kH];
-  float b3;
-  float fscale[3], fshift[3];
-};
 
 // The same network weights in kernel parameters (constant bank): inference
 // reads them as direct FMA operands, with no shared-memory load instructions.
@@ -181,63 +158,159 @@ __device__ __forceinline__ void features(const W& ms, float t, float x, float v,
   f2 = round_bf16((v - ms.fshift[2]) * ms.fscale[2]);
 }
 
-// Issue half of one network evaluation for the warpgroup's 128 rows: layer 1
-// on the CUDA cores into the H tile, then (one thread) layer 2 as four
-// tcgen05 MMAs into the warpgroup's 64 TMEM columns, committed to `bar`.
-template <class W>
-__device__ __forceinline__ void mlp_issue(int wg, int tid, const W& ms, unsigned char* sH,
-                                          const unsigned char* sW2, uint32_t tmem_d, uint64_t* bar, float t,
-                                          float x, float v) {
-  float f0, f1, f2;
-  features(ms, t, x, v, f0, f1, f2);
-  layer1_row(ms.l1, f0, f1, f2, sH, tid);
+// ---- fused inference: a three-stage tensor-core pipeline per warpgroup ---------
+// One evaluation of g for the warpgroup's 128 paths (one row each) is
+//   L1: a1 = X W1^T (X row = BF16 features, 1, 1; W1 column 3 = b1)
+//   S1: H = SiLU(a1); a2 = H W2^T + X B2^T (B2 columns 3, 4 = b2 split into
+//       BF16 high and low parts, so the bias is exact to ~2^-16)
+//   S2: H = SiLU(a2); (g_hi, g_lo) = H W3^T (W3 rows 0, 1 = w3 high / low)
+//   g = g_hi + g_lo + b3,
+// each stage a wait on the previous MMAs, a TMEM read, packed-BF16 SiLU into
+// the warpgroup's H tile and the next MMAs.  The path kernel runs S1 and S2
+// at marked steps between two monitoring dates, so the tensor-core latency
+// hides behind path stepping; at the date any stage still pending runs
+// there.  TMEM: the warpgroup's 64 columns hold a1, then a2, then g.
+constexpr uint32_t kW1Lbo = 1024, kW1Sbo = 128;  // W1, B2 [64 x 16] K-major
+constexpr int kW1Bytes = kH * kIn * 2;
+constexpr uint32_t kW3Lbo = 256, kW3Sbo = 128;   // W3 [16 x 64] K-major
+constexpr int kW3Bytes = 16 * kH * 2;
+
+struct EvalPipe {
+  unsigned char* sX;  // [128 x 16] this warpgroup's inputs
+  unsigned char* sH;  // [128 x 64] its hidden activations
+  uint32_t tmem;      // its 64 TMEM columns
+  uint64_t* bar;
+  uint32_t phase;
+  int stage;          // 0 idle, 1 L1 in flight, 2 layer 2 in flight, 3 layer 3 in flight
+};
+
+// Makes this warpgroup's shared-memory tile writes and TMEM reads visible to
+// the MMAs that its first warp (thread 0 issues) starts next: warps 1-3
+// arrive on the warpgroup's named barrier and go on; warp 0 waits for all.
+__device__ __forceinline__ void wg_publish(int wg, int tid) {
   tc::fence_smem_to_async();
   tc::fence_before_sync();
-  wg_sync(wg);
-  tc::fence_after_sync();
+  if (tid < 32) {
+    wg_sync(wg);
+    tc::fence_after_sync();
+  } else if (wg == 0) {
+    asm volatile("bar.arrive 1, 128;" ::: "memory");
+  } else {
+    asm volatile("bar.arrive 2, 128;" ::: "memory");
+  }
+}
+
+// 16 FP32 TMEM columns of this thread's lane, without the wait.
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+// SiLU of this row's 64 TMEM accumulators (packed BF16) into row r of sH,
+// 32 columns per TMEM round trip.
+__device__ __forceinline__ void silu_row_from_tmem(uint32_t taddr, unsigned char* sH, int r) {
+#pragma unroll
+  for (int c = 0; c < kH; c += 32) {
+    uint32_t u[32];
+    tmem_ld16_nowait(taddr + (uint32_t)c, u);
+    tmem_ld16_nowait(taddr + (uint32_t)c + 16u, u + 16);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    float acc[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) acc[j] = __uint_as_float(u[j]);
+#pragma unroll
+    for (int h = 0; h < 32; h += 8)
+      *reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, c + h, kHLbo, kHSbo)) =
+          make_uint4(silu_bf16x2(acc[h], acc[h + 1]), silu_bf16x2(acc[h + 2], acc[h + 3]),
+                     silu_bf16x2(acc[h + 4], acc[h + 5]), silu_bf16x2(acc[h + 6], acc[h + 7]));
+  }
+}
+
+__device__ __forceinline__ void eval_issue_l1(int wg, int tid, const MlpConst& wc, EvalPipe& P,
+                                              const unsigned char* sW1, float t, float x, float v) {
+  float f0, f1, f2;
+  features(wc, t, x, v, f0, f1, f2);
+  *reinterpret_cast<uint4*>(P.sX + tc::kmajor_off(tid, 0, kXLbo, kXSbo)) =
+      make_uint4(pack_bf16x2(f0, f1), pack_bf16x2(f2, 1.f), pack_bf16x2(1.f, 0.f), 0u);
+  wg_publish(wg, tid);
+  if (tid == 0) {
+    tc::mma_bf16(P.tmem, tc::smem_desc(smem_addr(P.sX), kXLbo, kXSbo), tc::smem_desc(smem_addr(sW1), kW1Lbo, kW1Sbo),
+                 tc::idesc_bf16(128, kH, false, false), 0u);
+    tc::commit(P.bar);
+  }
+  P.stage = 1;
+}
+
+__device__ __forceinline__ void eval_stage1(int wg, int tid, EvalPipe& P, const unsigned char* sW2,
+                                            const unsigned char* sB2, int32_t* status) {
+  mma_wait(P.bar, P.phase, status);
+  silu_row_from_tmem(P.tmem + ((uint32_t)(32 * (tid >> 5)) << 16), P.sH, tid);
+  wg_publish(wg, tid);
   if (tid == 0) {
     const uint32_t idesc = tc::idesc_bf16(128, kH, false, false);
 #pragma unroll
     for (int s = 0; s < kH / 16; ++s)
-      tc::mma_bf16(tmem_d, tc::smem_desc(smem_addr(sH) + 2u * s * kHLbo, kHLbo, kHSbo),
+      tc::mma_bf16(P.tmem, tc::smem_desc(smem_addr(P.sH) + 2u * s * kHLbo, kHLbo, kHSbo),
                    tc::smem_desc(smem_addr(sW2) + 2u * s * kW2Lbo, kW2Lbo, kW2Sbo), idesc, s > 0 ? 1u : 0u);
-    tc::commit(bar);
+    tc::mma_bf16(P.tmem, tc::smem_desc(smem_addr(P.sX), kXLbo, kXSbo), tc::smem_desc(smem_addr(sB2), kW1Lbo, kW1Sbo),
+                 idesc, 1u);
+    tc::commit(P.bar);
   }
+  P.stage = 2;
 }
 
-// Completes an evaluation: waits for the MMAs, reads this row's 64 layer-2
-// accumulators, applies bias and SiLU (packed BF16) and the FP32 layer-3 dot
-// product.  Optionally returns the FP32 pre-activations a2 and the BF16
-// activations h2 (as floats).
-template <class W>
-__device__ __forceinline__ float mlp_collect(int tid, const W& ms, uint32_t tmem_d, uint64_t* bar,
-                                             uint32_t& phase, int32_t* status, float* a2 = nullptr,
-                                             float* h2 = nullptr) {
-  mma_wait(bar, phase, status);
-  const uint32_t lane_base = (uint32_t)(32 * ((tid >> 5) & 3)) << 16;
-  float g = ms.b3;
+__device__ __forceinline__ void eval_stage2(int wg, int tid, EvalPipe& P, const unsigned char* sW3, int32_t* status) {
+  mma_wait(P.bar, P.phase, status);
+  silu_row_from_tmem(P.tmem + ((uint32_t)(32 * (tid >> 5)) << 16), P.sH, tid);
+  wg_publish(wg, tid);
+  if (tid == 0) {
+    const uint32_t idesc = tc::idesc_bf16(128, 16, false, false);
 #pragma unroll
-  for (int c = 0; c < kH; c += 16) {
-    float acc[16];
-    tc::tmem_ld16(tmem_d + lane_base + (uint32_t)c, acc);
-#pragma unroll
-    for (int j = 0; j < 16; j += 2) {
-      const float aa = acc[j] + ms.b2[c + j], ab = acc[j + 1] + ms.b2[c + j + 1];
-      const uint32_t sp = silu_bf16x2(aa, ab);
-      const float ha = bf16_lo(sp), hb = bf16_hi(sp);
-      if (a2) {
-        a2[c + j] = aa;
-        a2[c + j + 1] = ab;
-      }
-      if (h2) {
-        h2[c + j] = ha;
-        h2[c + j + 1] = hb;
-      }
-      g = fmaf(ms.w3[c + j], ha, fmaf(ms.w3[c + j + 1], hb, g));
-    }
+    for (int s = 0; s < kH / 16; ++s)
+      tc::mma_bf16(P.tmem, tc::smem_desc(smem_addr(P.sH) + 2u * s * kHLbo, kHLbo, kHSbo),
+                   tc::smem_desc(smem_addr(sW3) + 2u * s * kW3Lbo, kW3Lbo, kW3Sbo), idesc, s > 0 ? 1u : 0u);
+    tc::commit(P.bar);
   }
-  tc::fence_before_sync();  // orders these TMEM reads before the next MMA into tmem_d
-  return g;
+  P.stage = 3;
+}
+
+__device__ __forceinline__ float eval_finish(int wg, int tid, const MlpConst& wc, EvalPipe& P,
+                                             const unsigned char* sW2, const unsigned char* sB2,
+                                             const unsigned char* sW3, int32_t* status) {
+  if (P.stage == 1) eval_stage1(wg, tid, P, sW2, sB2, status);
+  if (P.stage == 2) eval_stage2(wg, tid, P, sW3, status);
+  mma_wait(P.bar, P.phase, status);
+  uint32_t r0, r1;
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];"
+               : "=r"(r0), "=r"(r1)
+               : "r"(P.tmem + ((uint32_t)(32 * (tid >> 5)) << 16)));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  P.stage = 0;
+  return __uint_as_float(r0) + __uint_as_float(r1) + wc.b3;
+}
+
+// Weight tiles of the inference pipeline from the constant-bank copy.
+__device__ __forceinline__ void build_eval_tiles(const MlpConst& wc, unsigned char* sW1, unsigned char* sB2,
+                                                 unsigned char* sW3) {
+  for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x) {
+    const int n = i >> 4, k = i & 15;
+    const float4 l = wc.l1[n];
+    const float w = k == 0 ? l.x : k == 1 ? l.y : k == 2 ? l.z : k == 3 ? l.w : 0.f;
+    const float hi = round_bf16(wc.b2[n]);
+    const float b = k == 3 ? hi : k == 4 ? wc.b2[n] - hi : 0.f;
+    __nv_bfloat16 wb = __float2bfloat16_rn(w), bb = __float2bfloat16_rn(b);
+    *reinterpret_cast<__nv_bfloat16*>(sW1 + tc::kmajor_off(n, k, kW1Lbo, kW1Sbo)) = wb;
+    *reinterpret_cast<__nv_bfloat16*>(sB2 + tc::kmajor_off(n, k, kW1Lbo, kW1Sbo)) = bb;
+  }
+  for (int i = threadIdx.x; i < 16 * kH; i += blockDim.x) {
+    const int n = i / kH, k = i % kH;
+    const float hi = round_bf16(wc.w3[k]);
+    const float w = n == 0 ? hi : n == 1 ? wc.w3[k] - hi : 0.f;
+    *reinterpret_cast<__nv_bfloat16*>(sW3 + tc::kmajor_off(n, k, kW3Lbo, kW3Sbo)) = __float2bfloat16_rn(w);
+  }
 }
 
 // ---- path kernel -----------------------------------------------------------------
@@ -250,18 +323,22 @@ struct AsianSmem {
 };
 
 // Mode 2 pipelines the network with the simulation: the evaluation for
-// interval k is issued at its start date (layer 1 + the layer-2 MMAs) and
-// collected at its end date, so the tensor-core work overlaps the ~T/D of
-// path stepping in between.  Each warpgroup owns 64 TMEM columns.
+// interval k starts (layer 1) at its start date, advances one stage at each
+// step the table marks with slot -2, and completes at its end date.  Mode 2
+// reads the step table from global memory (L1-resident) so that its shared
+// memory stays under a quarter of the SM's.
 template <int MODE>
-__global__ void __launch_bounds__(kPathThreads, MODE == 2 ? 4 : 1)
+__global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : 1)
     heston_asian_kernel(tqf_heston_asian_args a, const __grid_constant__ MlpConst wc) {
   extern __shared__ __align__(1024) unsigned char smem[];
   AsianSmem* S = reinterpret_cast<AsianSmem*>(smem);
   unsigned char* tiles = smem + ((sizeof(AsianSmem) + 1023) & ~(size_t)1023);
   unsigned char* sW2 = tiles;
-  unsigned char* sHw = sW2 + kW2Bytes;  // 2 x [128 x 64]
-  float* table = reinterpret_cast<float*>(MODE == 2 ? sHw + 2 * kHBytes : tiles);  // [steps][8]
+  unsigned char* sW1 = sW2 + kW2Bytes;
+  unsigned char* sB2 = sW1 + kW1Bytes;
+  unsigned char* sW3 = sB2 + kW1Bytes;
+  unsigned char* sWg = sW3 + kW3Bytes;  // per warpgroup: X [128 x 16], H [128 x 64]
+  float* table = reinterpret_cast<float*>(tiles);  // modes 0, 1: [steps][8]
   const int tid = threadIdx.x & 127, wg = threadIdx.x >> 7;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int D = a.num_dates;
@@ -270,11 +347,16 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? 4 : 1)
     S->date_disc[i] = a.date_table[4 * i + 1];
   }
   for (int i = threadIdx.x; i < (kPathThreads / 32) * 5; i += blockDim.x) (&S->acc[0][0])[i] = 0.0;
-  for (int i = threadIdx.x; i < a.num_steps * 8; i += blockDim.x) table[i] = a.step_table[i];
+  if (MODE != 2)
+    for (int i = threadIdx.x; i < a.num_steps * 8; i += blockDim.x) table[i] = a.step_table[i];
+  EvalPipe P;
   if (MODE == 2) {
     const uint4* w2 = static_cast<const uint4*>(a.mlp.w2_bf16);
     for (int i = threadIdx.x; i < kH * kH / 8; i += blockDim.x)
       *reinterpret_cast<uint4*>(sW2 + tc::kmajor_off(i >> 3, 8 * (i & 7), kW2Lbo, kW2Sbo)) = w2[i];
+    build_eval_tiles(wc, sW1, sB2, sW3);
+    for (int i = threadIdx.x; i < 2 * (kXBytes + kHBytes) / 16; i += blockDim.x)
+      reinterpret_cast<uint4*>(sWg)[i] = make_uint4(0u, 0u, 0u, 0u);
     if (threadIdx.x == 0) {
       mbar_init(&S->bar[0], 1);
       mbar_init(&S->bar[1], 1);
@@ -285,10 +367,16 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? 4 : 1)
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  const uint32_t tmem_d = MODE == 2 ? S->tmem_slot + (uint32_t)(wg * kH) : 0u;
-  unsigned char* sH = sHw + wg * kHBytes;
-  uint64_t* bar = &S->bar[wg];
-  uint32_t phase = 0;
+  if (MODE == 2) {
+    P.sX = sWg + wg * (kXBytes + kHBytes);
+    P.sH = P.sX + kXBytes;
+    P.tmem = S->tmem_slot + (uint32_t)(wg * kH);
+    P.bar = &S->bar[wg];
+    P.phase = 0;
+    P.stage = 0;
+  }
+  const float4* gtab = reinterpret_cast<const float4*>(a.step_table);
+  const float4* stab = reinterpret_cast<const float4*>(table);
   const float K = (float)a.strike, discT = (float)a.discount_T, x0 = (float)a.x0, v0 = (float)a.v0;
   const float S0 = __expf(x0);
   const float inv_D = 1.f / (float)D;
@@ -300,8 +388,8 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? 4 : 1)
     const int64_t p = (valid ? path : 0) + a.draws.path_offset;
     const uint32_t plo = (uint32_t)p, phi = (uint32_t)((uint64_t)p >> 32);
     float x = x0, v = v0, avg = 0.f, cv = 0.f, prev = S0;
-    if (MODE == 2) mlp_issue(wg, tid, wc, sH, sW2, tmem_d, bar, 0.f, x0, v0);
-    if (MODE == 1 && valid) reinterpret_cast<float4*>(a.pilot_feats)[path * D] = make_float4(0.f, x0, v0, 0.f);
+    if (MODE == 2) eval_issue_l1(wg, tid, wc, P, sW1, 0.f, x0, v0);
+    if (MODE == 1 && valid) reinterpret_cast<float4*>(a.pilot_feats)[path] = make_float4(0.f, x0, v0, 0.f);
     float zbuf[4];
     for (int i = 0; i < a.num_steps; ++i) {
       if ((i & 1) == 0) {
@@ -311,8 +399,8 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? 4 : 1)
       }
       const float za = (i & 1) ? zbuf[2] : zbuf[0];
       const float zb = (i & 1) ? zbuf[3] : zbuf[1];
-      const float4 c0 = reinterpret_cast<const float4*>(table)[2 * i];
-      const float4 c1 = reinterpret_cast<const float4*>(table)[2 * i + 1];
+      const float4 c0 = MODE == 2 ? __ldg(gtab + 2 * i) : stab[2 * i];
+      const float4 c1 = MODE == 2 ? __ldg(gtab + 2 * i + 1) : stab[2 * i + 1];
       {
         const float vp = fmaxf(v, 0.f);
         const float sq = sqrt_approx(vp);
@@ -322,22 +410,26 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? 4 : 1)
         x = xn;
         v = vn;
       }
-      const int k = (int)c1.w;  // date index or -1 (uniform across the CTA)
+      const int k = (int)c1.w;  // date index, -1, or -2 (a pipeline stage; uniform across the CTA)
+      if (MODE == 2 && k == -2) {
+        if (P.stage == 1) eval_stage1(wg, tid, P, sW2, sB2, a.dev_status);
+        else if (P.stage == 2) eval_stage2(wg, tid, P, sW3, a.dev_status);
+      }
       if (k >= 0) {
         const float Sk = __expf(x);
         const float dsk = S->date_disc[k] * Sk - prev;
         avg += Sk;
         if (MODE == 2) {
-          const float g = mlp_collect(tid, wc, tmem_d, bar, phase, a.dev_status);
+          const float g = eval_finish(wg, tid, wc, P, sW2, sB2, sW3, a.dev_status);
           cv = fmaf(g, dsk, cv);
         }
         if (MODE == 1 && valid) {
-          a.pilot_dS[path * D + k] = dsk;
+          a.pilot_dS[k * N + path] = dsk;
           if (k + 1 < D)
-            reinterpret_cast<float4*>(a.pilot_feats)[path * D + k + 1] = make_float4(S->date_t[k], x, v, 0.f);
+            reinterpret_cast<float4*>(a.pilot_feats)[(k + 1) * N + path] = make_float4(S->date_t[k], x, v, 0.f);
         }
         prev = S->date_disc[k] * Sk;
-        if (MODE == 2 && k + 1 < D) mlp_issue(wg, tid, wc, sH, sW2, tmem_d, bar, S->date_t[k], x, v);
+        if (MODE == 2 && k + 1 < D) eval_issue_l1(wg, tid, wc, P, sW1, S->date_t[k], x, v);
       }
     }
     const float Y = discT * fmaxf(avg * inv_D - K, 0.f);
@@ -352,19 +444,19 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? 4 : 1)
       q[4] = q[0] * q[2];
 #pragma unroll
       for (int j = 0; j < 5; ++j) {
-        float s = q[j];
+        float sum = q[j];
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-        if (lane == 0) S->acc[warp][j] += (double)s;
+        for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+        if (lane == 0) S->acc[warp][j] += (double)sum;
       }
     }
   }
   tc::fence_before_sync();
   __syncthreads();
   if (MODE != 1 && threadIdx.x < 5) {
-    double s = 0.0;
-    for (int w = 0; w < kPathThreads / 32; ++w) s += S->acc[w][threadIdx.x];
-    static_cast<double*>(a.workspace)[(size_t)blockIdx.x * 5 + threadIdx.x] = s;
+    double sum = 0.0;
+    for (int w = 0; w < kPathThreads / 32; ++w) sum += S->acc[w][threadIdx.x];
+    static_cast<double*>(a.workspace)[(size_t)blockIdx.x * 5 + threadIdx.x] = sum;
   }
   if (MODE == 2 && warp == 0) {
     tc::fence_after_sync();
@@ -372,15 +464,12 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? 4 : 1)
   }
 }
 
-// Mode 2 holds W2 and two H tiles; its 45..56 KB of shared memory lets at most
-// 4 CTAs (4 x 128 TMEM columns = the SM's 512) share an SM, so no TMEM
-// allocation ever has to wait.
+// Mode 2 holds the weight tiles (14 KB) and per warpgroup an X and an H tile
+// (20 KB): with 128 TMEM columns per CTA, four CTAs share an SM.
 size_t asian_smem_bytes(int mode, int steps) {
   const size_t head = (sizeof(AsianSmem) + 1023) & ~(size_t)1023;
-  const size_t tiles = mode == 2 ? (size_t)kW2Bytes + 2 * kHBytes : 0;
-  size_t total = head + tiles + (size_t)steps * 8 * sizeof(float);
-  if (mode == 2 && total < 46 * 1024) total = 46 * 1024;
-  return total;
+  if (mode == 2) return head + kW2Bytes + 2 * kW1Bytes + kW3Bytes + 2 * (kXBytes + kHBytes);
+  return head + (size_t)steps * 8 * sizeof(float);
 }
 
 template <int MODE>
@@ -389,11 +478,12 @@ int asian_grid(int64_t n, size_t smem) {
   set_smem_config(k, smem);
   int occ = 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kPathThreads, smem) != cudaSuccess || occ < 1) occ = 1;
-  // The runtime reports one resident CTA for this tcgen05 kernel although its
-  // registers (64), shared memory and barriers allow four (ncu: all limits 4);
-  // size the persistent grid for four, the most whose 128 TMEM columns fit
-  // the SM's 512.
-  if (MODE == 2) occ = 4;
+  // The runtime's occupancy calculation admits one CTA per SM for any kernel
+  // that allocates TMEM (a query-only probe shows it for a trivial kernel),
+  // although this one's registers (64), shared memory and barriers allow
+  // four (ncu: all limits 4, four resident); size the persistent grid for
+  // four, the most whose 128 TMEM columns fit the SM's 512.
+  if (MODE == 2) occ = kCvCtasPerSm;
   int64_t g = (n + kPathThreads - 1) / kPathThreads;
   const int64_t cap = (int64_t)num_sms() * occ;
   if (g > cap) g = cap;
@@ -401,11 +491,13 @@ int asian_grid(int64_t n, size_t smem) {
 }
 
 // ---- training step ---------------------------------------------------------------------
-// One CTA = one warpgroup = one 128-row tile holding all num_dates rows of
-// paths_per_cta paths (paths_per_cta x num_dates <= 128), so the forward pass
-// runs once and the per-path residual never crosses CTAs.  With
-// q2 = w3 (.) SiLU'(a2) (known after the forward pass) and the per-row output
-// gradient d3 = -2 r_p dS_pk / B (known after the residual):
+// One CTA = one 128-row tile holding all num_dates rows of paths_per_cta
+// paths (paths_per_cta x num_dates <= 128), so the forward pass runs once and
+// the per-path residual never crosses CTAs.  Two threads share a row: warp w
+// reads TMEM lanes 32 (w % 4) .. + 31 and owns hidden columns
+// 32 (w / 4) .. + 31.  With q2 = w3 (.) SiLU'(a2) (known after the forward
+// pass) and the per-row output gradient d3 = -2 r_p dS_pk / B (known after
+// the residual):
 //   d2 = d3 q2,  d1 = d3 (Q2 W2) (.) SiLU'(a1),
 //   dW2 = Q2^T (d3 H1),  db2 = Q2^T d3,  dw3 = H2^T d3,  dW1 = D1^T X,
 // so the Q2 W2 product is issued before the residual is known and overlaps
@@ -415,9 +507,6 @@ int asian_grid(int64_t n, size_t smem) {
 // packed BF16, two values per instruction; its operands are BF16 anyway.
 // TMEM (128 columns): [64, 128) a1, then dW2; [0, 64) the layer-2
 // accumulator, then Q2 W2, then db2 | dw3 | dW1 (16 columns each).
-constexpr uint32_t kW1Lbo = 1024, kW1Sbo = 128;  // W1 [64 x 16] K-major
-constexpr int kW1Bytes = kH * kIn * 2;
-
 struct TrainSmem {
   uint64_t bar;
   uint32_t tmem_slot;
@@ -425,16 +514,21 @@ struct TrainSmem {
   float b2[kH];
   float w3[kH];
   uint32_t w3p[kH / 2];  // w3 as BF16 pairs
-  float4 fs;             // feature scale (x, y, z)
-  float4 fo;             // feature shift
   float b3, c;
-  float gds[128];     // g x dS~ per row
-  float resid[128];   // per path
-  float wloss[4], wsum[4], wb3[4];
+  float gpart[2][128];  // layer-3 partial sums of the two column halves
+  float ds[128];        // dS~ per row
+  float resid[128];     // per path
+  float Y[128];         // per path
+  float wloss[8], wsum[8], wb3[4];
 };
 
-__global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_train_args a) {
-  extern __shared__ __align__(1024) unsigned char smem[];
+// One training step's gradient for this CTA's tile: loads the pilot rows
+// and the current parameters, runs the forward and backward passes and
+// writes the CTA's gradient partials.  TMEM (128 columns), the MMA barrier
+// and the zeroed d3 tile are set up by the caller; `phase` is the MMA
+// barrier's parity, carried across calls.
+__device__ __forceinline__ void train_tile(const tqf_mlp_train_args& a, unsigned char* smem, uint32_t tm,
+                                           uint32_t& phase, bool dependent_launch, int tile, int tid) {
   TrainSmem* S = reinterpret_cast<TrainSmem*>(smem);
   unsigned char* t0 = smem + ((sizeof(TrainSmem) + 1023) & ~(size_t)1023);
   unsigned char* sW2 = t0;
@@ -448,9 +542,21 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
   const int D = a.num_dates;
   const int P = a.paths_per_cta;
   const int rows = P * D;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t p0 = a.path_begin + (int64_t)blockIdx.x * P;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int quarter = warp & 3, half = warp >> 2;
+  const int64_t p0 = a.path_begin + (int64_t)tile * P;
   const float inv_B = 1.f / (float)a.batch_paths;
+  // independent of the previous step: the pilot rows
+  if (tid < P) S->Y[tid] = a.Y[p0 + tid];
+  const int r = 32 * quarter + lane;
+  const int c0 = 32 * half;  // first hidden column of this thread
+  const bool in = r < rows;
+  const int pl = in ? r / D : 0, dd = in ? r % D : 0;
+  const int64_t gi = (int64_t)dd * a.pilot_paths + p0 + pl;
+  const float dsv = in ? a.dS[gi] : 0.f;
+  const float4 f = (in && half == 0) ? reinterpret_cast<const float4*>(a.feats)[gi] : make_float4(0.f, 0.f, 0.f, 0.f);
+  // the parameters (and the gradient buffer) belong to the previous step until it completes
+  if (dependent_launch) grid_dependency_wait();
   {
     // W2 (BF16 [64][64] row-major) and W1 (BF16 [64][16]) into K-major tiles
     const uint4* w2 = static_cast<const uint4*>(a.w2_bf16);
@@ -466,35 +572,16 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
     S->w3[i] = Pm[kOffW3 + i];
   }
   for (int i = tid; i < kH / 2; i += kTrainThreads) S->w3p[i] = pack_bf16x2(Pm[kOffW3 + 2 * i], Pm[kOffW3 + 2 * i + 1]);
-  for (int i = tid; i < 16 * 128 * 2 / 16; i += kTrainThreads)
-    reinterpret_cast<uint4*>(sT3)[i] = make_uint4(0u, 0u, 0u, 0u);
   if (tid == 0) {
     S->b3 = Pm[kOffB3];
     S->c = Pm[kOffC];
-    S->fs = make_float4(a.feat_scale[0], a.feat_scale[1], a.feat_scale[2], 0.f);
-    S->fo = make_float4(a.feat_shift[0], a.feat_shift[1], a.feat_shift[2], 0.f);
-    mbar_init(&S->bar, 1);
   }
-  if (warp == 0) tc::tmem_alloc(&S->tmem_slot, 128);
-  // this row's inputs
-  const int r = tid;
-  const bool in = r < rows;
-  const int pl = in ? r / D : 0, dd = in ? r % D : 0;
-  const int64_t gi = (p0 + pl) * D + dd;
-  const float4 f = in ? reinterpret_cast<const float4*>(a.feats)[gi] : make_float4(0.f, 0.f, 0.f, 0.f);
-  const float dsv = in ? a.dS[gi] : 0.f;
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  const uint32_t tm = S->tmem_slot;
-  const uint32_t t_fwd = tm, t_a1 = tm + 64, t_db2 = tm, t_dw3 = tm + 16, t_dw1 = tm + 32, t_dw2 = tm + 64;
-  const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
-  uint32_t phase = 0;
-  // ---- forward.  Layer 1: X row = (BF16 features, 1, 0...) -> a1 in TMEM
-  {
-    const float4 fs = S->fs, fo = S->fo;
-    const float f0 = round_bf16((f.x - fo.x) * fs.x), f1 = round_bf16((f.y - fo.y) * fs.y),
-                f2 = round_bf16((f.z - fo.z) * fs.z);
+  if (half == 0) {
+    // X row = (BF16 features, 1, 0, ...)
+    S->ds[r] = dsv;
+    const float f0 = round_bf16((f.x - a.feat_shift[0]) * a.feat_scale[0]);
+    const float f1 = round_bf16((f.y - a.feat_shift[1]) * a.feat_scale[1]);
+    const float f2 = round_bf16((f.z - a.feat_shift[2]) * a.feat_scale[2]);
     *reinterpret_cast<uint4*>(sX + tc::kmajor_off(r, 0, kXLbo, kXSbo)) =
         make_uint4(pack_bf16x2(f0, f1), pack_bf16x2(f2, 1.f), 0u, 0u);
     *reinterpret_cast<uint4*>(sX + tc::kmajor_off(r, 8, kXLbo, kXSbo)) = make_uint4(0u, 0u, 0u, 0u);
@@ -503,21 +590,27 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
+  const uint32_t t_fwd = tm, t_a1 = tm + 64, t_db2 = tm, t_dw3 = tm + 16, t_dw1 = tm + 32, t_dw2 = tm + 64;
+  const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;
+  // ---- forward.  Layer 1 -> a1 in TMEM
   if (tid == 0) {
     tc::mma_bf16(t_a1, tc::smem_desc(smem_addr(sX), kXLbo, kXSbo), tc::smem_desc(smem_addr(sW1), kW1Lbo, kW1Sbo),
                  tc::idesc_bf16(128, kH, false, false), 0u);
     tc::commit(&S->bar);
   }
   mma_wait(&S->bar, phase, a.dev_status);
+  {
+    uint32_t u[32];
+    tmem_ld16_nowait(t_a1 + lane_base + (uint32_t)c0, u);
+    tmem_ld16_nowait(t_a1 + lane_base + (uint32_t)c0 + 16u, u + 16);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int c = 0; c < kH; c += 16) {
-    float acc[16];
-    tc::tmem_ld16(t_a1 + lane_base + (uint32_t)c, acc);
-#pragma unroll
-    for (int h = 0; h < 16; h += 8)
-      *reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, c + h, kHLbo, kHSbo)) =
-          make_uint4(silu_bf16x2(acc[h], acc[h + 1]), silu_bf16x2(acc[h + 2], acc[h + 3]),
-                     silu_bf16x2(acc[h + 4], acc[h + 5]), silu_bf16x2(acc[h + 6], acc[h + 7]));
+    for (int h = 0; h < 32; h += 8)
+      *reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, c0 + h, kHLbo, kHSbo)) =
+          make_uint4(silu_bf16x2(__uint_as_float(u[h]), __uint_as_float(u[h + 1])),
+                     silu_bf16x2(__uint_as_float(u[h + 2]), __uint_as_float(u[h + 3])),
+                     silu_bf16x2(__uint_as_float(u[h + 4]), __uint_as_float(u[h + 5])),
+                     silu_bf16x2(__uint_as_float(u[h + 6]), __uint_as_float(u[h + 7])));
   }
   tc::fence_smem_to_async();
   tc::fence_before_sync();
@@ -533,37 +626,39 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
     tc::commit(&S->bar);
   }
   mma_wait(&S->bar, phase, a.dev_status);
-  // bias, SiLU (H2), layer 3 (g, FP32) and q2 = w3 SiLU'(a2) (Q2)
-  float g = S->b3;
-  const uint32_t keep = in ? 0xFFFFFFFFu : 0u;
+  // bias, SiLU (H2), this half's layer-3 partial sum and q2 = w3 SiLU'(a2) (Q2)
+  {
+    const uint32_t keep = in ? 0xFFFFFFFFu : 0u;
+    uint32_t u[32];
+    tmem_ld16_nowait(t_fwd + lane_base + (uint32_t)c0, u);
+    tmem_ld16_nowait(t_fwd + lane_base + (uint32_t)c0 + 16u, u + 16);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    float g = 0.f;
 #pragma unroll
-  for (int c = 0; c < kH; c += 16) {
-    float acc[16];
-    tc::tmem_ld16(t_fwd + lane_base + (uint32_t)c, acc);
-#pragma unroll
-    for (int h = 0; h < 16; h += 8) {
-      const float4 ba = *reinterpret_cast<const float4*>(&S->b2[c + h]);
-      const float4 bb = *reinterpret_cast<const float4*>(&S->b2[c + h + 4]);
-      const float4 wa = *reinterpret_cast<const float4*>(&S->w3[c + h]);
-      const float4 wb = *reinterpret_cast<const float4*>(&S->w3[c + h + 4]);
-      const uint4 wp = *reinterpret_cast<const uint4*>(&S->w3p[(c + h) / 2]);
+    for (int h = 0; h < 32; h += 8) {
+      const int col = c0 + h;
+      const float4 ba = *reinterpret_cast<const float4*>(&S->b2[col]);
+      const float4 bb = *reinterpret_cast<const float4*>(&S->b2[col + 4]);
+      const float4 wa = *reinterpret_cast<const float4*>(&S->w3[col]);
+      const float4 wb = *reinterpret_cast<const float4*>(&S->w3[col + 4]);
+      const uint4 wp = *reinterpret_cast<const uint4*>(&S->w3p[col / 2]);
       const float bias[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
       const float w3v[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
       const uint32_t w3pv[4] = {wp.x, wp.y, wp.z, wp.w};
       uint32_t hp[4], qp[4];
 #pragma unroll
       for (int j = 0; j < 8; j += 2) {
-        const float aa = acc[h + j] + bias[j], ab = acc[h + j + 1] + bias[j + 1];
+        const float aa = __uint_as_float(u[h + j]) + bias[j], ab = __uint_as_float(u[h + j + 1]) + bias[j + 1];
         const uint32_t sp = silu_bf16x2(aa, ab);
         g = fmaf(w3v[j], bf16_lo(sp), fmaf(w3v[j + 1], bf16_hi(sp), g));
         hp[j >> 1] = sp;
         qp[j >> 1] = bf2_mul(w3pv[j >> 1], dsilu_bf16x2(pack_bf16x2(aa, ab))) & keep;
       }
-      *reinterpret_cast<uint4*>(sH2 + tc::kmajor_off(r, c + h, kHLbo, kHSbo)) = make_uint4(hp[0], hp[1], hp[2], hp[3]);
-      *reinterpret_cast<uint4*>(sQ2 + tc::kmajor_off(r, c + h, kHLbo, kHSbo)) = make_uint4(qp[0], qp[1], qp[2], qp[3]);
+      *reinterpret_cast<uint4*>(sH2 + tc::kmajor_off(r, col, kHLbo, kHSbo)) = make_uint4(hp[0], hp[1], hp[2], hp[3]);
+      *reinterpret_cast<uint4*>(sQ2 + tc::kmajor_off(r, col, kHLbo, kHSbo)) = make_uint4(qp[0], qp[1], qp[2], qp[3]);
     }
+    S->gpart[half][r] = g;
   }
-  S->gds[r] = in ? g * dsv : 0.f;
   tc::fence_smem_to_async();
   tc::fence_before_sync();
   __syncthreads();
@@ -579,13 +674,17 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
   }
   // ---- per-path residuals r_p = Y_p - c - sum_k g_pk dS~_pk (one warp per path)
   {
+    const float b3 = S->b3;
     float wl = 0.f, ws = 0.f;
-    for (int p = warp; p < P; p += 4) {
+    for (int p = warp; p < P; p += kTrainThreads / 32) {
       float sum = 0.f;
-      for (int k = lane; k < D; k += 32) sum += S->gds[p * D + k];
+      for (int k = lane; k < D; k += 32) {
+        const int row = p * D + k;
+        sum = fmaf((S->gpart[0][row] + S->gpart[1][row]) + b3, S->ds[row], sum);
+      }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
-      const float rr = a.Y[p0 + p] - S->c - sum;
+      const float rr = S->Y[p] - S->c - sum;
       if (lane == 0) S->resid[p] = rr;
       wl = fmaf(rr, rr, wl);
       ws += rr;
@@ -597,20 +696,20 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
   }
   __syncthreads();
   const float d3 = in ? -2.f * S->resid[pl] * dsv * inv_B : 0.f;
-  {
+  if (half == 0) {
     float b3p = d3;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) b3p += __shfl_xor_sync(0xffffffffu, b3p, off);
-    if (lane == 0) S->wb3[warp] = b3p;
+    if (lane == 0) S->wb3[quarter] = b3p;
+    *reinterpret_cast<uint4*>(sT3 + tc::mnmajor_off(0, r, kOnesLbo, kOnesSbo)) =
+        make_uint4(pack_bf16x2(d3, 0.f), 0u, 0u, 0u);
   }
-  *reinterpret_cast<uint4*>(sT3 + tc::mnmajor_off(0, r, kOnesLbo, kOnesSbo)) =
-      make_uint4(pack_bf16x2(d3, 0.f), 0u, 0u, 0u);
-  // H1 row scaled by d3 (the B operand of dW2)
+  // this half of the H1 row scaled by d3 (the B operand of dW2)
   {
     const uint32_t d3p = pack_bf16x2(d3, d3);
 #pragma unroll
-    for (int jc = 0; jc < 8; ++jc) {
-      uint4* line = reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, 8 * jc, kHLbo, kHSbo));
+    for (int jc = 0; jc < 4; ++jc) {
+      uint4* line = reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, c0 + 8 * jc, kHLbo, kHSbo));
       uint4 w = *line;
       w.x = bf2_mul(w.x, d3p);
       w.y = bf2_mul(w.y, d3p);
@@ -621,19 +720,21 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
   }
   // d1 = d3 (Q2 W2) (.) SiLU'(a1)
   mma_wait(&S->bar, phase, a.dev_status);
+  {
+    uint32_t p2[32], a1[32];
+    tmem_ld16_nowait(t_fwd + lane_base + (uint32_t)c0, p2);
+    tmem_ld16_nowait(t_fwd + lane_base + (uint32_t)c0 + 16u, p2 + 16);
+    tmem_ld16_nowait(t_a1 + lane_base + (uint32_t)c0, a1);
+    tmem_ld16_nowait(t_a1 + lane_base + (uint32_t)c0 + 16u, a1 + 16);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int c = 0; c < kH; c += 16) {
-    float p2[16], a1[16];
-    tc::tmem_ld16(t_fwd + lane_base + (uint32_t)c, p2);
-    tc::tmem_ld16(t_a1 + lane_base + (uint32_t)c, a1);
-#pragma unroll
-    for (int h = 0; h < 16; h += 8) {
+    for (int h = 0; h < 32; h += 8) {
       uint32_t dp[4];
 #pragma unroll
       for (int j = 0; j < 8; j += 2)
-        dp[j >> 1] = bf2_mul(pack_bf16x2(d3 * p2[h + j], d3 * p2[h + j + 1]),
-                             dsilu_bf16x2(pack_bf16x2(a1[h + j], a1[h + j + 1])));
-      *reinterpret_cast<uint4*>(sD1 + tc::kmajor_off(r, c + h, kHLbo, kHSbo)) = make_uint4(dp[0], dp[1], dp[2], dp[3]);
+        dp[j >> 1] = bf2_mul(pack_bf16x2(d3 * __uint_as_float(p2[h + j]), d3 * __uint_as_float(p2[h + j + 1])),
+                             dsilu_bf16x2(pack_bf16x2(__uint_as_float(a1[h + j]), __uint_as_float(a1[h + j + 1]))));
+      *reinterpret_cast<uint4*>(sD1 + tc::kmajor_off(r, c0 + h, kHLbo, kHSbo)) = make_uint4(dp[0], dp[1], dp[2], dp[3]);
     }
   }
   tc::fence_smem_to_async();
@@ -659,53 +760,91 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_t
   }
   mma_wait(&S->bar, phase, a.dev_status);
   // ---- this CTA's gradient partials.  M = 64 accumulators: row m lives in
-  // lane 32 (m / 16) + m % 16.
-  float* G = a.grad_partials + (size_t)blockIdx.x * kGradWidth;
+  // lane 32 (m / 16) + m % 16; each half of the warps writes 32 columns of dW2.
+  float* G = a.grad_partials + (size_t)tile * kGradWidth;
   {
-    float v[kH];
-#pragma unroll
-    for (int c = 0; c < kH; c += 16) tc::tmem_ld16(t_dw2 + lane_base + (uint32_t)c, v + c);
-    float vb[16], vw1[16], vw3[16];
-    tc::tmem_ld16(t_db2 + lane_base, vb);
-    tc::tmem_ld16(t_dw1 + lane_base, vw1);
-    tc::tmem_ld16(t_dw3 + lane_base, vw3);
+    uint32_t v[32];
+    tmem_ld16_nowait(t_dw2 + lane_base + (uint32_t)c0, v);
+    tmem_ld16_nowait(t_dw2 + lane_base + (uint32_t)c0 + 16u, v + 16);
+    uint32_t vb[16];
+    tmem_ld16_nowait((half == 0 ? t_db2 : t_dw3) + lane_base, vb);
+    uint32_t vw1[16];
+    tmem_ld16_nowait(t_dw1 + lane_base, vw1);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     if (lane < 16) {
-      const int m = 16 * warp + lane;
-      float4* gw2 = reinterpret_cast<float4*>(G + kOffW2 + m * kH);
+      const int m = 16 * quarter + lane;
+      float4* gw2 = reinterpret_cast<float4*>(G + kOffW2 + m * kH + c0);
 #pragma unroll
-      for (int j = 0; j < kH / 4; ++j) gw2[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-      G[kOffB2 + m] = vb[0];
-      G[kOffW3 + m] = vw3[0];
-      float4* gw1 = reinterpret_cast<float4*>(G + kOffW1 + m * kIn);
-      gw1[0] = make_float4(vw1[0], vw1[1], vw1[2], vw1[3]);
+      for (int j = 0; j < 8; ++j)
+        gw2[j] = make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]), __uint_as_float(v[4 * j + 2]),
+                             __uint_as_float(v[4 * j + 3]));
+      if (half == 0) {
+        G[kOffB2 + m] = __uint_as_float(vb[0]);
+        float4* gw1 = reinterpret_cast<float4*>(G + kOffW1 + m * kIn);
+        gw1[0] = make_float4(__uint_as_float(vw1[0]), __uint_as_float(vw1[1]), __uint_as_float(vw1[2]),
+                             __uint_as_float(vw1[3]));
 #pragma unroll
-      for (int j = 1; j < kIn / 4; ++j) gw1[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int j = 1; j < kIn / 4; ++j) gw1[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+      } else {
+        G[kOffW3 + m] = __uint_as_float(vb[0]);
+      }
     }
   }
   if (tid == 0) {
     float l = 0.f, cs = 0.f, b3 = 0.f;
-    for (int w = 0; w < 4; ++w) {
+    for (int w = 0; w < kTrainThreads / 32; ++w) {
       l += S->wloss[w];
       cs += S->wsum[w];
-      b3 += S->wb3[w];
     }
+    for (int w = 0; w < 4; ++w) b3 += S->wb3[w];
     G[kOffB3] = b3;
     G[kOffC] = -2.f * cs * inv_B;
     G[kNumParams] = l * inv_B;
     G[kNumParams + 1] = 0.f;
   }
+}
+
+// Shared memory of one tile's working set (train_tile): 128 TMEM columns and
+// ~88 KB per training CTA, so two CTAs share an SM.
+size_t __host__ __device__ train_smem_bytes() {
+  return ((sizeof(TrainSmem) + 1023) & ~(size_t)1023) + kW2Bytes + kW1Bytes + kXBytes + 4 * kHBytes + 16 * 128 * 2;
+}
+
+// Sets up what train_tile expects for each of the CTA's `tiles` tiles: the
+// MMA barrier and the zeroed d3 tile; TMEM (128 columns per tile) is
+// allocated once, its base left in the first tile's slot.
+__device__ __forceinline__ void train_setup(unsigned char* smem, int tiles) {
+  const size_t stride = train_smem_bytes();
+  for (int t = 0; t < tiles; ++t) {
+    unsigned char* base = smem + t * stride;
+    unsigned char* sT3 = base + ((sizeof(TrainSmem) + 1023) & ~(size_t)1023) + kW2Bytes + kW1Bytes + kXBytes + 4 * kHBytes;
+    for (int i = threadIdx.x; i < 16 * 128 * 2 / 16; i += blockDim.x)
+      reinterpret_cast<uint4*>(sT3)[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (threadIdx.x == 0) mbar_init(&reinterpret_cast<TrainSmem*>(base)->bar, 1);
+  }
+  if (threadIdx.x < 32) tc::tmem_alloc(&reinterpret_cast<TrainSmem*>(smem)->tmem_slot, 128u * (uint32_t)tiles);
+  tc::fence_smem_to_async();
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) {
+  tc::fence_after_sync();
+}
+
+__device__ __forceinline__ void train_teardown(unsigned char* smem, int tiles) {
+  tc::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(tm, 128);
+    tc::tmem_dealloc(reinterpret_cast<TrainSmem*>(smem)->tmem_slot, 128u * (uint32_t)tiles);
   }
 }
 
-// 128 TMEM columns and ~86 KB of shared memory per training CTA: two CTAs
-// share an SM.
-size_t train_smem_bytes() {
-  return ((sizeof(TrainSmem) + 1023) & ~(size_t)1023) + kW2Bytes + kW1Bytes + kXBytes + 4 * kHBytes + 16 * 128 * 2;
+__global__ void __launch_bounds__(kTrainThreads) mlp_train_step_kernel(tqf_mlp_train_args a) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  allow_dependent_launch();
+  train_setup(smem, 1);
+  uint32_t phase = 0;
+  train_tile(a, smem, reinterpret_cast<TrainSmem*>(smem)->tmem_slot, phase, true, (int)blockIdx.x, (int)threadIdx.x);
+  train_teardown(smem, 1);
 }
 
 // ---- Adam ------------------------------------------------------------------------------
@@ -715,8 +854,17 @@ size_t train_smem_bytes() {
 constexpr int kAdamSlices = 32;
 __global__ void __launch_bounds__(32 * kAdamSlices) mlp_adam_kernel(tqf_mlp_adam_args a) {
   __shared__ float part[kAdamSlices][33];
+  allow_dependent_launch();
   const int lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
   const int i = blockIdx.x * 32 + lane;
+  // the moments and parameters are not written by the training step: read them early
+  float m0 = 0.f, v0 = 0.f, p0 = 0.f;
+  if (slice == 0 && i < kNumParams) {
+    m0 = a.m[i];
+    v0 = a.v[i];
+    p0 = a.params[i];
+  }
+  grid_dependency_wait();  // the gradient partials of the training step
   float g = 0.f;
   if (i <= kNumParams) {
     const float* src = a.grad_partials + i;
@@ -734,10 +882,10 @@ __global__ void __launch_bounds__(32 * kAdamSlices) mlp_adam_kernel(tqf_mlp_adam
     return;
   }
   if (i >= kOffW1 && i < kOffW2 && (i - kOffW1) % kIn >= 4) return;  // padded input columns stay zero
-  float m = a.m[i] = a.beta1 * a.m[i] + (1.f - a.beta1) * g;
-  float v = a.v[i] = a.beta2 * a.v[i] + (1.f - a.beta2) * g * g;
+  float m = a.m[i] = a.beta1 * m0 + (1.f - a.beta1) * g;
+  float v = a.v[i] = a.beta2 * v0 + (1.f - a.beta2) * g * g;
   const float mh = m / a.bias1, vh = v / a.bias2;
-  const float p = a.params[i] - a.lr * mh / (sqrtf(vh) + a.eps);
+  const float p = p0 - a.lr * mh / (sqrtf(vh) + a.eps);
   a.params[i] = p;
   uint16_t* w1b = static_cast<uint16_t*>(a.w1_bf16);
   uint16_t* w2b = static_cast<uint16_t*>(a.w2_bf16);
@@ -850,6 +998,9 @@ extern "C" int tqf_mlp_train_step(const tqf_mlp_train_args* a, void* stream) {
               "tqf_mlp_train_step: batch_paths must be a positive multiple of paths_per_cta");
   TQF_REQUIRE(a->feats && a->dS && a->Y && a->params && a->w1_bf16 && a->w2_bf16 && a->grad_partials,
               "tqf_mlp_train_step: null pointer");
+  TQF_REQUIRE(a->path_begin >= 0 && a->path_begin + a->batch_paths <= a->pilot_paths,
+              "tqf_mlp_train_step: minibatch [%lld, %lld) outside the %lld pilot paths", (long long)a->path_begin,
+              (long long)(a->path_begin + a->batch_paths), (long long)a->pilot_paths);
   TQF_REQUIRE((reinterpret_cast<uintptr_t>(a->feats) & 15u) == 0 && (reinterpret_cast<uintptr_t>(a->w2_bf16) & 15u) == 0 &&
                   (reinterpret_cast<uintptr_t>(a->grad_partials) & 15u) == 0 &&
                   (reinterpret_cast<uintptr_t>(a->w1_bf16) & 7u) == 0,
@@ -857,7 +1008,18 @@ extern "C" int tqf_mlp_train_step(const tqf_mlp_train_args* a, void* stream) {
   const int grid = a->batch_paths / a->paths_per_cta;
   const size_t smem = train_smem_bytes();
   set_smem_config(mlp_train_step_kernel, smem);
-  mlp_train_step_kernel<<<grid, kTrainThreads, smem, static_cast<cudaStream_t>(stream)>>>(*a);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kTrainThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = static_cast<cudaStream_t>(stream);
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, mlp_train_step_kernel, *a);
+  if (e != cudaSuccess) return check_cuda(e, "mlp_train_step_kernel");
   return check_launch("mlp_train_step_kernel");
 }
 
@@ -866,7 +1028,17 @@ extern "C" int tqf_mlp_adam(const tqf_mlp_adam_args* a, void* stream) {
   TQF_REQUIRE(a && a->params && a->m && a->v && a->grad_partials && a->w1_bf16 && a->w2_bf16,
               "tqf_mlp_adam: null pointer");
   TQF_REQUIRE(a->num_partials >= 1, "tqf_mlp_adam: num_partials must be >= 1");
-  const int blocks = (kNumParams + 1 + 31) / 32;
-  mlp_adam_kernel<<<blocks, 32 * kAdamSlices, 0, static_cast<cudaStream_t>(stream)>>>(*a);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.gridDim = dim3((kNumParams + 1 + 31) / 32);
+  cfg.blockDim = dim3(32 * kAdamSlices);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = static_cast<cudaStream_t>(stream);
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, mlp_adam_kernel, *a);
+  if (e != cudaSuccess) return check_cuda(e, "mlp_adam_kernel");
   return check_launch("mlp_adam_kernel");
 }

@@ -289,6 +289,24 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
+// Bounded wait that lets the hardware suspend the thread until the phase
+// completes (or ~64 us pass) on each try instead of polling: waiting warps
+// take no issue slots.  Gives up after `limit` tries (about a second).
+__device__ __forceinline__ bool mbar_wait_suspend(uint64_t* bar, uint32_t parity, int limit = 1 << 14) {
+  for (int it = 0; it < limit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(65536u)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
 // Stages `nbytes` (multiple of 16) from global `src` into shared `dst` with
 // one elected thread issuing bulk copies of <= 64 KiB; every thread of the
 // CTA returns true once the data is visible, or false (uniformly) after a

@@ -412,6 +412,7 @@ class MlpTrainArgs(ctypes.Structure):
         ("paths_per_cta", c_i32),
         ("pad0", c_i32),
         ("path_begin", c_i64),
+        ("pilot_paths", c_i64),
         ("feats", c_vp),
         ("dS", c_vp),
         ("Y", c_vp),

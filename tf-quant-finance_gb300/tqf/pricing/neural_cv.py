@@ -60,6 +60,25 @@ class AsianEstimate:
     se_control: float = 0.0
 
 
+def stage_marks(date_steps) -> np.ndarray:
+    """Steps at which the fused inference advances its network pipeline.
+
+    The evaluation for interval k starts after step date_steps[k-1] (before
+    step 0 for k = 0) and must be complete after step date_steps[k]; its two
+    middle stages run about a third and two thirds of the way between, at
+    steps strictly inside the interval (none when the interval is too short:
+    the kernel then runs them at the date)."""
+    marks = []
+    prev = -1
+    for s in np.asarray(date_steps, dtype=np.int64).tolist():
+        gap = s - prev
+        a = prev + max(1, int(round(gap / 3.0)))
+        b = prev + max(a - prev + 1, int(round(2.0 * gap / 3.0)))
+        marks += [m for m in (a, b) if prev < m < s]
+        prev = s
+    return np.asarray(marks, dtype=np.int64)
+
+
 def _bf16_bits(x: torch.Tensor) -> torch.Tensor:
     return x.to(torch.bfloat16).view(torch.int16)
 
@@ -69,7 +88,8 @@ class HestonAsianCV:
     martingale control variate."""
 
     def __init__(self, *, spot=100.0, variance=0.04, mean_reversion=2.0, theta=0.04, volvol=0.3, rho=-0.7,
-                 rate=0.02, expiry=1.0, strike=100.0, num_dates=52, num_time_steps=252, init_seed=0):
+                 rate=0.02, expiry=1.0, strike=100.0, num_dates=52, num_time_steps=252, init_seed=0,
+                 pipeline_stages=True):
         self.device = _lib.require_cuda()
         d = self.device
         self.spot, self.v0, self.kappa, self.theta, self.xi, self.rho = spot, variance, mean_reversion, theta, volvol, rho
@@ -83,6 +103,8 @@ class HestonAsianCV:
             raise ValueError("monitoring dates must map to distinct grid points after t = 0")
         slots = np.full(self.num_steps, -1, np.int32)
         slots[ti - 1] = np.arange(self.num_dates)  # state after step i is at grid point i + 1
+        if pipeline_stages:
+            slots[stage_marks(ti - 1)] = -2
         dt = (grid[1:] - grid[:-1]).astype(f32)
         coef = HestonFullTruncation(rate, mean_reversion, theta, volvol, rho)
         rows = heston_model.full_truncation_table(coef, grid, dt, np.sqrt(dt).astype(f32), slots, self.num_steps)
@@ -168,11 +190,15 @@ class HestonAsianCV:
     def pilot(self, num_paths=1 << 20, seed=(977, 5)):
         d = self.device
         D = self.num_dates
-        self.feats = torch.empty((num_paths, D, 4), dtype=torch.float32, device=d)
-        self.dS = torch.empty((num_paths, D), dtype=torch.float32, device=d)
+        # date-major storage (coalesced stores in the path kernel); the
+        # attributes are [N, D, ...] views of it
+        self._feats_dm = torch.empty((D, num_paths, 4), dtype=torch.float32, device=d)
+        self._dS_dm = torch.empty((D, num_paths), dtype=torch.float32, device=d)
+        self.feats = self._feats_dm.permute(1, 0, 2)
+        self.dS = self._dS_dm.t()
         self.Y = torch.empty((num_paths,), dtype=torch.float32, device=d)
         a = self._args(1, num_paths, seed, 0)
-        a.pilot_feats, a.pilot_dS, a.pilot_Y = self.feats.data_ptr(), self.dS.data_ptr(), self.Y.data_ptr()
+        a.pilot_feats, a.pilot_dS, a.pilot_Y = self._feats_dm.data_ptr(), self._dS_dm.data_ptr(), self.Y.data_ptr()
         s = torch.cuda.current_stream()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s)
@@ -189,7 +215,8 @@ class HestonAsianCV:
         t.batch_paths = int(batch_paths)
         t.paths_per_cta = self.train_paths_per_cta
         t.path_begin = int(path_begin)
-        t.feats, t.dS, t.Y = self.feats.data_ptr(), self.dS.data_ptr(), self.Y.data_ptr()
+        t.pilot_paths = self.num_pilot
+        t.feats, t.dS, t.Y = self._feats_dm.data_ptr(), self._dS_dm.data_ptr(), self.Y.data_ptr()
         t.params = self.params.data_ptr()
         t.w1_bf16, t.w2_bf16 = self.w1_bf16.data_ptr(), self.w2_bf16.data_ptr()
         for i in range(3):
@@ -209,13 +236,15 @@ class HestonAsianCV:
         s = partials.sum(0)
         return s[:NUM_PARAMS], float(s[NUM_PARAMS])
 
-    def train(self, steps=2000, batch_paths=1024, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, graph=True,
+    def train(self, steps=2000, batch_paths=512, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, graph=True,
               init_intercept=True):
         """Adam on minibatches of pilot paths taken in order (wrapping).  The
         2 x steps kernel launches are captured once into a CUDA graph and
         replayed (graph=True) so that host launch overhead stays out of the
-        loop; ``train_seconds`` is the GPU time of the replay.  Before the
-        first step the loss offset c starts at the pilot mean of Y
+        loop; each kernel is a programmatic dependent launch, so the next one
+        starts its independent prologue while the previous one finishes.
+        ``train_seconds`` is the GPU time of the replay.  Before the first
+        step the loss offset c starts at the pilot mean of Y
         (init_intercept), so that the residuals start centred."""
         if batch_paths % self.train_paths_per_cta:
             raise ValueError(f"batch_paths must be a multiple of {self.train_paths_per_cta}")
@@ -325,4 +354,4 @@ def time_to_ci(estimate: AsianEstimate, rel_halfwidth=1e-4, z=1.96) -> dict:
     return {"paths": n_req, "seconds": estimate.seconds * n_req / estimate.num_paths}
 
 
-__all__ = ["HestonAsianCV", "AsianEstimate", "time_to_ci"]
+__all__ = ["HestonAsianCV", "AsianEstimate", "time_to_ci", "stage_marks"]
