@@ -185,19 +185,14 @@ struct EvalPipe {
 };
 
 // Makes this warpgroup's shared-memory tile writes and TMEM reads visible to
-// the MMAs that its first warp (thread 0 issues) starts next: warps 1-3
-// arrive on the warpgroup's named barrier and go on; warp 0 waits for all.
+// the MMAs that its thread 0 issues next.  (A variant in which warps 1-3
+// only arrive on the named barrier measured ~1% slower.)
 __device__ __forceinline__ void wg_publish(int wg, int tid) {
+  (void)tid;
   tc::fence_smem_to_async();
   tc::fence_before_sync();
-  if (tid < 32) {
-    wg_sync(wg);
-    tc::fence_after_sync();
-  } else if (wg == 0) {
-    asm volatile("bar.arrive 1, 128;" ::: "memory");
-  } else {
-    asm volatile("bar.arrive 2, 128;" ::: "memory");
-  }
+  wg_sync(wg);
+  tc::fence_after_sync();
 }
 
 // 16 FP32 TMEM columns of this thread's lane, without the wait.
@@ -210,19 +205,19 @@ __device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t* r) {
 }
 
 // SiLU of this row's 64 TMEM accumulators (packed BF16) into row r of sH,
-// 32 columns per TMEM round trip.
+// 16 columns per TMEM round trip (fewer live registers than 32 at a time,
+// which measured faster at this kernel's 64-register budget).
 __device__ __forceinline__ void silu_row_from_tmem(uint32_t taddr, unsigned char* sH, int r) {
 #pragma unroll
-  for (int c = 0; c < kH; c += 32) {
-    uint32_t u[32];
+  for (int c = 0; c < kH; c += 16) {
+    uint32_t u[16];
     tmem_ld16_nowait(taddr + (uint32_t)c, u);
-    tmem_ld16_nowait(taddr + (uint32_t)c + 16u, u + 16);
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    float acc[32];
+    float acc[16];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) acc[j] = __uint_as_float(u[j]);
+    for (int j = 0; j < 16; ++j) acc[j] = __uint_as_float(u[j]);
 #pragma unroll
-    for (int h = 0; h < 32; h += 8)
+    for (int h = 0; h < 16; h += 8)
       *reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, c + h, kHLbo, kHSbo)) =
           make_uint4(silu_bf16x2(acc[h], acc[h + 1]), silu_bf16x2(acc[h + 2], acc[h + 3]),
                      silu_bf16x2(acc[h + 4], acc[h + 5]), silu_bf16x2(acc[h + 6], acc[h + 7]));
