@@ -133,6 +133,69 @@ __device__ __forceinline__ void box_muller_f64(uint4 r, double& z0, double& z1) 
   z1 = rad * s;
 }
 
+// ---- packed FP32 pairs ------------------------------------------------------
+// sm_100-family f32x2 arithmetic: one issued instruction does the two lanes'
+// work, each lane rounded exactly as the scalar .rn operation would be.
+__device__ __forceinline__ uint64_t f2_bits(float2 a) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 f2_from_bits(uint64_t r) {
+  float2 v;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+  return v;
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_from_bits(d);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+  uint64_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_from_bits(d);
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)), "l"(f2_bits(c)));
+  return f2_from_bits(d);
+}
+__device__ __forceinline__ float lg2_ftz(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ void sincos_ftz(float x, float& s, float& c) {
+  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"(x));
+  asm("cos.approx.ftz.f32 %0, %1;" : "=f"(c) : "f"(x));
+}
+
+// The four normals of one Philox block as two pairs, even = (z0, z2) and
+// odd = (z1, z3), with (z0, z1) from words (x, y) and (z2, z3) from (z, w):
+// the arithmetic of box_muller_f32 run on both halves at once in f32x2
+// instructions.  Every input of the flush-to-zero SFU forms is a normal
+// number (u1 >= 2^-32; the angle is 0 or at least 2 pi 2^-23 in magnitude),
+// so the results equal box_muller_f32's bit for bit.
+__device__ __forceinline__ void box_muller_pair_f32(uint4 r, float2& even, float2& odd) {
+  const float2 hi = make_float2(__uint_as_float(0x3f800000u | (r.x >> 9)), __uint_as_float(0x3f800000u | (r.z >> 9)));
+  const float2 lo = make_float2(__uint_as_float(0x3f800000u | (r.x << 23 >> 9)),
+                                __uint_as_float(0x3f800000u | (r.z << 23 >> 9)));
+  const float2 two_minus_hi = fma2(hi, make_float2(-1.f, -1.f), make_float2(2.f, 2.f));  // 2 - hi, exact product
+  const float2 u1 = fma2(add2(lo, make_float2(-1.f, -1.f)), make_float2(-1.1920928955078125e-07f, -1.1920928955078125e-07f),
+                         two_minus_hi);
+  const float2 m = mul2(make_float2(-1.3862943611198906f, -1.3862943611198906f), make_float2(lg2_ftz(u1.x), lg2_ftz(u1.y)));
+  const float2 rad = make_float2(sqrt_approx(m.x), sqrt_approx(m.y));
+  const float2 u2 = add2(make_float2(__uint_as_float(0x3f800000u | (r.y >> 9)), __uint_as_float(0x3f800000u | (r.w >> 9))),
+                         make_float2(-1.f, -1.f));
+  const float2 ang = mul2(add2(u2, make_float2(-0.5f, -0.5f)), make_float2(6.283185307179586f, 6.283185307179586f));
+  float2 s, c;
+  sincos_ftz(ang.x, s.x, c.x);
+  sincos_ftz(ang.y, s.y, c.y);
+  even = mul2(rad, c);
+  odd = mul2(rad, s);
+}
+
 // Four float normals of block b for path n: draw dims 4b..4b+3.
 __device__ __forceinline__ void philox_normals4_f32(int64_t block, int64_t path,
                                                     uint32_t k0, uint32_t k1,
