@@ -3,14 +3,12 @@
 // with full-truncation Heston coefficients, tff/models/euler_sampling.py:513-537).
 //
 // Network g(t, log S, v): 3 -> 64 -> 64 -> 1, SiLU, BF16 weights and
-// activations, FP32 accumulation.  Layer 2 (64 x 64, the GEMM-shaped part)
-// runs on the tcgen05 tensor cores: a warpgroup's 128 rows (one per thread)
-// form an M = 128 tile with the accumulator in TMEM.  Layer 1 (K = 3) is 192
-// FMAs per row on the CUDA cores with the same BF16-rounded operands the
-// tensor cores would use; W1 column 3 holds its bias (input feature 1).
-// SiLU runs in packed BF16 (one SFU tanh per pair); layer 3 is a 64-term
-// FP32 dot product.  The backward GEMMs (d1 = d2 W2, dW2 = d2^T H1,
-// db2 = d2^T 1, dW1 = d1^T X) are tcgen05 MMAs.
+// activations, FP32 accumulation.  Every layer runs on the tcgen05 tensor
+// cores: a warpgroup's 128 rows (one per thread) form an M = 128 tile with
+// the accumulator in TMEM.  Layer 1 is K = 16 (three features, a 1 for the
+// bias in W1 column 3, zero padding); layer 3 has N = 16 (w3 split into BF16
+// high and low rows).  SiLU runs in packed BF16 (one SFU tanh per pair).
+// The backward GEMMs (Q2 W2, dW2, db2, dw3, dW1) are tcgen05 MMAs as well.
 //
 // heston_asian_kernel<MODE>: full-truncation Euler paths (Philox in-kernel),
 //   num_dates monitoring dates marked in the step table's slot column.
@@ -41,6 +39,9 @@ constexpr int kIn = 16;           // padded input width (K of layer 1)
 constexpr int kMaxDates = 64;
 constexpr int kPathThreads = 256;  // two warpgroups
 constexpr int kCvCtasPerSm = 4;    // fused-inference CTAs per SM (4 x 128 TMEM columns = 512)
+// Plain and pilot path kernels: register bound for 5 CTAs per SM (48
+// registers; 4 and 6 measured within 1% of it).
+constexpr int kPlainCtasPerSm = 5;
 constexpr int kTrainThreads = 256;  // two threads per tile row
 // parameter vector layout (FP32 master copy)
 constexpr int kOffW1 = 0;
@@ -323,8 +324,9 @@ struct AsianSmem {
 // reads the step table from global memory (L1-resident) so that its shared
 // memory stays under a quarter of the SM's.
 template <int MODE>
-__global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : 1)
-    heston_asian_kernel(tqf_heston_asian_args a, const __grid_constant__ MlpConst wc) {
+__global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : kPlainCtasPerSm)
+    heston_asian_kernel(tqf_heston_asian_args a, const __grid_constant__ MlpConst wc,
+                        const float4* __restrict__ pair_table) {
   extern __shared__ __align__(1024) unsigned char smem[];
   AsianSmem* S = reinterpret_cast<AsianSmem*>(smem);
   unsigned char* tiles = smem + ((sizeof(AsianSmem) + 1023) & ~(size_t)1023);
@@ -333,7 +335,7 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : 1)
   unsigned char* sB2 = sW1 + kW1Bytes;
   unsigned char* sW3 = sB2 + kW1Bytes;
   unsigned char* sWg = sW3 + kW3Bytes;  // per warpgroup: X [128 x 16], H [128 x 64]
-  float* table = reinterpret_cast<float*>(tiles);  // modes 0, 1: [steps][8]
+  float* table = reinterpret_cast<float*>(tiles);  // modes 0, 1: two-step blocks (ft_pair_block)
   const int tid = threadIdx.x & 127, wg = threadIdx.x >> 7;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int D = a.num_dates;
@@ -343,7 +345,8 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : 1)
   }
   for (int i = threadIdx.x; i < (kPathThreads / 32) * 5; i += blockDim.x) (&S->acc[0][0])[i] = 0.0;
   if (MODE != 2)
-    for (int i = threadIdx.x; i < a.num_steps * 8; i += blockDim.x) table[i] = a.step_table[i];
+    for (int p = threadIdx.x; p < (a.num_steps + 1) / 2; p += blockDim.x)
+      ft_pair_block(a.step_table, a.num_steps, p, reinterpret_cast<float4*>(table) + 4 * p);
   EvalPipe P;
   if (MODE == 2) {
     const uint4* w2 = static_cast<const uint4*>(a.mlp.w2_bf16);
@@ -370,8 +373,8 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : 1)
     P.phase = 0;
     P.stage = 0;
   }
-  const float4* gtab = reinterpret_cast<const float4*>(a.step_table);
-  const float4* stab = reinterpret_cast<const float4*>(table);
+  // two-step blocks: mode 2 from global memory (L1-resident), modes 0, 1 from shared memory
+  const float4* tp = MODE == 2 ? pair_table : reinterpret_cast<const float4*>(table);
   const float K = (float)a.strike, discT = (float)a.discount_T, x0 = (float)a.x0, v0 = (float)a.v0;
   const float S0 = __expf(x0);
   const float inv_D = 1.f / (float)D;
@@ -385,27 +388,9 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : 1)
     float x = x0, v = v0, avg = 0.f, cv = 0.f, prev = S0;
     if (MODE == 2) eval_issue_l1(wg, tid, wc, P, sW1, 0.f, x0, v0);
     if (MODE == 1 && valid) reinterpret_cast<float4*>(a.pilot_feats)[path] = make_float4(0.f, x0, v0, 0.f);
-    float zbuf[4];
-    for (int i = 0; i < a.num_steps; ++i) {
-      if ((i & 1) == 0) {
-        const uint4 r = philox4x32_10(make_uint4((uint32_t)(i >> 1), plo, phi, 0u), a.draws.key0, a.draws.key1);
-        box_muller_f32(r.x, r.y, zbuf[0], zbuf[1]);
-        box_muller_f32(r.z, r.w, zbuf[2], zbuf[3]);
-      }
-      const float za = (i & 1) ? zbuf[2] : zbuf[0];
-      const float zb = (i & 1) ? zbuf[3] : zbuf[1];
-      const float4 c0 = MODE == 2 ? __ldg(gtab + 2 * i) : stab[2 * i];
-      const float4 c1 = MODE == 2 ? __ldg(gtab + 2 * i + 1) : stab[2 * i + 1];
-      {
-        const float vp = fmaxf(v, 0.f);
-        const float sq = sqrt_approx(vp);
-        const float dw0 = za * c0.y, dw1 = zb * c0.y;
-        const float xn = x + fmaf(-c0.x, vp, c0.z) + sq * dw0;
-        const float vn = v + fmaf(-c0.w, vp, c1.x) + sq * fmaf(c1.z, dw1, c1.y * dw0);
-        x = xn;
-        v = vn;
-      }
-      const int k = (int)c1.w;  // date index, -1, or -2 (a pipeline stage; uniform across the CTA)
+    // after each step: k = its slot (date index, -1, or -2 for a pipeline
+    // stage; uniform across the CTA)
+    auto after_step = [&](int k) {
       if (MODE == 2 && k == -2) {
         if (P.stage == 1) eval_stage1(wg, tid, P, sW2, sB2, a.dev_status);
         else if (P.stage == 2) eval_stage2(wg, tid, P, sW3, a.dev_status);
@@ -425,6 +410,49 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : 1)
         }
         prev = S->date_disc[k] * Sk;
         if (MODE == 2 && k + 1 < D) eval_issue_l1(wg, tid, wc, P, sW1, S->date_t[k], x, v);
+      }
+    };
+    // steps 2 pb and 2 pb + 1 from Philox block pb, in f32x2 pairs
+    auto two_steps = [&](int pb, bool both) {
+      const uint4 r = philox4x32_10(make_uint4((uint32_t)pb, plo, phi, 0u), a.draws.key0, a.draws.key1);
+      float2 ze, zo;
+      box_muller_pair_f32(r, ze, zo);
+      const float4 qa = MODE == 2 ? __ldg(tp + 4 * pb) : tp[4 * pb];
+      const float4 qs = MODE == 2 ? __ldg(tp + 4 * pb + 2) : tp[4 * pb + 2];
+      const float4 qx = MODE == 2 ? __ldg(tp + 4 * pb + 3) : tp[4 * pb + 3];
+      float2 dw0, e;
+      ft_pair_increments(ze, zo, qs, qx, dw0, e);
+      ft_half_step(qa, dw0.x, e.x, x, v);
+      after_step((int)qx.z);
+      if (both) {
+        const float4 qb = MODE == 2 ? __ldg(tp + 4 * pb + 1) : tp[4 * pb + 1];
+        ft_half_step(qb, dw0.y, e.y, x, v);
+        after_step((int)qx.w);
+      }
+    };
+    if constexpr (MODE != 2) {
+      const int full = a.num_steps >> 1;
+#pragma unroll 1
+      for (int pb = 0; pb < full; ++pb) two_steps(pb, true);
+      if (a.num_steps & 1) two_steps(full, false);
+    } else {
+      // one step per iteration (a single copy of the network stages in the
+      // loop body), the block's normals and increments taken at even steps
+      float2 dw0 = make_float2(0.f, 0.f), e = make_float2(0.f, 0.f);
+      float2 slots = make_float2(-1.f, -1.f);
+      for (int i = 0; i < a.num_steps; ++i) {
+        const int pb = i >> 1;
+        const bool odd = (i & 1) != 0;
+        if (!odd) {
+          const uint4 r = philox4x32_10(make_uint4((uint32_t)pb, plo, phi, 0u), a.draws.key0, a.draws.key1);
+          float2 ze, zo;
+          box_muller_pair_f32(r, ze, zo);
+          const float4 qx = __ldg(tp + 4 * pb + 3);
+          ft_pair_increments(ze, zo, __ldg(tp + 4 * pb + 2), qx, dw0, e);
+          slots = make_float2(qx.z, qx.w);
+        }
+        ft_half_step(__ldg(tp + 4 * pb + (odd ? 1 : 0)), odd ? dw0.y : dw0.x, odd ? e.y : e.x, x, v);
+        after_step((int)(odd ? slots.y : slots.x));
       }
     }
     const float Y = discT * fmaxf(avg * inv_D - K, 0.f);
@@ -464,8 +492,18 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : 1)
 size_t asian_smem_bytes(int mode, int steps) {
   const size_t head = (sizeof(AsianSmem) + 1023) & ~(size_t)1023;
   if (mode == 2) return head + kW2Bytes + 2 * kW1Bytes + kW3Bytes + 2 * (kXBytes + kHBytes);
-  return head + (size_t)steps * 8 * sizeof(float);
+  return head + (size_t)((steps + 1) & ~1) * 8 * sizeof(float);
 }
+
+// Mode 2 reads the step table as two-step blocks from global memory: this
+// kernel writes them into the caller's workspace, after the partial sums.
+__global__ void ft_pair_table_kernel(const float* __restrict__ rows, int steps, float4* __restrict__ out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < (steps + 1) / 2) ft_pair_block(rows, steps, p, out + 4 * p);
+}
+
+size_t asian_partials_bytes(int grid) { return ((size_t)grid * 5 * sizeof(double) + 15) & ~(size_t)15; }
+size_t asian_pair_table_bytes(int steps) { return (size_t)((steps + 1) / 2) * 16 * sizeof(float); }
 
 template <int MODE>
 int asian_grid(int64_t n, size_t smem) {
@@ -908,7 +946,7 @@ static float bf16_round_host(float x) {
 extern "C" size_t tqf_heston_asian_workspace_bytes(int32_t mode, int64_t num_paths, int32_t num_steps) {
   const size_t smem = asian_smem_bytes(mode, num_steps);
   int grid = mode == 2 ? asian_grid<2>(num_paths, smem) : asian_grid<0>(num_paths, smem);
-  return (size_t)grid * 5 * sizeof(double);
+  return asian_partials_bytes(grid) + (mode == 2 ? asian_pair_table_bytes(num_steps) : 0);
 }
 
 extern "C" int tqf_heston_asian(const tqf_heston_asian_args* a, void* stream) {
@@ -936,9 +974,10 @@ extern "C" int tqf_heston_asian(const tqf_heston_asian_args* a, void* stream) {
   else if (a->mode == 1) grid = asian_grid<1>(a->num_paths, smem);
   else grid = asian_grid<2>(a->num_paths, smem);
   if (a->mode != 1) {
-    const size_t need = (size_t)grid * 5 * sizeof(double);
+    const size_t need = asian_partials_bytes(grid) + (a->mode == 2 ? asian_pair_table_bytes(a->num_steps) : 0);
     TQF_REQUIRE(a->out && a->workspace && a->workspace_bytes >= need, "tqf_heston_asian: workspace %zu < %zu",
                 a->workspace_bytes, need);
+    TQF_REQUIRE((reinterpret_cast<uintptr_t>(a->workspace) & 15u) == 0, "tqf_heston_asian: workspace must be 16-byte aligned");
   }
   MlpConst wc;
   memset(&wc, 0, sizeof(wc));
@@ -957,9 +996,18 @@ extern "C" int tqf_heston_asian(const tqf_heston_asian_args* a, void* stream) {
       wc.fshift[j] = a->mlp.feat_shift[j];
     }
   }
-  if (a->mode == 0) heston_asian_kernel<0><<<grid, kPathThreads, smem, s>>>(*a, wc);
-  else if (a->mode == 1) heston_asian_kernel<1><<<grid, kPathThreads, smem, s>>>(*a, wc);
-  else heston_asian_kernel<2><<<grid, kPathThreads, smem, s>>>(*a, wc);
+  if (a->mode == 0) {
+    heston_asian_kernel<0><<<grid, kPathThreads, smem, s>>>(*a, wc, nullptr);
+  } else if (a->mode == 1) {
+    heston_asian_kernel<1><<<grid, kPathThreads, smem, s>>>(*a, wc, nullptr);
+  } else {
+    float4* pairs = reinterpret_cast<float4*>(static_cast<unsigned char*>(a->workspace) + asian_partials_bytes(grid));
+    const int np = (a->num_steps + 1) / 2;
+    ft_pair_table_kernel<<<(np + 127) / 128, 128, 0, s>>>(a->step_table, a->num_steps, pairs);
+    int rc = check_launch("ft_pair_table_kernel");
+    if (rc) return rc;
+    heston_asian_kernel<2><<<grid, kPathThreads, smem, s>>>(*a, wc, pairs);
+  }
   int rc = check_launch("heston_asian_kernel");
   if (rc || a->mode == 1) return rc;
   return reduce_partials(static_cast<const double*>(a->workspace), grid, 5, a->out, s);

@@ -92,39 +92,20 @@ __device__ __forceinline__ void ft_step(const T* __restrict__ row, T z0, T z1, T
   ft_step<T>(load_ft_row<T>(row), z0, z1, x, v);
 }
 
-// Rewrites a staged float FT table [steps][8] in place as two-step blocks:
-// for steps a = 2p, b = 2p + 1 the 16 floats
-//   (-hdt_a, -kdt_a, rdt_a, kthdt_a), (-hdt_b, -kdt_b, rdt_b, kthdt_b),
-//   (sdt_a, sdt_b, xirho_a, xirho_b), (xisq_a, xisq_b, slot_a, slot_b),
-// so that the paired loop reads its constants as f32x2 operands with four
-// 16-byte loads per two steps.  An odd last step pairs with a zero step.
-// Each thread rewrites whole blocks of its own; the caller synchronises.
+// Rewrites a staged float FT table [steps][8] in place as two-step blocks
+// (ft_pair_block).  Each thread rewrites whole blocks of its own; the caller
+// synchronises.
 __device__ __forceinline__ void pair_ft_table(float* tb, int steps) {
   const int pairs = (steps + 1) >> 1;
   for (int p = threadIdx.x; p < pairs; p += blockDim.x) {
+    float4 q[4];
+    ft_pair_block(tb, steps, p, q);
     float4* blk = reinterpret_cast<float4*>(tb + 16 * p);
-    const float4 a0 = blk[0], a1 = blk[1];
-    float4 b0 = make_float4(0.f, 0.f, 0.f, 0.f), b1 = make_float4(0.f, 0.f, 0.f, -1.f);
-    if (2 * p + 1 < steps) {
-      b0 = blk[2];
-      b1 = blk[3];
-    }
-    blk[0] = make_float4(-a0.x, -a0.w, a0.z, a1.x);
-    blk[1] = make_float4(-b0.x, -b0.w, b0.z, b1.x);
-    blk[2] = make_float4(a0.y, b0.y, a1.y, b1.y);
-    blk[3] = make_float4(a1.z, b1.z, a1.w, b1.w);
+    blk[0] = q[0];
+    blk[1] = q[1];
+    blk[2] = q[2];
+    blk[3] = q[3];
   }
-}
-
-// One full-truncation step from a pair block's half q = (-hdt, -kdt, rdt,
-// kthdt) and the step's dw0 and e = xi rho dw0 + xi sqrt(1 - rho^2) dw1:
-// ft_step's arithmetic with the two drift sums in one f32x2 add.
-__device__ __forceinline__ void ft_half_step(const float4 q, float dw0, float e, float& x, float& v) {
-  const float vp = fmaxf(v, 0.f);
-  const float sq = sqrt_approx(vp);
-  const float2 u = add2(make_float2(x, v), make_float2(fmaf(q.x, vp, q.z), fmaf(q.y, vp, q.w)));
-  x = fmaf(sq, dw0, u.x);
-  v = fmaf(sq, e, u.y);
 }
 
 template <typename T>
@@ -274,10 +255,9 @@ __global__ void __launch_bounds__(kBlock)
                 ze = mul2(ze, make_float2(sign, sign));
                 zo = mul2(zo, make_float2(sign, sign));
               }
-              const float4 qa = tp[4 * pb], qs = tp[4 * pb + 2], qx = tp[4 * pb + 3];
-              const float2 sdt = make_float2(qs.x, qs.y);
-              const float2 dw0 = mul2(ze, sdt), dw1 = mul2(zo, sdt);
-              const float2 e = fma2(make_float2(qx.x, qx.y), dw1, mul2(make_float2(qs.z, qs.w), dw0));
+              const float4 qa = tp[4 * pb], qx = tp[4 * pb + 3];
+              float2 dw0, e;
+              ft_pair_increments(ze, zo, tp[4 * pb + 2], qx, dw0, e);
               ft_half_step(qa, dw0.x, e.x, x, v);
               if (STORE) {
                 const int slot = (int)qx.z;

@@ -196,6 +196,51 @@ __device__ __forceinline__ void box_muller_pair_f32(uint4 r, float2& even, float
   odd = mul2(rad, s);
 }
 
+// ---- full-truncation Heston steps in pairs ---------------------------------
+// Block p of the two-step layout of a float FT table [steps][8] with rows
+// (dt/2, sqrt dt, r dt, kappa dt, kappa theta dt, xi rho, xi sqrt(1-rho^2),
+// slot): for steps a = 2p, b = 2p + 1 the 16 floats
+//   (-hdt_a, -kdt_a, rdt_a, kthdt_a), (-hdt_b, -kdt_b, rdt_b, kthdt_b),
+//   (sdt_a, sdt_b, xirho_a, xirho_b), (xisq_a, xisq_b, slot_a, slot_b),
+// so that a loop taking both steps of a Philox block reads its constants as
+// f32x2 operands with four 16-byte loads.  An odd last step pairs with a
+// zero step whose slot is -1.  All reads happen before the caller writes.
+__device__ __forceinline__ void ft_pair_block(const float* rows, int steps, int p, float4 q[4]) {
+  const float4* r = reinterpret_cast<const float4*>(rows + 16 * p);
+  const float4 a0 = r[0], a1 = r[1];
+  float4 b0 = make_float4(0.f, 0.f, 0.f, 0.f), b1 = make_float4(0.f, 0.f, 0.f, -1.f);
+  if (2 * p + 1 < steps) {
+    b0 = r[2];
+    b1 = r[3];
+  }
+  q[0] = make_float4(-a0.x, -a0.w, a0.z, a1.x);
+  q[1] = make_float4(-b0.x, -b0.w, b0.z, b1.x);
+  q[2] = make_float4(a0.y, b0.y, a1.y, b1.y);
+  q[3] = make_float4(a1.z, b1.z, a1.w, b1.w);
+}
+
+// Increments of both steps of a block: dw0 = z_even sqrt dt, dw1 = z_odd
+// sqrt dt and e = xi rho dw0 + xi sqrt(1 - rho^2) dw1, each as a pair
+// (step a, step b); qs, qx are the block's third and fourth float4.
+__device__ __forceinline__ void ft_pair_increments(float2 ze, float2 zo, float4 qs, float4 qx, float2& dw0,
+                                                   float2& e) {
+  const float2 sdt = make_float2(qs.x, qs.y);
+  dw0 = mul2(ze, sdt);
+  const float2 dw1 = mul2(zo, sdt);
+  e = fma2(make_float2(qx.x, qx.y), dw1, mul2(make_float2(qs.z, qs.w), dw0));
+}
+
+// One full-truncation step from a block's half q = (-hdt, -kdt, rdt, kthdt),
+// the step's dw0 and e: the scalar step's arithmetic, with the two drift
+// sums in one f32x2 add.
+__device__ __forceinline__ void ft_half_step(const float4 q, float dw0, float e, float& x, float& v) {
+  const float vp = fmaxf(v, 0.f);
+  const float sq = sqrt_approx(vp);
+  const float2 u = add2(make_float2(x, v), make_float2(fmaf(q.x, vp, q.z), fmaf(q.y, vp, q.w)));
+  x = fmaf(sq, dw0, u.x);
+  v = fmaf(sq, e, u.y);
+}
+
 // Four float normals of block b for path n: draw dims 4b..4b+3.
 __device__ __forceinline__ void philox_normals4_f32(int64_t block, int64_t path,
                                                     uint32_t k0, uint32_t k1,
