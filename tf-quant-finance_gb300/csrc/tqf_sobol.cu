@@ -70,19 +70,31 @@ __device__ __forceinline__ uint32_t sobol_direct(const uint32_t* __restrict__ v_
 }
 
 // ---- [n, dim] row-major output (sobol.sample) ---------------------------------
-// Block = DX dim-threads x PT point-threads; each thread owns VEC consecutive
-// dims and P points with stride PT (= 2^m).
+// Block = DX dim-threads x PT point-threads (PT = 2^mt); each thread owns VEC
+// consecutive dims.  The grid's CTAs interleave row by row: CTA b takes rows
+// PT (b + gridDim.x s) .. + PT - 1, so a thread's rows are 2^m = PT gridDim.x
+// apart (gridDim.x a power of two) and at any time the whole grid writes one
+// contiguous window of rows, as a fill does, which keeps the HBM writes
+// sequential.  The walk table G_m holds the `levels` prefixes that the
+// indices can reach (c <= bit length of (last index >> m)).
+// Shape by output kind (measured on dim 1024): the store-bound outputs take
+// whole rows per CTA (up to 1024 dims, ~2 CTAs per SM as the walk table
+// allows), which keeps each row's 4 KB a single CTA's contiguous write; the
+// inverse-normal outputs, bound by erfinv's arithmetic, take half-rows (512
+// dims, half the table) and ~4 CTAs per SM for more resident warps.
+__host__ __device__ constexpr bool arithmetic_bound(int kind) {
+  return kind == TQF_SOBOL_NORMAL_F32 || kind == TQF_SOBOL_NORMAL_F64;
+}
 template <int KIND, int VEC>
 __global__ void __launch_bounds__(kThreads)
     sobol_rowmajor_kernel(const uint32_t* __restrict__ v, int dim, int64_t n, uint32_t first_index,
-                          int nd, int dx, int m, int P, void* __restrict__ out_raw) {
+                          int nd, int dx, int mt, int m, int levels, void* __restrict__ out_raw) {
   using T = typename SobolOut<KIND>::T;
   T* out = static_cast<T*>(out_raw);
-  extern __shared__ uint32_t g_tab[];  // [32 - m][dx * VEC]
+  extern __shared__ uint32_t g_tab[];  // [levels][dx * VEC]
   const int sh = 32 - nd;
   const int width = dx * VEC;
   const int dim0 = blockIdx.y * width;
-  const int levels = 32 - m;
   for (int idx = threadIdx.x; idx < width; idx += blockDim.x) {
     const int d = dim0 + idx;
     uint32_t run = 0;
@@ -94,10 +106,10 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
   const int tx = threadIdx.x % dx;
   const int py = threadIdx.x / dx;
-  const int PT = 1 << m;
   const int dl = tx * VEC;  // local dim
   const int d = dim0 + dl;
-  int64_t row = (int64_t)blockIdx.x * PT * P + py;
+  const int64_t stride = (int64_t)1 << m;
+  int64_t row = ((int64_t)blockIdx.x << mt) + py;
   uint32_t i = first_index + (uint32_t)row;
   uint32_t x[VEC];
 #pragma unroll
@@ -105,7 +117,7 @@ __global__ void __launch_bounds__(kThreads)
   const float scf = __uint_as_float((uint32_t)(127 - nd) << 23);  // 2^-nd
   const double scd = ldexp(1.0, -nd);
   const bool full = (VEC == 4) && (d + 3 < dim);
-  for (int s = 0; s < P && row < n; ++s) {
+  for (; row < n; row += stride) {
     T* dst = out + row * (int64_t)dim + d;
     if (VEC == 4 && full && sizeof(T) == 4) {
       uint4 w;
@@ -123,8 +135,7 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t* g = g_tab + c * width + dl;
 #pragma unroll
     for (int e = 0; e < VEC; ++e) x[e] ^= g[e];
-    i += (uint32_t)PT;
-    row += PT;
+    i += (uint32_t)stride;
   }
 }
 
@@ -180,22 +191,37 @@ int launch_rowmajor(const uint32_t* v, int dim, int64_t n, uint32_t first, int n
                     cudaStream_t s) {
   const bool vec4 = (dim % 4 == 0) && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0);
   const int vec = vec4 ? 4 : 1;
+  // a CTA spans up to dx_cap * vec dims with dx dim-threads
   int need = (dim + vec - 1) / vec;
   int dx = 1;
-  while (dx < need && dx < 64) dx <<= 1;
+  const int dx_cap = arithmetic_bound(KIND) ? 128 : 256;
+  while (dx < need && dx < dx_cap) dx <<= 1;
   const int pt = kThreads / dx;
-  int m = 0;
-  while ((1 << m) < pt) ++m;
-  const int P = 128;
-  const int64_t gx = (n + (int64_t)pt * P - 1) / ((int64_t)pt * P);
+  int mt = 0;
+  while ((1 << mt) < pt) ++mt;
   const int gy = (dim + dx * vec - 1) / (dx * vec);
-  TQF_REQUIRE(gx <= 2147483647LL && gy <= 65535, "tqf_sobol_sample: request too large for one launch");
-  const size_t smem = (size_t)(32 - m) * dx * vec * sizeof(uint32_t);
+  // a power of two along the rows, and no more CTAs than rows / pt
+  int64_t want = (int64_t)(arithmetic_bound(KIND) ? 4 : 2) * num_sms() / gy;
+  if (want < 1) want = 1;
+  int64_t gx = 1;
+  while (gx * 2 <= want && gx * 2 * pt <= n) gx *= 2;
+  int q = 0;
+  while ((1LL << q) < gx) ++q;
+  const int m = mt + q;
+  TQF_REQUIRE(m <= 31 && gy <= 65535, "tqf_sobol_sample: request too large for one launch");
+  // c = trailing ones of (i >> m) <= bit length of (last index >> m)
+  const uint32_t last = (uint32_t)(first + (uint32_t)(n - 1)) >> m;
+  int levels = 1;
+  while (levels < 32 - m && (last >> (levels - 1)) != 0u) ++levels;
+  const size_t smem = (size_t)levels * dx * vec * sizeof(uint32_t);
   dim3 grid((unsigned)gx, (unsigned)gy);
-  if (vec4)
-    sobol_rowmajor_kernel<KIND, 4><<<grid, kThreads, smem, s>>>(v, dim, n, first, nd, dx, m, P, out);
-  else
-    sobol_rowmajor_kernel<KIND, 1><<<grid, kThreads, smem, s>>>(v, dim, n, first, nd, dx, m, P, out);
+  if (vec4) {
+    set_smem_config(sobol_rowmajor_kernel<KIND, 4>, smem);
+    sobol_rowmajor_kernel<KIND, 4><<<grid, kThreads, smem, s>>>(v, dim, n, first, nd, dx, mt, m, levels, out);
+  } else {
+    set_smem_config(sobol_rowmajor_kernel<KIND, 1>, smem);
+    sobol_rowmajor_kernel<KIND, 1><<<grid, kThreads, smem, s>>>(v, dim, n, first, nd, dx, mt, m, levels, out);
+  }
   return check_launch("sobol_rowmajor_kernel");
 }
 
