@@ -51,10 +51,10 @@ PARAMS = dict(spot=100.0, variance=0.04, mean_reversion=2.0, theta=0.04, volvol=
 ALU_OPS_PER_PATH_STEP = 40 + 14 + 14
 # DRAM bytes (read + write) per launch of the fused kernel: mean of two
 # full-size launches (2^22 paths x 252 steps, 64 strikes) captured with
-# `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum` (47,616 + 0 and
-# 39,936 + 0 bytes): the step table, strikes and parameters; the per-CTA FP64
-# partial sums stay in L2.  profiles/heston_ft_f32_pricing.md.
-NCU_TRAFFIC_BYTES = 43776
+# `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum` (43,776 + 0 and
+# 155,392 + 0 bytes): the step table, strikes and parameters; the per-CTA FP64
+# partial sums stay in L2 (the ncu summary of this kernel under profiles/).
+NCU_TRAFFIC_BYTES = 99584
 
 
 def strikes():
@@ -402,7 +402,8 @@ def run_sobol(dim=1024, total_points=1 << 26, chunk=1 << 20, timed_chunks=8):
     for the uint32, float32 and float32 inverse-normal outputs.  Timed chunks
     are spread over the index range (chunk c * total/(timed*chunk)); each is
     written once, larger than L2.  Roofline: 4 B written per element against
-    the measured copy bandwidth."""
+    the measured copy bandwidth, and against the write-only bandwidth of a
+    fill of the same buffer measured here."""
     import torch
     from tqf import _lib
     from tqf.math.random import sobol
@@ -416,6 +417,19 @@ def run_sobol(dim=1024, total_points=1 << 26, chunk=1 << 20, timed_chunks=8):
     peak = peaks.get("hbm_gbs")
     res = {"config": f"dim {dim}, {total_points} points, nd {nd}, chunks of {chunk} points, "
                      f"{timed_chunks} chunks timed (every {spacing}th)"}
+    # write-only ceiling of this GPU: torch's fill of the same 4 GiB buffer
+    # (the measured copy bandwidth counts read + write bytes)
+    fill_ms = []
+    for j in range(8):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out.fill_(j)
+        e1.record(stream)
+        e1.synchronize()
+        if j >= 3:
+            fill_ms.append(e0.elapsed_time(e1))
+    fill_gbs = chunk * dim * 4 / (sorted(fill_ms)[len(fill_ms) // 2] / 1e3) / 1e9
+    res["write_fill_gbs"] = fill_gbs
     for kind, tag in [(_lib.SOBOL_U32, "u32"), (_lib.SOBOL_F32, "f32"), (_lib.SOBOL_NORMAL_F32, "normal_f32")]:
         def launch(c):
             _lib.call("tqf_sobol_sample", v.data_ptr(), dim, chunk, c * chunk, nd, kind, out.data_ptr(),
@@ -433,7 +447,7 @@ def run_sobol(dim=1024, total_points=1 << 26, chunk=1 << 20, timed_chunks=8):
         sec = sum(ms) / 1e3 / timed_chunks
         gbs = chunk * dim * 4 / sec / 1e9
         res[tag] = {"seconds_per_chunk": sec, "points_per_s": chunk / sec, "write_gbs": gbs,
-                    "frac_of_hbm": gbs / peak, "peak_source": peak_src,
+                    "frac_of_hbm": gbs / peak, "peak_source": peak_src, "frac_of_write_fill": gbs / fill_gbs,
                     "full_set_seconds": sec * total_points / chunk}
     del out
     torch.cuda.empty_cache()
