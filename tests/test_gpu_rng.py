@@ -16,7 +16,10 @@ def _u32(t):
 
 @pytest.mark.parametrize("dim,n,skip", [(1, 1, 0), (2, 5, 0), (5, 31, 0), (7, 1000, 17), (16, 4099, 0),
                                         (1024, 3000, 0), (13, 2 ** 16, 123), (1, 3, 2 ** 31 - 5),
-                                        (504, 4097, 0), (33, 777, 2 ** 20)])
+                                        (504, 4097, 0), (33, 777, 2 ** 20),
+                                        # several column slices per row: whole (2048), partial last
+                                        # slice (1028), scalar stores (1025, 4099)
+                                        (2048, 1500, 0), (1028, 777, 3), (1025, 2000, 5), (4099, 300, 1)])
 def test_sobol_integers_bit_exact(cuda, dim, n, skip):
     from tqf.math.random import sobol
     got = _u32(sobol.sample_uint32(dim, n, skip))
@@ -63,6 +66,19 @@ def test_sobol_normals_close_to_erfinv(cuda):
     got64 = sobol.sample_normal(12, 5000, skip=5, dtype=torch.float64).cpu().numpy()
     want64 = osobol.normal_from_uniform(osobol.sample(12, 5000, skip=5, dtype=np.float64))
     np.testing.assert_allclose(got64, want64, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("dim,n,skip", [(1024, 3000, 7), (1030, 1000, 0)])
+def test_sobol_wide_outputs_match_oracle(cuda, dim, n, skip):
+    """float32, float32-normal and float64 outputs of wide requests (whole-row
+    and half-row CTAs, scalar stores for dim % 4 != 0) against the oracle."""
+    from tqf.math.random import sobol
+    u32 = osobol.sample(dim, n, skip=skip, dtype=np.float32)
+    np.testing.assert_array_equal(sobol.sample(dim, n, skip=skip).cpu().numpy(), u32)
+    np.testing.assert_array_equal(sobol.sample(dim, n, skip=skip, dtype=torch.float64).cpu().numpy(),
+                                  osobol.sample(dim, n, skip=skip, dtype=np.float64))
+    got = sobol.sample_normal(dim, n, skip=skip).cpu().numpy()
+    np.testing.assert_allclose(got, osobol.normal_from_uniform(u32), rtol=2e-6, atol=2e-6)
 
 
 def test_sobol_draw_layout(cuda):
