@@ -637,6 +637,9 @@ typedef struct tqf_heston_asian_args {
 } tqf_heston_asian_args;
 
 TQF_API int tqf_heston_asian(const tqf_heston_asian_args* args, void* stream);
+/* Device workspace (16-byte aligned) that modes 0 and 2 need: the per-CTA
+ * FP64 partial sums and, for mode 2, a two-step-block copy of the step table
+ * that the call writes before its path kernel reads it. */
 TQF_API size_t tqf_heston_asian_workspace_bytes(int32_t mode, int64_t num_paths, int32_t num_steps);
 /* Resident CTAs per SM of the tqf_heston_asian kernel for `mode`, or a
  * negative TQF_E_* code. */
