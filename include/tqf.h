@@ -770,6 +770,16 @@ TQF_API int tqf_european_payoff_sums(int32_t dtype, const void* values, int64_t 
 
 TQF_API size_t tqf_european_workspace_bytes(int64_t num_values, int32_t num_strikes);
 
+/* Monte Carlo estimate from payoff sums (the [num_strikes][2] (sum, sum of
+ * squares) output of the pricing calls): price_se[j] = discount * mean_j and
+ * price_se[num_strikes + j] = discount * sqrt(var_j / n) with the unbiased
+ * variance, all in FP64 on the device.  The reference's callers take the
+ * discounted mean of payoff tensors themselves (e.g.
+ * tff/models/heston/heston_model_test.py:349-352); this is that step as one
+ * kernel. */
+TQF_API int tqf_mc_price_stats(const double* sums, int32_t num_strikes, int64_t num_paths, double discount,
+                               double* price_se, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

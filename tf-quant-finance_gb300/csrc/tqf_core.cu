@@ -277,3 +277,30 @@ int tqf_european_payoff_sums(int32_t dtype, const void* values, int64_t stride,
 }
 
 }  // extern "C"
+
+// ---- Monte Carlo estimate from payoff sums ---------------------------------
+namespace tqf {
+namespace {
+__global__ void mc_price_stats_kernel(const double* __restrict__ sums, int ns, int64_t n, double discount,
+                                      double* __restrict__ price_se) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ns) return;
+  const double dn = (double)n;
+  const double mean = sums[2 * j] / dn;
+  double var = sums[2 * j + 1] / dn - mean * mean;
+  var = (var > 0.0 ? var : 0.0) * (dn / (n > 1 ? dn - 1.0 : 1.0));
+  price_se[j] = discount * mean;
+  price_se[ns + j] = discount * sqrt(var / dn);
+}
+}  // namespace
+}  // namespace tqf
+
+extern "C" int tqf_mc_price_stats(const double* sums, int32_t num_strikes, int64_t num_paths, double discount,
+                                  double* price_se, void* stream) {
+  tqf::clear_error();
+  TQF_REQUIRE(sums && price_se, "tqf_mc_price_stats: null pointer");
+  TQF_REQUIRE(num_strikes >= 1 && num_paths >= 1, "tqf_mc_price_stats: num_strikes and num_paths must be >= 1");
+  tqf::mc_price_stats_kernel<<<(num_strikes + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(
+      sums, num_strikes, num_paths, discount, price_se);
+  return tqf::check_launch("mc_price_stats_kernel");
+}

@@ -473,6 +473,7 @@ _SIGNATURES = {
     "tqf_heston_workspace_bytes": (ctypes.c_size_t, [c_i32, c_i32, c_i64, c_i32]),
     "tqf_european_payoff_sums": (ctypes.c_int, [c_i32, c_vp, c_i64, c_i64, c_i32, ctypes.POINTER(Payoff), c_vp]),
     "tqf_european_workspace_bytes": (ctypes.c_size_t, [c_i64, c_i32]),
+    "tqf_mc_price_stats": (ctypes.c_int, [c_vp, c_i32, c_i64, ctypes.c_double, c_vp, c_vp]),
     "tqf_heston_euler_adjoint": (ctypes.c_int, [ctypes.POINTER(HestonAdjointArgs), c_vp]),
     "tqf_heston_adjoint_workspace_bytes": (ctypes.c_size_t, [c_i64]),
     "tqf_cholesky_f64": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp, c_vp]),

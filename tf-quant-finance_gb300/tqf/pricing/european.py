@@ -36,22 +36,30 @@ class MonteCarloResult:
 
 
 def stats_from_sums(sums: torch.Tensor, n: int, discount: float) -> MonteCarloResult:
-    s1 = sums[:, 0]
-    s2 = sums[:, 1]
-    mean = s1 / n
-    var = torch.clamp(s2 / n - mean * mean, min=0.0) * (n / max(n - 1, 1))
-    se = torch.sqrt(var / n)
-    return MonteCarloResult(price=discount * mean, standard_error=discount * se, sums=sums,
+    """Discounted means and standard errors (unbiased variance) of the
+    [n_strikes, 2] payoff sums, in one kernel (tqf_mc_price_stats)."""
+    ns = int(sums.shape[0])
+    price_se = torch.empty((2, ns), dtype=torch.float64, device=sums.device)
+    _lib.call("tqf_mc_price_stats", sums.data_ptr(), ns, int(n), float(discount), price_se.data_ptr(),
+              _lib.stream_ptr(sums.device))
+    return MonteCarloResult(price=price_se[0], standard_error=price_se[1], sums=sums,
                             num_paths=n, discount=discount)
 
 
 def make_payoff(strikes, is_call, dtype, device, num_paths, ws_bytes_fn, tag):
-    k = torch.as_tensor(utils.to_numpy(strikes, np.float64).reshape(-1), dtype=dtype).to(device)
+    if isinstance(strikes, torch.Tensor) and strikes.dtype == dtype and not strikes.is_cuda:
+        # host tensor in the compute dtype: one copy, asynchronous on the
+        # current stream when the tensor is pinned (the caller keeps it
+        # unchanged until the stream has passed the call, as for any
+        # non-blocking copy), synchronous otherwise
+        k = strikes.reshape(-1).to(device, non_blocking=strikes.is_pinned())
+    else:
+        k = torch.as_tensor(utils.to_numpy(strikes, np.float64).reshape(-1), dtype=dtype).to(device)
     ns = int(k.numel())
     calls = None
     if is_call is not None:
         calls = torch.as_tensor(np.broadcast_to(np.asarray(is_call, dtype=np.uint8), (ns,)).copy()).to(device)
-    out = torch.zeros((ns, 2), dtype=torch.float64, device=device)
+    out = torch.empty((ns, 2), dtype=torch.float64, device=device)  # written whole by the sum reduction
     nbytes = int(ws_bytes_fn(ns))
     ws = workspace(nbytes, device, tag)
     p = _lib.Payoff()

@@ -38,29 +38,41 @@ def heston_european_mc(*, strikes, expiry, spot, variance, mean_reversion, theta
                        scheme="full_truncation", random_type=RandomType.STATELESS, seed=(1, 2),
                        dtype=torch.float32, path_offset=0, normal_draws=None):
     """Returns a MonteCarloResult with per-strike discounted prices and
-    standard errors (FP64 on the device)."""
+    standard errors (FP64 on the device).  Strikes given as a pinned host
+    tensor in the compute dtype are copied asynchronously on the current
+    stream (keep them unchanged until the stream has passed the call)."""
     device = _lib.require_cuda()
     td = utils.torch_dtype(dtype)
     np_dt = utils.np_dtype(td)
     T, r = float(expiry), float(discount_rate)
     steps = int(num_time_steps)
     N = int(num_samples)
-    all_times = np.linspace(0.0, T, steps + 1).astype(np_dt)
-    dt = (all_times[1:] - all_times[:-1]).astype(np_dt)
-    sqrt_dt = np.sqrt(dt).astype(np_dt)
-    no_slots = np.full(steps, -1, dtype=np.int32)
     qe = scheme == "qe"
     params = (float(mean_reversion), float(theta), float(volvol), float(rho))
+
+    def grid():  # uniform grid, built only when the step table is not cached
+        all_times = np.linspace(0.0, T, steps + 1).astype(np_dt)
+        dt = (all_times[1:] - all_times[:-1]).astype(np_dt)
+        return all_times, dt, np.sqrt(dt).astype(np_dt), np.full(steps, -1, dtype=np.int32)
+
     if qe:
-        model = heston_model.HestonModel(*params, dtype=np_dt)
         key = ("qe", np_dt.str, T, steps, params, device.index)
-        tab = _table(key, lambda: model._qe_table(all_times, 1e-6, no_slots, steps), td, device)
+
+        def build():
+            all_times, _, _, no_slots = grid()
+            return heston_model.HestonModel(*params, dtype=np_dt)._qe_table(all_times, 1e-6, no_slots, steps)
+
+        tab = _table(key, build, td, device)
         x0, scale = float(np.log(spot)), float(np.exp(r * T))
     else:
-        h = HestonFullTruncation(r, *params)
         key = ("ft", np_dt.str, T, steps, params, r, device.index)
-        tab = _table(key, lambda: heston_model.full_truncation_table(h, all_times, dt, sqrt_dt, no_slots, steps),
-                     td, device)
+
+        def build():
+            all_times, dt, sqrt_dt, no_slots = grid()
+            return heston_model.full_truncation_table(HestonFullTruncation(r, *params), all_times, dt, sqrt_dt,
+                                                      no_slots, steps)
+
+        tab = _table(key, build, td, device)
         x0, scale = float(np.log(spot)), 1.0
     if normal_draws is not None:
         draws = mvn.memory_draws(normal_draws, path_axis=0, step_axis=1)
