@@ -99,17 +99,31 @@ __device__ __forceinline__ float sqrt_approx(float x) {
 }
 __device__ __forceinline__ double sqrt_approx(double x) { return sqrt(x); }
 
+// Flush-to-zero SFU forms: the same approximations as __log2f / __sincosf
+// on normal inputs, without the subnormal handling around them.
+__device__ __forceinline__ float lg2_ftz(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ void sincos_ftz(float x, float& s, float& c) {
+  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"(x));
+  asm("cos.approx.ftz.f32 %0, %1;" : "=f"(c) : "f"(x));
+}
+
 // Two N(0,1) from two 32-bit words (radius from a, angle from b).  Uses the
 // SFU approximations (lg2, sqrt, sin, cos); the angle is taken in [-pi, pi)
-// where the hardware sin/cos are accurate.
+// where the hardware sin/cos are accurate.  All SFU inputs are normal numbers
+// (u1 >= 2^-32; the angle is 0 or at least 2 pi 2^-23 in magnitude), so the
+// flush-to-zero forms change nothing.
 __device__ __forceinline__ void box_muller_f32(uint32_t a, uint32_t b, float& z0,
                                                float& z1) {
   const float u1 = u01_oc_f32(a);
   const float u2 = u01_co_f32(b);
-  const float rad = sqrt_approx(__fmul_rn(-1.3862943611198906f, __log2f(u1)));  // sqrt(-2 ln u1)
+  const float rad = sqrt_approx(__fmul_rn(-1.3862943611198906f, lg2_ftz(u1)));  // sqrt(-2 ln u1)
   const float ang = __fmul_rn(__fsub_rn(u2, 0.5f), 6.283185307179586f);
   float s, c;
-  __sincosf(ang, &s, &c);
+  sincos_ftz(ang, s, c);
   z0 = __fmul_rn(rad, c);
   z1 = __fmul_rn(rad, s);
 }
@@ -161,16 +175,6 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)), "l"(f2_bits(c)));
   return f2_from_bits(d);
 }
-__device__ __forceinline__ float lg2_ftz(float x) {
-  float y;
-  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ void sincos_ftz(float x, float& s, float& c) {
-  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"(x));
-  asm("cos.approx.ftz.f32 %0, %1;" : "=f"(c) : "f"(x));
-}
-
 // The four normals of one Philox block as two pairs, even = (z0, z2) and
 // odd = (z1, z3), with (z0, z1) from words (x, y) and (z2, z3) from (z, w):
 // the arithmetic of box_muller_f32 run on both halves at once in f32x2
@@ -241,13 +245,18 @@ __device__ __forceinline__ void ft_half_step(const float4 q, float dw0, float e,
   v = fmaf(sq, e, u.y);
 }
 
-// Four float normals of block b for path n: draw dims 4b..4b+3.
+// Four float normals of block b for path n: draw dims 4b..4b+3 (the two
+// Box–Muller pairs in f32x2 form, equal to box_muller_f32 on each pair).
 __device__ __forceinline__ void philox_normals4_f32(int64_t block, int64_t path,
                                                     uint32_t k0, uint32_t k1,
                                                     float z[4]) {
   uint4 r = philox4x32_10(philox_counter(block, path), k0, k1);
-  box_muller_f32(r.x, r.y, z[0], z[1]);
-  box_muller_f32(r.z, r.w, z[2], z[3]);
+  float2 ze, zo;
+  box_muller_pair_f32(r, ze, zo);
+  z[0] = ze.x;
+  z[1] = zo.x;
+  z[2] = ze.y;
+  z[3] = zo.y;
 }
 // Two double normals of block b: draw dims 2b, 2b+1.
 __device__ __forceinline__ void philox_normals2_f64(int64_t block, int64_t path,
