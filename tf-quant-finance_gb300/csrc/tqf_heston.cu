@@ -23,11 +23,16 @@ constexpr int kQeCols = 12;
 constexpr size_t kMaxStagedTable = 96 * 1024;
 
 struct SmemLayout {
-  size_t bar, table, acc, spot, strike, call, total;
+  size_t bar, table, acc, spot, strike, call, stage, total;
 };
 
+// Recorded states are staged in shared memory, kStage<T> consecutive slots
+// (128 bytes of a path's output row) per flush; see SlotStager.
 template <typename T>
-SmemLayout smem_layout(int steps, int cols, int ns, bool staged) {
+constexpr int kStage = 128 / (2 * (int)sizeof(T));
+
+template <typename T>
+SmemLayout smem_layout(int steps, int cols, int ns, bool staged, bool store) {
   SmemLayout L;
   size_t off = 0;
   L.bar = off;
@@ -45,6 +50,9 @@ SmemLayout smem_layout(int steps, int cols, int ns, bool staged) {
   off += (size_t)ns * sizeof(T);
   L.call = off;
   off += (size_t)ns;
+  off = (off + 15) & ~(size_t)15;
+  L.stage = off;
+  if (store) off += (size_t)kStage<T> * (kBlock + 1) * 2 * sizeof(T);
   L.total = (off + 15) & ~(size_t)15;
   return L;
 }
@@ -151,15 +159,49 @@ struct Vec2<double> {
   using type = double2;
 };
 
+// Coalesced output of the recorded states.  Each recorded step a thread puts
+// its (x, v) into row `cnt` of a [kStage][kBlock + 1] shared-memory buffer;
+// when the buffer is full, or the next slot does not continue the buffered
+// run, the CTA writes the run out: consecutive threads take consecutive slots
+// of one path, so a warp stores whole 128-byte pieces of two output rows
+// instead of 32 scattered 8-byte pieces (the padded row stride keeps the
+// shared-memory reads conflict-free).  Slots come from the step table, so
+// every thread of the CTA puts and flushes at the same steps.
 template <typename T>
-__device__ __forceinline__ void store_state(const tqf_path_output& o, int64_t path, int slot, T x,
-                                            T v) {
+struct SlotStager {
   using V2 = typename Vec2<T>::type;
-  V2 w;
-  w.x = x;
-  w.y = v;
-  reinterpret_cast<V2*>(o.ptr)[path * o.num_slots + slot] = w;
-}
+  static constexpr int S = kStage<T>;
+  V2* buf;
+  int cnt, slot0;
+  __device__ explicit SlotStager(unsigned char* smem) : buf(reinterpret_cast<V2*>(smem)), cnt(0), slot0(0) {}
+  __device__ __forceinline__ void put(const tqf_path_output& o, int64_t row0, int64_t N, int slot, T x, T v) {
+    if (cnt > 0 && (cnt == S || slot != slot0 + cnt)) flush(o, row0, N);
+    if (cnt == 0) slot0 = slot;
+    V2 w;
+    w.x = x;
+    w.y = v;
+    buf[cnt * (kBlock + 1) + threadIdx.x] = w;
+    ++cnt;
+  }
+  __device__ __forceinline__ void flush(const tqf_path_output& o, int64_t row0, int64_t N) {
+    __syncthreads();
+    V2* out = reinterpret_cast<V2*>(o.ptr);
+    if (cnt == S) {
+#pragma unroll 4
+      for (int idx = threadIdx.x; idx < S * kBlock; idx += kBlock) {
+        const int p = idx / S, j = idx % S;
+        if (row0 + p < N) out[(row0 + p) * o.num_slots + slot0 + j] = buf[j * (kBlock + 1) + p];
+      }
+    } else {
+      for (int idx = threadIdx.x; idx < cnt * kBlock; idx += kBlock) {
+        const int p = idx / cnt, j = idx - p * cnt;
+        if (row0 + p < N) out[(row0 + p) * o.num_slots + slot0 + j] = buf[j * (kBlock + 1) + p];
+      }
+    }
+    __syncthreads();
+    cnt = 0;
+  }
+};
 
 // SCHEME 0 = full-truncation Euler, 1 = QE.  SRC = TQF_DRAWS_* (compile-time);
 // ANTI: antithetic Philox pairing.
@@ -205,15 +247,21 @@ __global__ void __launch_bounds__(kBlock)
   const T spot_scale = (T)a.payoff.spot_scale;
   const int64_t N = a.num_paths;
   const int64_t per_round = (int64_t)gridDim.x * kBlock;
+  SlotStager<T> stg(smem + L.stage);
   for (int64_t base = 0; base < N; base += per_round) {
-    const int64_t path = base + (int64_t)blockIdx.x * kBlock + threadIdx.x;
+    const int64_t row0 = base + (int64_t)blockIdx.x * kBlock;
+    const int64_t path = row0 + threadIdx.x;
     const bool valid = path < N;
+    // with stores every thread runs the steps (the stager's flushes are CTA
+    // barriers); a thread past the last path simulates that path again and
+    // its output is dropped
+    const int64_t pc = valid ? path : N - 1;
     T x = x0, v = v0;
-    if (valid) {
-      if (STORE && a.output.init_slot >= 0) store_state<T>(a.output, path, a.output.init_slot, x, v);
+    if (valid || STORE) {
+      if (STORE && a.output.init_slot >= 0) stg.put(a.output, row0, N, a.output.init_slot, x, v);
       if (SRC == TQF_DRAWS_PHILOX && sizeof(T) == 4) {
         // Canonical stream, 2 normals per step: block b = steps 2b, 2b+1.
-        int64_t p = path;
+        int64_t p = pc;
         float sign = 1.f;
         if (ANTI && p >= a.draws.antithetic_half) {
           p -= a.draws.antithetic_half;
@@ -233,13 +281,13 @@ __global__ void __launch_bounds__(kBlock)
             ft_step<T>(row, (T)za, (T)zb, x, v);
             if (STORE) {
               const int slot = (int)row.slot;
-              if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+              if (slot >= 0) stg.put(a.output, row0, N, slot, x, v);
             }
           } else {
             qe_step<T>(r0, (T)za, (T)zb, x, v);
             if (STORE) {
               const int slot = (int)r0[COLS - 1];
-              if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+              if (slot >= 0) stg.put(a.output, row0, N, slot, x, v);
             }
           }
         };
@@ -261,13 +309,13 @@ __global__ void __launch_bounds__(kBlock)
               ft_half_step(qa, dw0.x, e.x, x, v);
               if (STORE) {
                 const int slot = (int)qx.z;
-                if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+                if (slot >= 0) stg.put(a.output, row0, N, slot, x, v);
               }
               if (both) {
                 ft_half_step(tp[4 * pb + 1], dw0.y, e.y, x, v);
                 if (STORE) {
                   const int slot = (int)qx.w;
-                  if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+                  if (slot >= 0) stg.put(a.output, row0, N, slot, x, v);
                 }
               }
             };
@@ -294,7 +342,7 @@ __global__ void __launch_bounds__(kBlock)
           one_step(i, z0, z1);
         }
       } else {
-        DrawSource<T> src(a.draws, path, 2);
+        DrawSource<T> src(a.draws, pc, 2);
         for (int i = 0; i < steps; ++i) {
           const T z0 = src.get(i, 0);
           const T z1 = src.get(i, 1);
@@ -303,11 +351,12 @@ __global__ void __launch_bounds__(kBlock)
           else qe_step<T>(r0, z0, z1, x, v);
           if (STORE) {
             const int slot = (int)r0[COLS - 1];
-            if (slot >= 0) store_state<T>(a.output, path, slot, x, v);
+            if (slot >= 0) stg.put(a.output, row0, N, slot, x, v);
           }
         }
       }
     }
+    if (STORE && stg.cnt > 0) stg.flush(a.output, row0, N);
     if (PRICE) {
       __syncthreads();
       s_spot[threadIdx.x] = valid ? spot_scale * exp(x) : T(NAN);
@@ -483,7 +532,7 @@ template <typename T, int SCHEME>
 int grid_for(int64_t N, int ns, int steps, bool staged, int src, bool store, bool price,
              SmemLayout* out_layout, bool anti = false) {
   const int cols = SCHEME == 0 ? kFtCols : kQeCols;
-  SmemLayout L = smem_layout<T>(steps, cols, price ? ns : 0, staged);
+  SmemLayout L = smem_layout<T>(steps, cols, price ? ns : 0, staged, store);
   if (out_layout) *out_layout = L;
   auto k = pick_kernel<T, SCHEME>(src, store, price, anti);
   set_smem_config(k, L.total);
