@@ -21,7 +21,18 @@ struct AffineCoef {
   T m[DM], M[DM * DM], s0[DM], s1[DM], C[DM * DM];
 };
 
-template <typename T, int DM, int SRC>
+// Shared memory: mbarrier, coefficients, the staged step table, then (STAGE)
+// the output staging buffer.
+template <typename T, int DM>
+__host__ __device__ inline size_t affine_stage_offset(int steps, bool staged) {
+  const size_t head = (16 + sizeof(AffineCoef<T, DM>) + 15) & ~(size_t)15;
+  return (head + (staged ? (size_t)steps * kCols * sizeof(T) : 0) + 15) & ~(size_t)15;
+}
+
+// STAGE: recorded states go through the coalescing RowStager (chosen when a
+// path's output row is long enough for scattered stores to cost more than
+// the stager's registers and shared memory).
+template <typename T, int DM, int SRC, bool STAGE>
 __global__ void __launch_bounds__(kBlock)
     euler_affine_kernel(tqf_euler_affine_args a, int staged) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -57,19 +68,31 @@ __global__ void __launch_bounds__(kBlock)
   const int64_t N = a.num_paths;
   T* out = static_cast<T*>(a.output.ptr);
   const int ns = a.output.num_slots;
-  for (int64_t path = (int64_t)blockIdx.x * kBlock + threadIdx.x; path < N;
-       path += (int64_t)gridDim.x * kBlock) {
+  // with the stager every thread runs every round (a thread past the last
+  // path simulates that path again and its output is dropped)
+  const bool stage_out = STAGE && out != nullptr;
+  RowStager<T, DM, kBlock> stg(smem + affine_stage_offset<T, DM>(steps, staged != 0), dim);
+  const int64_t per_round = (int64_t)gridDim.x * kBlock;
+  for (int64_t base = 0; base < N; base += per_round) {
+    const int64_t row0 = base + (int64_t)blockIdx.x * kBlock;
+    const int64_t path = row0 + threadIdx.x;
+    if (path >= N && !stage_out) break;
+    const int64_t pc = path < N ? path : N - 1;
     T x[DM];
-    const T* x0 = static_cast<const T*>(a.x0) + (a.x0_per_path ? path * dim : 0);
+    const T* x0 = static_cast<const T*>(a.x0) + (a.x0_per_path ? pc * dim : 0);
 #pragma unroll
     for (int j = 0; j < DM; ++j) x[j] = j < dim ? x0[j] : T(0);
     if (out && a.output.init_slot >= 0) {
-      T* o = out + (path * ns + a.output.init_slot) * dim;
+      if (stage_out) {
+        stg.put(out, ns, row0, N, a.output.init_slot, x);
+      } else {
+        T* o = out + (path * ns + a.output.init_slot) * dim;
 #pragma unroll
-      for (int j = 0; j < DM; ++j)
-        if (j < dim) o[j] = x[j];
+        for (int j = 0; j < DM; ++j)
+          if (j < dim) o[j] = x[j];
+      }
     }
-    DrawSource<T> src(a.draws, path, dim);
+    DrawSource<T> src(a.draws, pc, dim);
     for (int i = 0; i < steps; ++i) {
       const T* row = table + (size_t)i * kCols;
       const T dt = row[0], sdt = row[1];
@@ -93,12 +116,17 @@ __global__ void __launch_bounds__(kBlock)
       for (int r = 0; r < DM; ++r) x[r] = xn[r];
       const int slot = (int)row[2];
       if (out && slot >= 0) {
-        T* o = out + (path * ns + slot) * dim;
+        if (stage_out) {
+          stg.put(out, ns, row0, N, slot, x);
+        } else {
+          T* o = out + (path * ns + slot) * dim;
 #pragma unroll
-        for (int j = 0; j < DM; ++j)
-          if (j < dim) o[j] = x[j];
+          for (int j = 0; j < DM; ++j)
+            if (j < dim) o[j] = x[j];
+        }
       }
     }
+    if (stage_out && stg.cnt > 0) stg.flush(out, ns, row0, N);
   }
 }
 
@@ -138,11 +166,17 @@ int launch_affine(const tqf_euler_affine_args& a, cudaStream_t s) {
   const size_t tab_bytes = (size_t)a.num_steps * kCols * sizeof(T);
   const bool staged = tab_bytes > 0 && tab_bytes <= 96 * 1024 &&
                       (reinterpret_cast<uintptr_t>(a.step_table) & 15u) == 0;
-  const size_t head = (16 + sizeof(AffineCoef<T, DM>) + 15) & ~(size_t)15;
-  const size_t smem = head + (staged ? tab_bytes : 0);
+  // stage the output when a path's row is at least 64 bytes
+  const bool stage_out =
+      a.output.ptr != nullptr && (size_t)a.output.num_slots * a.dim * sizeof(T) >= 64;
+  const size_t smem =
+      affine_stage_offset<T, DM>(a.num_steps, staged) + (stage_out ? RowStager<T, DM, kBlock>::kBytes : 0);
+  const bool philox = a.draws.source == TQF_DRAWS_PHILOX;
   void (*k)(tqf_euler_affine_args, int) =
-      a.draws.source == TQF_DRAWS_PHILOX ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX>
-                                         : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY>;
+      stage_out ? (philox ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX, true>
+                          : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY, true>)
+                : (philox ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX, false>
+                          : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY, false>);
   if (smem > 48 * 1024) set_smem_config(k, smem);
   int occ = 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem) != cudaSuccess || occ < 1)

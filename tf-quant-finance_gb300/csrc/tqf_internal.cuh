@@ -245,6 +245,56 @@ __device__ __forceinline__ void ft_half_step(const float4 q, float dw0, float e,
   v = fmaf(sq, e, u.y);
 }
 
+// ---- coalesced output of recorded path states ---------------------------------
+// A CTA of THREADS paths records w <= W values per recorded slot into output
+// rows out[path][slot][w].  Each recorded step a thread puts its w values
+// into the next w rows of a [S w][THREADS + 1] shared-memory buffer (S slots
+// ~ 128 bytes of a path's row); when the buffer is full, or the next slot
+// does not continue the buffered run, the CTA writes the run out with
+// consecutive threads on consecutive values of one path, so each warp stores
+// whole pieces of output rows instead of 32 scattered ones (the padded row
+// stride keeps the shared-memory reads conflict-free; the value -> (path,
+// offset) walk is incremental, one division per flush).  put() and flush()
+// are CTA barriers: every thread of the CTA calls them at the same steps (the
+// slots come from a table shared by the CTA), including threads whose path
+// is past the end (their values are dropped).
+template <typename T, int W, int THREADS>
+struct RowStager {
+  static constexpr int kRowValues = 128 / (int)sizeof(T);
+  static constexpr int kMaxPerPath = W > kRowValues ? W : kRowValues;
+  static constexpr size_t kBytes = (size_t)kMaxPerPath * (THREADS + 1) * sizeof(T);
+  T* buf;
+  int w, S, cnt, slot0;
+  __device__ RowStager(void* smem, int width)
+      : buf(static_cast<T*>(smem)), w(width), S(kRowValues / width > 0 ? kRowValues / width : 1), cnt(0),
+        slot0(0) {}
+  __device__ __forceinline__ void put(T* out, int num_slots, int64_t row0, int64_t N, int slot, const T* x) {
+    if (cnt > 0 && (cnt == S || slot != slot0 + cnt)) flush(out, num_slots, row0, N);
+    if (cnt == 0) slot0 = slot;
+#pragma unroll
+    for (int c = 0; c < W; ++c)
+      if (c < w) buf[(cnt * w + c) * (THREADS + 1) + threadIdx.x] = x[c];
+    ++cnt;
+  }
+  __device__ __forceinline__ void flush(T* out, int num_slots, int64_t row0, int64_t N) {
+    __syncthreads();
+    const int per = cnt * w;  // values of one path in this run
+    const int dq = THREADS / per, dr = THREADS - dq * per;
+    int p = threadIdx.x / per, e = threadIdx.x - p * per;
+    for (int idx = threadIdx.x; idx < per * THREADS; idx += THREADS) {
+      if (row0 + p < N) out[((row0 + p) * num_slots + slot0) * w + e] = buf[e * (THREADS + 1) + p];
+      p += dq;
+      e += dr;
+      if (e >= per) {
+        e -= per;
+        ++p;
+      }
+    }
+    __syncthreads();
+    cnt = 0;
+  }
+};
+
 // Four float normals of block b for path n: draw dims 4b..4b+3 (the two
 // Box–Muller pairs in f32x2 form, equal to box_muller_f32 on each pair).
 __device__ __forceinline__ void philox_normals4_f32(int64_t block, int64_t path,
