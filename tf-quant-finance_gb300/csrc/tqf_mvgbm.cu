@@ -50,18 +50,29 @@ __device__ __forceinline__ void load_coef(GbmCoef<T, DM>* c, int dim, const void
   }
 }
 
-template <typename T, int DM>
+// STAGE: recorded states go through the coalescing RowStager (dynamic
+// shared memory), chosen when a path's output row is at least 64 bytes; then
+// every thread runs every round and a thread past the last path simulates
+// that path again with its output dropped.
+template <typename T, int DM, bool STAGE>
 __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
   __shared__ GbmCoef<T, DM> coef;
+  extern __shared__ __align__(16) unsigned char stage_smem[];
   const int dim = a.dim;
   load_coef<T, DM>(&coef, dim, a.chol, a.drift, a.vol);
   __syncthreads();
   const T* table = static_cast<const T*>(a.step_table);
   T* out = static_cast<T*>(a.output.ptr);
   const int ns = a.output.num_slots;
-  for (int64_t path = (int64_t)blockIdx.x * kBlock + threadIdx.x; path < a.num_paths;
-       path += (int64_t)gridDim.x * kBlock) {
-    const T* x0p = static_cast<const T*>(a.x0) + (a.x0_per_path ? path * dim : 0);
+  const int64_t N = a.num_paths;
+  RowStager<T, DM, kBlock> stg(stage_smem, dim);
+  const int64_t per_round = (int64_t)gridDim.x * kBlock;
+  for (int64_t base = 0; base < N; base += per_round) {
+    const int64_t row0 = base + (int64_t)blockIdx.x * kBlock;
+    const int64_t path = row0 + threadIdx.x;
+    if (!STAGE && path >= N) break;
+    const int64_t pc = path < N ? path : N - 1;
+    const T* x0p = static_cast<const T*>(a.x0) + (a.x0_per_path ? pc * dim : 0);
     T x0[DM], cs[DM];
 #pragma unroll
     for (int j = 0; j < DM; ++j) {
@@ -69,12 +80,16 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
       cs[j] = T(0);
     }
     if (a.output.init_slot >= 0) {
-      T* o = out + (path * ns + a.output.init_slot) * dim;
+      if (STAGE) {
+        stg.put(out, ns, row0, N, a.output.init_slot, x0);
+      } else {
+        T* o = out + (path * ns + a.output.init_slot) * dim;
 #pragma unroll
-      for (int j = 0; j < DM; ++j)
-        if (j < dim) o[j] = x0[j];
+        for (int j = 0; j < DM; ++j)
+          if (j < dim) o[j] = x0[j];
+      }
     }
-    DrawSource<T> src(a.draws, path, dim);
+    DrawSource<T> src(a.draws, pc, dim);
     for (int i = 0; i < a.num_steps; ++i) {
       const T dt = table[i * 4], sdt = table[i * 4 + 1];
       const int slot = (int)table[i * 4 + 2];
@@ -89,12 +104,20 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
         cs[r] += coef.drift[r] * dt + sdt * coef.sigma[r] * y;
       }
       if (slot >= 0) {
-        T* o = out + (path * ns + slot) * dim;
+        if constexpr (STAGE) {
+          T xs[DM];
 #pragma unroll
-        for (int j = 0; j < DM; ++j)
-          if (j < dim) o[j] = x0[j] * exp(cs[j]);
+          for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
+          stg.put(out, ns, row0, N, slot, xs);
+        } else {
+          T* o = out + (path * ns + slot) * dim;
+#pragma unroll
+          for (int j = 0; j < DM; ++j)
+            if (j < dim) o[j] = x0[j] * exp(cs[j]);
+        }
       }
     }
+    if (STAGE && stg.cnt > 0) stg.flush(out, ns, row0, N);
   }
 }
 
@@ -384,13 +407,18 @@ __global__ void __launch_bounds__(256) cholesky_f64_kernel(const double* __restr
 
 template <typename T, int DM>
 int launch_paths(const tqf_mvgbm_args& a, cudaStream_t s) {
+  // stage the output when a path's row is at least 64 bytes
+  const bool stage = (size_t)a.output.num_slots * a.dim * sizeof(T) >= 64;
+  auto k = stage ? mvgbm_paths_kernel<T, DM, true> : mvgbm_paths_kernel<T, DM, false>;
+  const size_t smem = stage ? RowStager<T, DM, kBlock>::kBytes : 0;
+  if (smem > 48 * 1024) set_smem_config(k, smem);
   int occ = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mvgbm_paths_kernel<T, DM>, kBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem);
   if (occ < 1) occ = 1;
   int64_t grid = (a.num_paths + kBlock - 1) / kBlock;
   const int64_t cap = (int64_t)num_sms() * occ;
   if (grid > cap) grid = cap;
-  mvgbm_paths_kernel<T, DM><<<(unsigned)grid, kBlock, 0, s>>>(a);
+  k<<<(unsigned)grid, kBlock, smem, s>>>(a);
   return check_launch("mvgbm_paths_kernel");
 }
 
