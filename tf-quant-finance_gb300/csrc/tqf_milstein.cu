@@ -74,7 +74,19 @@ __device__ __forceinline__ void stratonovich_J(int d, int order, T dt, T sqrt_dt
     for (int j = 0; j < DM; ++j) J[i][j] = i == j ? dw[i] * dw[i] / T(2) : J[i][j] + dt * acc[i][j] / two_pi;
 }
 
-template <typename T, int DM, int SRC>
+// Shared memory: mbarrier, coefficients, staged step table, then (STAGE)
+// the output staging buffer.
+template <typename T, int DM>
+__host__ __device__ inline size_t milstein_stage_offset(int steps, bool staged) {
+  const size_t head = (16 + sizeof(AffineMil<T, DM>) + 15) & ~(size_t)15;
+  return (head + (staged ? (size_t)steps * 4 * sizeof(T) : 0) + 15) & ~(size_t)15;
+}
+
+// STAGE: recorded states go through the coalescing RowStager, chosen when a
+// path's output row is at least 64 bytes; then every thread runs every round
+// and a thread past the last path simulates that path again with its output
+// dropped.
+template <typename T, int DM, int SRC, bool STAGE>
 __global__ void __launch_bounds__(kBlock) milstein_affine_kernel(tqf_milstein_affine_args a, double rho_c,
                                                                  int staged) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -109,19 +121,29 @@ __global__ void __launch_bounds__(kBlock) milstein_affine_kernel(tqf_milstein_af
   const int K = d + 3 * d * order;  // normals per step
   T* out = static_cast<T*>(a.output.ptr);
   const int ns = a.output.num_slots;
-  for (int64_t path = (int64_t)blockIdx.x * kBlock + threadIdx.x; path < a.num_paths;
-       path += (int64_t)gridDim.x * kBlock) {
+  const int64_t N = a.num_paths;
+  RowStager<T, DM, kBlock> stg(smem + milstein_stage_offset<T, DM>(a.num_steps, staged != 0), d);
+  const int64_t per_round = (int64_t)gridDim.x * kBlock;
+  for (int64_t base = 0; base < N; base += per_round) {
+    const int64_t row0 = base + (int64_t)blockIdx.x * kBlock;
+    const int64_t path = row0 + threadIdx.x;
+    if (!STAGE && path >= N) break;
+    const int64_t pc = path < N ? path : N - 1;
     T x[DM];
-    const T* x0 = static_cast<const T*>(a.x0) + (a.x0_per_path ? path * d : 0);
+    const T* x0 = static_cast<const T*>(a.x0) + (a.x0_per_path ? pc * d : 0);
 #pragma unroll(DM <= 4 ? DM : 1)
     for (int j = 0; j < DM; ++j) x[j] = j < d ? x0[j] : T(0);
     if (a.output.init_slot >= 0) {
-      T* o = out + (path * ns + a.output.init_slot) * d;
+      if (STAGE) {
+        stg.put(out, ns, row0, N, a.output.init_slot, x);
+      } else {
+        T* o = out + (path * ns + a.output.init_slot) * d;
 #pragma unroll(DM <= 4 ? DM : 1)
-      for (int j = 0; j < DM; ++j)
-        if (j < d) o[j] = x[j];
+        for (int j = 0; j < DM; ++j)
+          if (j < d) o[j] = x[j];
+      }
     }
-    DrawSource<T> src(a.draws, path, K);
+    DrawSource<T> src(a.draws, pc, K);
     for (int i = 0; i < a.num_steps; ++i) {
       const T dt = table[i * 4], sdt = table[i * 4 + 1];
       const int slot = (int)table[i * 4 + 2];
@@ -167,12 +189,17 @@ __global__ void __launch_bounds__(kBlock) milstein_affine_kernel(tqf_milstein_af
 #pragma unroll(DM <= 4 ? DM : 1)
       for (int k = 0; k < DM; ++k) x[k] = xn[k];
       if (slot >= 0) {
-        T* o = out + (path * ns + slot) * d;
+        if (STAGE) {
+          stg.put(out, ns, row0, N, slot, x);
+        } else {
+          T* o = out + (path * ns + slot) * d;
 #pragma unroll(DM <= 4 ? DM : 1)
-        for (int j = 0; j < DM; ++j)
-          if (j < d) o[j] = x[j];
+          for (int j = 0; j < DM; ++j)
+            if (j < d) o[j] = x[j];
+        }
       }
     }
+    if (STAGE && stg.cnt > 0) stg.flush(out, ns, row0, N);
   }
 }
 
@@ -244,11 +271,16 @@ template <typename T, int DM>
 int launch_affine(const tqf_milstein_affine_args& a, cudaStream_t s) {
   const size_t tab_bytes = (size_t)a.num_steps * 4 * sizeof(T);
   const bool staged = tab_bytes > 0 && tab_bytes <= 96 * 1024 && (reinterpret_cast<uintptr_t>(a.step_table) & 15u) == 0;
-  const size_t head = (16 + sizeof(AffineMil<T, DM>) + 15) & ~(size_t)15;
-  const size_t smem = head + (staged ? tab_bytes : 0);
-  void (*k)(tqf_milstein_affine_args, double, int) = a.draws.source == TQF_DRAWS_PHILOX
-                                                         ? milstein_affine_kernel<T, DM, TQF_DRAWS_PHILOX>
-                                                         : milstein_affine_kernel<T, DM, TQF_DRAWS_MEMORY>;
+  // stage the output when a path's row is at least 64 bytes
+  const bool stage = (size_t)a.output.num_slots * a.dim * sizeof(T) >= 64;
+  const size_t smem =
+      milstein_stage_offset<T, DM>(a.num_steps, staged) + (stage ? RowStager<T, DM, kBlock>::kBytes : 0);
+  const bool philox = a.draws.source == TQF_DRAWS_PHILOX;
+  void (*k)(tqf_milstein_affine_args, double, int) =
+      stage ? (philox ? milstein_affine_kernel<T, DM, TQF_DRAWS_PHILOX, true>
+                      : milstein_affine_kernel<T, DM, TQF_DRAWS_MEMORY, true>)
+            : (philox ? milstein_affine_kernel<T, DM, TQF_DRAWS_PHILOX, false>
+                      : milstein_affine_kernel<T, DM, TQF_DRAWS_MEMORY, false>);
   if (smem > 48 * 1024) set_smem_config(k, smem);
   int occ = 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem) != cudaSuccess || occ < 1) occ = 1;

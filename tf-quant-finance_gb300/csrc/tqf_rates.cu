@@ -14,24 +14,42 @@ namespace {
 
 constexpr int kBlock = 256;
 
-template <typename T, int DM>
+// STAGE: recorded rates go through the coalescing RowStager (dynamic shared
+// memory), chosen when a path's output row is at least 64 bytes; then every
+// thread runs every round and a thread past the last path simulates that path
+// again with its output dropped.
+template <typename T, int DM, bool STAGE>
 __global__ void __launch_bounds__(kBlock) hull_white_kernel(tqf_hull_white_args a) {
+  extern __shared__ __align__(16) unsigned char stage_smem[];
   const int d = a.dim;
   const T* tab = static_cast<const T*>(a.table);
   const T* f0 = static_cast<const T*>(a.f0);
   const T* L = static_cast<const T*>(a.chol);
   T* out = static_cast<T*>(a.output.ptr);
   const int ns = a.output.num_slots;
-  for (int64_t path = (int64_t)blockIdx.x * kBlock + threadIdx.x; path < a.num_paths;
-       path += (int64_t)gridDim.x * kBlock) {
+  const int64_t N = a.num_paths;
+  RowStager<T, DM, kBlock> stg(stage_smem, d);
+  const int64_t per_round = (int64_t)gridDim.x * kBlock;
+  for (int64_t base = 0; base < N; base += per_round) {
+    const int64_t row0 = base + (int64_t)blockIdx.x * kBlock;
+    const int64_t path = row0 + threadIdx.x;
+    if (!STAGE && path >= N) break;
+    const int64_t pc = path < N ? path : N - 1;
     T x[DM];
 #pragma unroll
     for (int k = 0; k < DM; ++k) x[k] = T(0);
     if (a.output.init_slot >= 0) {
-      T* o = out + (path * ns + a.output.init_slot) * d;
-      for (int k = 0; k < d; ++k) o[k] = f0[k];
+      if constexpr (STAGE) {
+        T r0[DM];
+#pragma unroll
+        for (int k = 0; k < DM; ++k) r0[k] = k < d ? f0[k] : T(0);
+        stg.put(out, ns, row0, N, a.output.init_slot, r0);
+      } else {
+        T* o = out + (path * ns + a.output.init_slot) * d;
+        for (int k = 0; k < d; ++k) o[k] = f0[k];
+      }
     }
-    DrawSource<T> src(a.draws, path, d);
+    DrawSource<T> src(a.draws, pc, d);
     for (int i = 0; i < a.num_steps; ++i) {
       T z[DM], y[DM];
 #pragma unroll
@@ -56,26 +74,37 @@ __global__ void __launch_bounds__(kBlock) hull_white_kernel(tqf_hull_white_args 
         if (k < d) x[k] = row[3 * k] * x[k] + row[3 * k + 1] + row[3 * k + 2] * y[k];
       const int slot = a.slots[i];
       if (slot >= 0) {
-        T* o = out + (path * ns + slot) * d;
         const T* f = f0 + (size_t)(i + 1) * d;
+        if constexpr (STAGE) {
+          T r[DM];
 #pragma unroll
-        for (int k = 0; k < DM; ++k)
-          if (k < d) o[k] = x[k] + f[k];
+          for (int k = 0; k < DM; ++k) r[k] = k < d ? x[k] + f[k] : T(0);
+          stg.put(out, ns, row0, N, slot, r);
+        } else {
+          T* o = out + (path * ns + slot) * d;
+#pragma unroll
+          for (int k = 0; k < DM; ++k)
+            if (k < d) o[k] = x[k] + f[k];
+        }
       }
     }
+    if (STAGE && stg.cnt > 0) stg.flush(out, ns, row0, N);
   }
 }
 
 template <typename T, int DM>
 int launch(const tqf_hull_white_args& a, cudaStream_t s) {
+  // stage the output when a path's row is at least 64 bytes
+  const bool stage = (size_t)a.output.num_slots * a.dim * sizeof(T) >= 64;
+  auto k = stage ? hull_white_kernel<T, DM, true> : hull_white_kernel<T, DM, false>;
+  const size_t smem = stage ? RowStager<T, DM, kBlock>::kBytes : 0;
+  if (smem > 48 * 1024) set_smem_config(k, smem);
   int occ = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, hull_white_kernel<T, DM>, kBlock, 0) != cudaSuccess ||
-      occ < 1)
-    occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem) != cudaSuccess || occ < 1) occ = 1;
   int64_t grid = (a.num_paths + kBlock - 1) / kBlock;
   const int64_t cap = (int64_t)num_sms() * occ;
   if (grid > cap) grid = cap;
-  hull_white_kernel<T, DM><<<(unsigned)grid, kBlock, 0, s>>>(a);
+  k<<<(unsigned)grid, kBlock, smem, s>>>(a);
   return check_launch("hull_white_kernel");
 }
 
