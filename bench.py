@@ -549,6 +549,61 @@ def run_basket(paths_n=1 << 22, price_paths=1 << 22, n_steps=64, reps=10):
     return res
 
 
+def run_stored_paths(n_paths=N_PATHS, n_steps=N_STEPS, reps=5):
+    """Path sampling with every step recorded (the drop-in sample_paths /
+    euler_sampling.sample outputs, [N, 252, d] float32): Heston QE and
+    full-truncation Euler, GBM through euler_sampling (d = 1, 2, 3) and the
+    exact GBM sampler; the same calls recording only t = T show the cost of
+    the stores.  Median of `reps` calls through the public API, CUDA events;
+    write GB/s counts the output bytes."""
+    import torch
+    import tqf
+    from tqf.math.random import RandomType
+    from tqf.models import coefficients as co
+
+    def timed(fn):
+        out = fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = fn()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+            del out
+        return sorted(ts)[len(ts) // 2]
+
+    N = n_paths
+    times = (np.arange(1, n_steps + 1, dtype=np.float64) / n_steps).astype(np.float32)
+    last = np.array([1.0], np.float32)
+    rnd = dict(num_samples=N, random_type=RandomType.STATELESS, seed=[1, 2])
+    x0h = np.array([np.log(100.0), 0.04], np.float32)
+    heston = tqf.models.HestonModel(2.0, 0.04, 0.3, -0.7)
+    ft_drift, ft_vol = co.heston_full_truncation(0.02, 2.0, 0.04, 0.3, -0.7)
+    cases = {
+        "heston_qe": (2, lambda t: heston.sample_paths(t, x0h, num_time_steps=n_steps, **rnd)),
+        "heston_ft_euler": (2, lambda t: tqf.models.euler_sampling.sample(2, ft_drift, ft_vol, t, num_time_steps=n_steps,
+                                                                          initial_state=x0h, **rnd)),
+    }
+    for d in (1, 2, 3):
+        drift, vol = co.gbm(np.full(d, 0.05, np.float32), np.full(d, 0.2, np.float32),
+                            (0.5 * np.eye(d) + 0.5).astype(np.float32))
+        cases[f"gbm_euler_d{d}"] = (d, (lambda dr, vo, dd: lambda t: tqf.models.euler_sampling.sample(
+            dd, dr, vo, t, num_time_steps=n_steps, initial_state=np.full(dd, 100.0, np.float32), **rnd))(drift, vol, d))
+    gbm = tqf.models.GeometricBrownianMotion(0.05, 0.2, dtype=np.float32)
+    cases["gbm_exact"] = (1, lambda t: gbm.sample_paths(t, initial_state=100.0, **rnd))
+    res = {"config": f"{N} paths x {n_steps} steps, float32, every step recorded vs t = T only, Philox draws"}
+    for name, (d, fn) in cases.items():
+        t_all = timed(lambda: fn(times))
+        t_last = timed(lambda: fn(last))
+        gb = N * n_steps * d * 4 / 1e9
+        res[name] = {"all_steps_ms": t_all * 1e3, "last_only_ms": t_last * 1e3, "output_gb": gb,
+                     "write_gbs": gb / t_all}
+    return res
+
+
 def run_greeks(n_paths=N_PATHS, n_steps=N_STEPS, reps=5):
     """Pathwise adjoint Greeks on the headline workload: the 7 sensitivities
     (spot, variance, mean reversion, theta, vol of vol, rho, rate) of the sum
@@ -611,6 +666,8 @@ def main():
     ap.add_argument("--no-sobol", action="store_true")
     ap.add_argument("--no-lsm", action="store_true")
     ap.add_argument("--no-greeks", action="store_true")
+    ap.add_argument("--no-stored-paths", action="store_true")
+    ap.add_argument("--stored-paths-only", action="store_true", help="run only the stored-path measurement")
     ap.add_argument("--greeks-only", action="store_true", help="run only the adjoint-Greeks measurement")
     ap.add_argument("--lsm-only", action="store_true", help="run only the Longstaff-Schwartz measurement")
     ap.add_argument("--lsm-paths", type=int, default=1 << 20)
@@ -639,6 +696,9 @@ def main():
 
     if args.lsm_only:
         print(json.dumps({"lsm": run_lsm(n_paths=args.lsm_paths)}))
+        return
+    if args.stored_paths_only:
+        print(json.dumps({"stored_paths": run_stored_paths(n_paths=args.paths)}))
         return
     if args.greeks_only:
         print(json.dumps({"greeks": run_greeks(n_paths=args.paths)}))
@@ -676,6 +736,8 @@ def main():
         line["lsm"] = run_lsm(n_paths=args.lsm_paths)
     if rank == 0 and world == 1 and not args.no_greeks:
         line["greeks"] = run_greeks(n_paths=args.paths)
+    if rank == 0 and world == 1 and not args.no_stored_paths:
+        line["stored_paths"] = run_stored_paths(n_paths=args.paths)
     if rank == 0:
         line["cpu_baseline"] = cpu
         print(json.dumps(line))
