@@ -123,28 +123,38 @@ __device__ __forceinline__ float qe_erf<float>(float x) { return erff(x); }
 template <>
 __device__ __forceinline__ double qe_erf<double>(double x) { return erf(x); }
 
+// Division and square root of the QE step: in float32 the SFU square root
+// and the fast division (both within 2 ulp; the operands are moderate
+// positive numbers: m >= theta (1 - E) > 0, psi > 0, b2 >= 1), in float64
+// the IEEE operations.  log and erf stay the library functions (log(1 - p)
+// near 1 needs their accuracy).
+__device__ __forceinline__ float qe_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double qe_div(double a, double b) { return a / b; }
+__device__ __forceinline__ float qe_sqrt(float a) { return sqrt_approx(a); }
+__device__ __forceinline__ double qe_sqrt(double a) { return sqrt(a); }
+
 template <typename T>
 __device__ __forceinline__ void qe_step(const T* __restrict__ row, T zv, T zx, T& x, T& v) {
   if (row[0] != T(0)) return;  // dt <= tolerance: state kept, draws consumed
   const T theta = row[1], E = row[2], A = row[3], B = row[4];
   const T m = theta + (v - theta) * E;
   const T s2 = v * A + B;
-  const T psi = s2 / (m * m);
+  const T psi = qe_div(s2, m * m);
   T v_next;
   if (psi < T(1.5)) {
-    const T psi_inv = T(2) / psi;
-    const T b2 = psi_inv - T(1) + sqrt(psi_inv * (psi_inv - T(1)));
-    const T a = m / (T(1) + b2);
-    const T t = sqrt(b2) + zv;
+    const T psi_inv = qe_div(T(2), psi);
+    const T b2 = psi_inv - T(1) + qe_sqrt(psi_inv * (psi_inv - T(1)));
+    const T a = qe_div(m, T(1) + b2);
+    const T t = qe_sqrt(b2) + zv;
     v_next = a * (t * t);
   } else {
-    const T p = (psi - T(1)) / (psi + T(1));
-    const T beta = (T(1) - p) / m;
-    const T u = T(0.5) * (T(1) + qe_erf<T>(zv / T(1.41421356237309504880)));
-    v_next = u > p ? (log(T(1) - p) - log(T(1) - u)) / beta : T(0);
+    const T p = qe_div(psi - T(1), psi + T(1));
+    const T beta = qe_div(T(1) - p, m);
+    const T u = T(0.5) * (T(1) + qe_erf<T>(qe_div(zv, T(1.41421356237309504880))));
+    v_next = u > p ? qe_div(log(T(1) - p) - log(T(1) - u), beta) : T(0);
   }
   const T k0 = row[5], k1 = row[6], k2 = row[7], k3 = row[8], k4 = row[9];
-  x = x + k0 + k1 * v + k2 * v_next + sqrt(k3 * v + k4 * v_next) * zx;
+  x = x + k0 + k1 * v + k2 * v_next + qe_sqrt(k3 * v + k4 * v_next) * zx;
   v = v_next;
 }
 
@@ -329,11 +339,10 @@ __global__ void __launch_bounds__(kBlock)
 #pragma unroll 2
         for (; i + 1 < steps; i += 2) {
           const uint4 r = philox4x32_10(make_uint4((uint32_t)(i >> 1), plo, phi, 0u), k0, k1);
-          float z0, z1, z2, z3;
-          box_muller_f32(r.x, r.y, z0, z1);
-          box_muller_f32(r.z, r.w, z2, z3);
-          one_step(i, z0, z1);
-          one_step(i + 1, z2, z3);
+          float2 ze, zo;  // (z0, z2), (z1, z3): box_muller_f32 of (x, y) and (z, w)
+          box_muller_pair_f32(r, ze, zo);
+          one_step(i, ze.x, zo.x);
+          one_step(i + 1, ze.y, zo.y);
         }
         if (i < steps) {
           const uint4 r = philox4x32_10(make_uint4((uint32_t)(i >> 1), plo, phi, 0u), k0, k1);
