@@ -18,17 +18,62 @@ constexpr int kBlock = 256;
 // memory), chosen when a path's output row is at least 64 bytes; then every
 // thread runs every round and a thread past the last path simulates that path
 // again with its output dropped.
+// Per-step tables in shared memory (when they fit): transition constants
+// [steps][d][3], forward rates [steps + 1][d], Cholesky factors [steps][d][d]
+// (optional) and output slots [steps], each 16-byte aligned.
+template <typename T>
+struct HwTables {
+  size_t tab, f0, chol, slots, total;
+};
+template <typename T>
+__host__ __device__ inline HwTables<T> hw_tables(int steps, int d, bool chol) {
+  HwTables<T> t;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off = (off + bytes + 15) & ~(size_t)15;
+    return at;
+  };
+  t.tab = take((size_t)steps * d * 3 * sizeof(T));
+  t.f0 = take((size_t)(steps + 1) * d * sizeof(T));
+  t.chol = take(chol ? (size_t)steps * d * d * sizeof(T) : 0);
+  t.slots = take((size_t)steps * sizeof(int32_t));
+  t.total = off;
+  return t;
+}
+constexpr size_t kHwMaxSmemTables = 64 * 1024;
+
 template <typename T, int DM, bool STAGE>
-__global__ void __launch_bounds__(kBlock) hull_white_kernel(tqf_hull_white_args a) {
+__global__ void __launch_bounds__(kBlock) hull_white_kernel(tqf_hull_white_args a, int tables_in_smem) {
   extern __shared__ __align__(16) unsigned char stage_smem[];
   const int d = a.dim;
   const T* tab = static_cast<const T*>(a.table);
   const T* f0 = static_cast<const T*>(a.f0);
   const T* L = static_cast<const T*>(a.chol);
+  const int32_t* slots = a.slots;
+  size_t stage_off = 0;
+  if (tables_in_smem) {
+    const HwTables<T> lay = hw_tables<T>(a.num_steps, d, L != nullptr);
+    T* s_tab = reinterpret_cast<T*>(stage_smem + lay.tab);
+    T* s_f0 = reinterpret_cast<T*>(stage_smem + lay.f0);
+    T* s_chol = reinterpret_cast<T*>(stage_smem + lay.chol);
+    int32_t* s_slots = reinterpret_cast<int32_t*>(stage_smem + lay.slots);
+    for (int i = threadIdx.x; i < a.num_steps * d * 3; i += kBlock) s_tab[i] = tab[i];
+    for (int i = threadIdx.x; i < (a.num_steps + 1) * d; i += kBlock) s_f0[i] = f0[i];
+    if (L)
+      for (int i = threadIdx.x; i < a.num_steps * d * d; i += kBlock) s_chol[i] = L[i];
+    for (int i = threadIdx.x; i < a.num_steps; i += kBlock) s_slots[i] = slots[i];
+    __syncthreads();
+    tab = s_tab;
+    f0 = s_f0;
+    if (L) L = s_chol;
+    slots = s_slots;
+    stage_off = lay.total;
+  }
   T* out = static_cast<T*>(a.output.ptr);
   const int ns = a.output.num_slots;
   const int64_t N = a.num_paths;
-  RowStager<T, DM, kBlock> stg(stage_smem, d);
+  RowStager<T, DM, kBlock> stg(stage_smem + stage_off, d);
   const int64_t per_round = (int64_t)gridDim.x * kBlock;
   for (int64_t base = 0; base < N; base += per_round) {
     const int64_t row0 = base + (int64_t)blockIdx.x * kBlock;
@@ -72,7 +117,7 @@ __global__ void __launch_bounds__(kBlock) hull_white_kernel(tqf_hull_white_args 
 #pragma unroll
       for (int k = 0; k < DM; ++k)
         if (k < d) x[k] = row[3 * k] * x[k] + row[3 * k + 1] + row[3 * k + 2] * y[k];
-      const int slot = a.slots[i];
+      const int slot = slots[i];
       if (slot >= 0) {
         const T* f = f0 + (size_t)(i + 1) * d;
         if constexpr (STAGE) {
@@ -97,14 +142,16 @@ int launch(const tqf_hull_white_args& a, cudaStream_t s) {
   // stage the output when a path's row is at least 64 bytes
   const bool stage = (size_t)a.output.num_slots * a.dim * sizeof(T) >= 64;
   auto k = stage ? hull_white_kernel<T, DM, true> : hull_white_kernel<T, DM, false>;
-  const size_t smem = stage ? RowStager<T, DM, kBlock>::kBytes : 0;
+  const size_t tables = hw_tables<T>(a.num_steps, a.dim, a.chol != nullptr).total;
+  const bool tables_in_smem = tables <= kHwMaxSmemTables;
+  const size_t smem = (tables_in_smem ? tables : 0) + (stage ? RowStager<T, DM, kBlock>::kBytes : 0);
   if (smem > 48 * 1024) set_smem_config(k, smem);
   int occ = 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem) != cudaSuccess || occ < 1) occ = 1;
   int64_t grid = (a.num_paths + kBlock - 1) / kBlock;
   const int64_t cap = (int64_t)num_sms() * occ;
   if (grid > cap) grid = cap;
-  k<<<(unsigned)grid, kBlock, smem, s>>>(a);
+  k<<<(unsigned)grid, kBlock, smem, s>>>(a, tables_in_smem ? 1 : 0);
   return check_launch("hull_white_kernel");
 }
 
