@@ -107,16 +107,6 @@ __device__ __forceinline__ uint32_t dsilu_bf16x2(uint32_t x2) {
   return bf2_mul(sg, bf2_fma(x2, om, kBf2One));
 }
 
-// Programmatic dependent launch: a kernel launched with programmatic stream
-// serialization may start before the previous kernel in the stream has
-// finished; grid_dependency_wait() blocks until that kernel has completed and
-// its memory is visible (a no-op for an ordinary launch), and
-// allow_dependent_launch() lets the next such kernel start launching.
-__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void allow_dependent_launch() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
 // Warpgroup barrier (named barrier 1 or 2, 128 threads).  Immediate barrier
 // ids keep the kernel's barrier count at 3; a register id would reserve all
 // 16 and make the occupancy calculator allow one CTA per SM.

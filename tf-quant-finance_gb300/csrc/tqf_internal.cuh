@@ -36,6 +36,32 @@ inline void set_smem_config(K kernel, size_t smem) {
   cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start before the previous kernel in the stream has
+// finished; grid_dependency_wait() blocks until that kernel has completed and
+// its memory is visible (a no-op for an ordinary launch), and
+// allow_dependent_launch() lets the next such kernel start launching.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void allow_dependent_launch() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launch configuration of a programmatic dependent launch on `stream`
+// (attr is filled in and must outlive the launch call).
+inline cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                                     cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg = {};
+  attr->id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr->val.programmaticStreamSerializationAllowed = 1;
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------
 // Ten rounds of the published round function; the key is bumped by the
 // Weyl constants between rounds.

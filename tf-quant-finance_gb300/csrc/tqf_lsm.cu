@@ -214,6 +214,8 @@ static_assert(sizeof(Acc<float>::S) == 8 && sizeof(Acc<double>::S) == 8, "8-byte
 template <typename T>
 __global__ void __launch_bounds__(1024)
     lsm_reduce_kernel(const typename Acc<T>::S* __restrict__ part, int rows, int width, double* __restrict__ out) {
+  grid_dependency_wait();  // a programmatic dependent launch in the exercise-date chain
+  allow_dependent_launch();
   using A = Acc<T>;
   __shared__ typename A::S s[32][33];
   const int c = threadIdx.x % 32, r = threadIdx.x / 32;
@@ -379,6 +381,8 @@ struct LsmCtx {
 template <typename T, int DM, int GR>
 __global__ void lsm_pass_kernel(tqf_lsm_args a, const T* __restrict__ xt, void* __restrict__ partials_raw,
                                 const double* __restrict__ beta, const double* __restrict__ means, int C) {
+  grid_dependency_wait();  // a programmatic dependent launch in the exercise-date chain
+  allow_dependent_launch();
   using A = Acc<T>;
   using S = typename A::S;
   constexpr int GN = GR > 0 ? GR : 1;                    // compile-time basis size (register mode)
@@ -628,6 +632,7 @@ __host__ inline void* pass_kernel_for(int d, int G) {
 }
 
 __global__ void lsm_scale_kernel(double* __restrict__ v, int n, double s) {
+  grid_dependency_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) v[i] *= s;
 }
@@ -670,6 +675,8 @@ template <int GC>
 __global__ void __launch_bounds__(kSolveThreads)
     lsm_solve_kernel(const double* __restrict__ sums, int Gr, double rcond, double* __restrict__ beta,
                      double* __restrict__ Vg, int warm) {
+  grid_dependency_wait();  // a programmatic dependent launch in the exercise-date chain
+  allow_dependent_launch();
   extern __shared__ __align__(16) unsigned char smem[];
   const int G = GC > 0 ? GC : Gr;  // compile-time size for small systems (constant index arithmetic)
   const int P = G + 1;  // row stride of A
@@ -877,18 +884,22 @@ int launch_pass(const tqf_lsm_args& a, cudaStream_t s) {
   void* k = pass_kernel_for<T>(d, G);
   void* params[] = {const_cast<tqf_lsm_args*>(&a), const_cast<T**>(&xt), &partials, const_cast<double**>(&beta),
                     const_cast<double**>(&means), &C};
-  int rc = check_cuda(cudaLaunchKernel(k, grid, dim3((unsigned)C), params, smem, s), "lsm_pass_kernel launch");
+  // The date loop's kernels are programmatic dependent launches: each starts
+  // launching while its predecessor finishes and waits (griddepcontrol.wait,
+  // at its top) before it reads anything.
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = pdl_config(grid, dim3((unsigned)C), smem, s, attr);
+  int rc = check_cuda(cudaLaunchKernelExC(&cfg, k, params), "lsm_pass_kernel launch");
   if (rc) return rc;
   rc = check_launch("lsm_pass_kernel");
   if (rc) return rc;
-  if (a.final_pass) {
-    lsm_reduce_kernel<T><<<(a.batch + 31) / 32, 1024, 0, s>>>(partials, gx, a.batch, a.out);
-    return check_launch("lsm_reduce_kernel");
-  }
-  if (a.acc_index >= 1) {
-    const int width = a.batch * lsm_entries(G);
-    lsm_reduce_kernel<T><<<(width + 31) / 32, 1024, 0, s>>>(partials, gx, width,
-                                                            reinterpret_cast<double*>(ws + L.sums));
+  const int width = a.final_pass ? a.batch : a.batch * lsm_entries(G);
+  if (a.final_pass || a.acc_index >= 1) {
+    double* out = a.final_pass ? a.out : reinterpret_cast<double*>(ws + L.sums);
+    cudaLaunchConfig_t rcfg = pdl_config(dim3((unsigned)((width + 31) / 32)), dim3(1024), 0, s, attr);
+    rc = check_cuda(cudaLaunchKernelEx(&rcfg, lsm_reduce_kernel<T>, static_cast<const S*>(partials), gx, width, out),
+                    "lsm_reduce_kernel launch");
+    if (rc) return rc;
     return check_launch("lsm_reduce_kernel");
   }
   return TQF_OK;
@@ -939,9 +950,13 @@ int launch_solve(const tqf_lsm_args& a, cudaStream_t s) {
     default: break;
   }
   set_smem_config(k, smem);
-  k<<<a.batch, G <= 16 ? 32 : kSolveThreads, smem, s>>>(reinterpret_cast<const double*>(ws + L.sums), G, rcond,
-                                                        reinterpret_cast<double*>(ws + L.beta),
-                                                        reinterpret_cast<double*>(ws + L.eig_v), warm);
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = pdl_config(dim3((unsigned)a.batch), dim3(G <= 16 ? 32 : kSolveThreads), smem, s, attr);
+  const int rc = check_cuda(cudaLaunchKernelEx(&cfg, k, reinterpret_cast<const double*>(ws + L.sums), G, rcond,
+                                               reinterpret_cast<double*>(ws + L.beta),
+                                               reinterpret_cast<double*>(ws + L.eig_v), warm),
+                            "lsm_solve_kernel launch");
+  if (rc) return rc;
   return check_launch("lsm_solve_kernel");
 }
 
@@ -1027,6 +1042,10 @@ extern "C" int tqf_lsm_price(const tqf_lsm_args* args, void* stream) {
   if (rc) return rc;
   const int64_t count = a.num_calibration > 0 ? a.num_paths - a.num_calibration : a.num_paths;
   TQF_REQUIRE(count >= 1, "tqf_lsm_price: no paths left to price after calibration");
-  lsm_scale_kernel<<<(a.batch + 255) / 256, 256, 0, s>>>(a.out, a.batch, 1.0 / (double)count);
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = pdl_config(dim3((unsigned)((a.batch + 255) / 256)), dim3(256), 0, s, attr);
+  rc = check_cuda(cudaLaunchKernelEx(&cfg, lsm_scale_kernel, a.out, a.batch, 1.0 / (double)count),
+                  "lsm_scale_kernel launch");
+  if (rc) return rc;
   return check_launch("lsm_scale_kernel");
 }
