@@ -452,8 +452,10 @@ __global__ void __launch_bounds__(kBlock) heston_adjoint_kernel(tqf_heston_adjoi
         const T theta = (T)a.theta, A = row.xirho, B = row.xisq;
         const T z0 = src.get(i, 0), z1 = src.get(i, 1);
         const T vp = v > T(0) ? v : T(0);
-        const T sq = sqrt(vp);
-        const T dsq = sq > T(0) ? T(0.5) / sq : T(0);
+        // the forward step's square root (sqrt_approx, shared with ft_step
+        // below) and its derivative 1 / (2 sqrt(v+))
+        const T sq = sqrt_approx(vp);
+        const T dsq = sq > T(0) ? qe_div(T(0.5), sq) : T(0);
         const T dw0 = z0 * sdt, dw1 = z1 * sdt;
         adj_param_step<0, T>(dt, dw0, dw1, vp, sq, dsq, kappa, theta, A, B, rho, xi, sr, xd[0], vd[0]);
         adj_param_step<1, T>(dt, dw0, dw1, vp, sq, dsq, kappa, theta, A, B, rho, xi, sr, xd[1], vd[1]);
