@@ -30,6 +30,28 @@ def test_adjoint_matches_autograd_restatement_on_same_draws(cuda):
     np.testing.assert_allclose(grad, g_ref, rtol=1e-7, atol=1e-9)
 
 
+def test_float32_adjoint_matches_float64_restatement(cuda):
+    """The float32 replay (SFU square roots, float32 tangents) against the
+    float64 autograd restatement on the same float32-rounded draws: within
+    2e-3 relative (float32 path arithmetic over 32 steps, and the odd path
+    whose payoff indicator flips at a strike)."""
+    from tqf.math.random import RandomType
+    from tqf.models import utils
+    from tqf.pricing import heston_european_mc, heston_european_vjp
+    N, steps = 20000, 32
+    strikes = np.array([80.0, 95.0, 100.0, 110.0, 130.0])
+    w = np.array([0.3, -1.0, 2.0, 0.5, 1.0])
+    draws = utils.generate_mc_normal_draws(2, steps, N, RandomType.STATELESS, seed=[2, 3],
+                                           dtype=torch.float32).permute(1, 0, 2).contiguous()
+    kw = dict(strikes=strikes, expiry=1.0, num_samples=N, num_time_steps=steps, dtype=torch.float32,
+              normal_draws=draws, **PARAMS)
+    res = heston_european_mc(**kw)
+    grad = heston_european_vjp(w, prices=res.price, **kw).cpu().numpy()
+    _, g_ref = heston_grad.price_and_grad([PARAMS[k] for k in ORDER], strikes, w, 1.0,
+                                          draws.cpu().numpy().astype(np.float64))
+    np.testing.assert_allclose(grad, g_ref, rtol=2e-3, atol=1e-4 * float(np.abs(g_ref).max()))
+
+
 @pytest.mark.parametrize("volvol,tol_rel", [(0.1, 1e-4), (0.3, 2e-2)])
 def test_adjoint_vs_common_random_number_bumps(cuda, volvol, tol_rel):
     """Pathwise Greeks vs central bump-and-revalue on the same Philox paths.

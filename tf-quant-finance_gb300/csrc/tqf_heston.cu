@@ -414,6 +414,41 @@ __device__ __forceinline__ void adj_param_step(T dt, T dw0, T dw1, T vp, T sq, T
   vd = vdn;
 }
 
+// The same tangent step for parameters P and Q at once, as the two lanes of
+// f32x2 pairs (float32 replay: tangents carried as pairs (0, 1), (2, 3),
+// (4, 5)).  The broadcast pairs hold one step's values in both lanes; the
+// parameter-specific terms enter as lane constants (0 in a lane without one).
+template <int P>
+__device__ __forceinline__ void adj_vol_terms(float rho, float xi, float sr, float& Ad, float& Bd) {
+  Ad = P == 4 ? rho : (P == 5 ? xi : 0.f);
+  Bd = P == 4 ? sr : (P == 5 ? -xi * rho / sr : 0.f);
+}
+template <int P, int Q>
+__device__ __forceinline__ void adj_pair_step(float2 dtb, float2 dw0b, float2 dw1b, float vp, float sq, float2 dsqb,
+                                              float2 nkb, float kappa, float theta, float2 Ab, float2 Bb,
+                                              float rho, float xi, float sr, float2& xd, float2& vd) {
+  const float m = vp > 0.f ? 1.f : 0.f;
+  const float2 vpd = mul2(vd, make_float2(m, m));
+  const float2 sqd = mul2(dsqb, vpd);
+  float2 xdn = fma2(dtb, mul2(make_float2(-0.5f, -0.5f), vpd), xd);
+  xdn = fma2(sqd, dw0b, xdn);
+  if (P == 6 || Q == 6) xdn = add2(xdn, make_float2(P == 6 ? dtb.x : 0.f, Q == 6 ? dtb.x : 0.f));
+  float2 vdn = fma2(dtb, mul2(nkb, vpd), vd);
+  if (P == 2 || Q == 2 || P == 3 || Q == 3) {
+    auto c = [&](int r) { return r == 2 ? dtb.x * (theta - vp) : (r == 3 ? dtb.x * kappa : 0.f); };
+    vdn = add2(vdn, make_float2(c(P), c(Q)));
+  }
+  float AdP, BdP, AdQ, BdQ;
+  adj_vol_terms<P>(rho, xi, sr, AdP, BdP);
+  adj_vol_terms<Q>(rho, xi, sr, AdQ, BdQ);
+  const float2 e0 = fma2(Ab, sqd, make_float2(AdP * sq, AdQ * sq));
+  const float2 e1 = fma2(Bb, sqd, make_float2(BdP * sq, BdQ * sq));
+  vdn = fma2(e0, dw0b, vdn);
+  vdn = fma2(e1, dw1b, vdn);
+  xd = xdn;
+  vd = vdn;
+}
+
 template <typename T, int SRC>
 __global__ void __launch_bounds__(kBlock) heston_adjoint_kernel(tqf_heston_adjoint_args a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -437,7 +472,44 @@ __global__ void __launch_bounds__(kBlock) heston_adjoint_kernel(tqf_heston_adjoi
     T q[kAdjParams];
 #pragma unroll
     for (int p = 0; p < kAdjParams; ++p) q[p] = T(0);
-    if (path < a.num_paths) {
+    if (path < a.num_paths && sizeof(T) == 4) {
+      if constexpr (sizeof(T) == 4) {
+        // float32: tangents of (log S0, v0), (kappa, theta), (xi, rho) in
+        // f32x2 pairs, the rate's alone
+        float x = (float)a.x0, v = (float)a.v0;
+        float2 xd01 = make_float2(1.f, 0.f), vd01 = make_float2(0.f, 1.f);
+        float2 xd23 = make_float2(0.f, 0.f), vd23 = xd23, xd45 = xd23, vd45 = xd23;
+        float xd6 = 0.f, vd6 = 0.f;
+        DrawSource<float> src(a.draws, path, 2);
+        const float kappa = (float)a.kappa, theta = (float)a.theta;
+        const float2 nkb = make_float2(-kappa, -kappa);
+        for (int i = 0; i < a.num_steps; ++i) {
+          const FtRow<float> row = load_ft_row<float>(table + (size_t)i * kFtCols);
+          const float dt = 2.f * row.hdt, sdt = row.sdt, A = row.xirho, B = row.xisq;
+          const float z0 = src.get(i, 0), z1 = src.get(i, 1);
+          const float vp = v > 0.f ? v : 0.f;
+          const float sq = sqrt_approx(vp);  // shared with ft_step below
+          const float dsq = sq > 0.f ? qe_div(0.5f, sq) : 0.f;
+          const float dw0 = z0 * sdt, dw1 = z1 * sdt;
+          const float2 dtb = make_float2(dt, dt), dw0b = make_float2(dw0, dw0), dw1b = make_float2(dw1, dw1);
+          const float2 dsqb = make_float2(dsq, dsq), Ab = make_float2(A, A), Bb = make_float2(B, B);
+          adj_pair_step<0, 1>(dtb, dw0b, dw1b, vp, sq, dsqb, nkb, kappa, theta, Ab, Bb, rho, xi, sr, xd01, vd01);
+          adj_pair_step<2, 3>(dtb, dw0b, dw1b, vp, sq, dsqb, nkb, kappa, theta, Ab, Bb, rho, xi, sr, xd23, vd23);
+          adj_pair_step<4, 5>(dtb, dw0b, dw1b, vp, sq, dsqb, nkb, kappa, theta, Ab, Bb, rho, xi, sr, xd45, vd45);
+          adj_param_step<6, float>(dt, dw0, dw1, vp, sq, dsq, kappa, theta, A, B, rho, xi, sr, xd6, vd6);
+          ft_step<float>(row, z0, z1, x, v);
+        }
+        const float S = exp(x);
+        float c = 0.f;
+        for (int j = 0; j < a.num_strikes; ++j) {
+          const bool call = s_call[j] != 0;
+          if (call ? (S > s_strike[j]) : (S < s_strike[j])) c += call ? s_w[j] : -s_w[j];
+        }
+        const float xdv[kAdjParams] = {xd01.x, xd01.y, xd23.x, xd23.y, xd45.x, xd45.y, xd6};
+#pragma unroll
+        for (int p = 0; p < kAdjParams; ++p) q[p] = c * S * xdv[p];
+      }
+    } else if (path < a.num_paths) {
       T x = (T)a.x0, v = (T)a.v0;
       T xd[kAdjParams], vd[kAdjParams];
 #pragma unroll
