@@ -52,6 +52,12 @@ def _run(spots, vols, rate, corr, weights, strike, expiry, num_time_steps, num_s
     if normal_draws is not None:
         keep.append(normal_draws)
         draws = mvn.memory_draws(normal_draws, path_axis=0, step_axis=1)
+    elif random_type in (RandomType.SOBOL, RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
+        # quasi-random: [steps, N, d] normal draws (dimension step * d + asset,
+        # points path_offset + 1 ...), read in place by the kernel
+        q = utils.generate_mc_normal_draws(d, steps, N, random_type, skip=int(path_offset), seed=seed, dtype=td)
+        keep.append(q)
+        draws = mvn.memory_draws(q, path_axis=1, step_axis=0)
     else:
         draws = mvn.philox_draws(random_type, seed, N, path_offset)
     out = torch.zeros(2 + 2 * d, dtype=torch.float64, device=device)

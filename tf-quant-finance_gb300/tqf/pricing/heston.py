@@ -33,6 +33,24 @@ def _table(key, build, td, device):
     return t
 
 
+_QUASI = (RandomType.SOBOL, RandomType.HALTON, RandomType.HALTON_RANDOMIZED)
+
+
+def _draws(random_type, seed, num_paths, num_steps, path_offset, normal_draws, td):
+    """(tqf_draws, tensor to keep alive): caller draws [N, steps, 2] read in
+    place; SOBOL / HALTON* as [steps, N, 2] normal draws generated on the
+    device (dimension step * 2 + component, points path_offset + 1 ... as in
+    generate_mc_normal_draws with skip = path_offset); otherwise the Philox
+    stream generated inside the kernel."""
+    if normal_draws is not None:
+        return mvn.memory_draws(normal_draws, path_axis=0, step_axis=1), normal_draws
+    if random_type in _QUASI:
+        q = utils.generate_mc_normal_draws(2, num_steps, num_paths, random_type, skip=int(path_offset), seed=seed,
+                                           dtype=td)
+        return mvn.memory_draws(q, path_axis=1, step_axis=0), q
+    return mvn.philox_draws(random_type, seed, num_paths, path_offset), None
+
+
 def heston_european_mc(*, strikes, expiry, spot, variance, mean_reversion, theta, volvol, rho,
                        discount_rate=0.0, is_call_options=None, num_samples, num_time_steps,
                        scheme="full_truncation", random_type=RandomType.STATELESS, seed=(1, 2),
@@ -74,10 +92,7 @@ def heston_european_mc(*, strikes, expiry, spot, variance, mean_reversion, theta
 
         tab = _table(key, build, td, device)
         x0, scale = float(np.log(spot)), 1.0
-    if normal_draws is not None:
-        draws = mvn.memory_draws(normal_draws, path_axis=0, step_axis=1)
-    else:
-        draws = mvn.philox_draws(random_type, seed, N, path_offset)
+    draws, draws_keep = _draws(random_type, seed, N, steps, path_offset, normal_draws, td)
     qe_flag = 1 if qe else 0
     p, out, keep = make_payoff(strikes, is_call_options, td, device, N,
                                lambda ns: _lib.load().tqf_heston_workspace_bytes(_lib.dtype_code(td), qe_flag, N, ns),
@@ -93,7 +108,7 @@ def heston_european_mc(*, strikes, expiry, spot, variance, mean_reversion, theta
     args.payoff = p
     args.dev_status = _lib.status_buffer(device).data_ptr()
     _lib.call("tqf_heston_qe" if qe else "tqf_heston_euler", args, _lib.stream_ptr(device))
-    del keep
+    del keep, draws_keep
     return stats_from_sums(out, N, float(np.exp(-r * T)))
 
 
@@ -127,10 +142,7 @@ def heston_european_vjp(grad_prices, *, strikes, expiry, spot, variance, mean_re
     calls = None
     if is_call_options is not None:
         calls = torch.as_tensor(np.broadcast_to(np.asarray(is_call_options, np.uint8), (ns,)).copy()).to(device)
-    if normal_draws is not None:
-        draws = mvn.memory_draws(normal_draws, path_axis=0, step_axis=1)
-    else:
-        draws = mvn.philox_draws(random_type, seed, N, path_offset)
+    draws, draws_keep = _draws(random_type, seed, N, steps, path_offset, normal_draws, td)
     out = torch.zeros(7, dtype=torch.float64, device=device)
     from tqf.pricing.european import workspace
     ws = workspace(int(_lib.load().tqf_heston_adjoint_workspace_bytes(N)), device, "heston_adjoint")
@@ -152,6 +164,7 @@ def heston_european_vjp(grad_prices, *, strikes, expiry, spot, variance, mean_re
     a.workspace_bytes = ws.numel()
     a.dev_status = _lib.status_buffer(device).data_ptr()
     _lib.call("tqf_heston_euler_adjoint", a, _lib.stream_ptr(device))
+    del draws_keep
     grad = out.clone()
     grad[0] = out[0] / float(spot)  # d/dS0 = (1/S0) d/dlog S0
     if prices is not None:
