@@ -604,6 +604,36 @@ def run_stored_paths(n_paths=N_PATHS, n_steps=N_STEPS, reps=5):
     return res
 
 
+def run_heston_sobol(n_paths=N_PATHS, n_steps=N_STEPS, reps=5):
+    """The Heston pricing workload with Sobol draws (the quasi-random variant
+    of the headline config: dimension 2 x 252 = 504, points 1 .. 2^22): the
+    draws are generated on the device ([252, 2^22, 2] float32, 8.5 GB) and
+    read in place by the fused kernel.  Median of `reps` calls through the
+    public API, CUDA events, draw generation included."""
+    import torch
+    from tqf.math.random import RandomType
+    from tqf.pricing import heston_european_mc
+    kw = dict(strikes=strikes(), expiry=1.0, spot=100.0, variance=0.04, mean_reversion=2.0, theta=0.04, volvol=0.3,
+              rho=-0.7, discount_rate=0.02, num_samples=n_paths, num_time_steps=n_steps,
+              random_type=RandomType.SOBOL)
+    res = heston_european_mc(**kw)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        res = heston_european_mc(**kw)
+        e1.record()
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    sec = sorted(ts)[len(ts) // 2]
+    k = strikes()
+    j = int(np.argmin(np.abs(k - 100.0)))
+    return {"config": f"Heston FT-Euler FP32, {n_paths} paths x {n_steps} steps, 64 strikes, Sobol dim {2 * n_steps}",
+            "seconds": sec, "path_steps_per_s": n_paths * n_steps / sec, "draw_bytes": n_paths * n_steps * 2 * 4,
+            "atm_call_price": float(res.price[j]), "strike": float(k[j])}
+
+
 def run_greeks(n_paths=N_PATHS, n_steps=N_STEPS, reps=5):
     """Pathwise adjoint Greeks on the headline workload: the 7 sensitivities
     (spot, variance, mean reversion, theta, vol of vol, rho, rate) of the sum
@@ -666,6 +696,7 @@ def main():
     ap.add_argument("--no-sobol", action="store_true")
     ap.add_argument("--no-lsm", action="store_true")
     ap.add_argument("--no-greeks", action="store_true")
+    ap.add_argument("--no-heston-sobol", action="store_true")
     ap.add_argument("--no-stored-paths", action="store_true")
     ap.add_argument("--stored-paths-only", action="store_true", help="run only the stored-path measurement")
     ap.add_argument("--greeks-only", action="store_true", help="run only the adjoint-Greeks measurement")
@@ -736,6 +767,8 @@ def main():
         line["lsm"] = run_lsm(n_paths=args.lsm_paths)
     if rank == 0 and world == 1 and not args.no_greeks:
         line["greeks"] = run_greeks(n_paths=args.paths)
+    if rank == 0 and world == 1 and not args.no_heston_sobol:
+        line["heston_sobol"] = run_heston_sobol(n_paths=args.paths)
     if rank == 0 and world == 1 and not args.no_stored_paths:
         line["stored_paths"] = run_stored_paths(n_paths=args.paths)
     if rank == 0:
