@@ -1041,16 +1041,8 @@ extern "C" int tqf_mlp_train_step(const tqf_mlp_train_args* a, void* stream) {
   const int grid = a->batch_paths / a->paths_per_cta;
   const size_t smem = train_smem_bytes();
   set_smem_config(mlp_train_step_kernel, smem);
-  cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(kTrainThreads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = static_cast<cudaStream_t>(stream);
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cudaLaunchConfig_t cfg = pdl_config(dim3(grid), dim3(kTrainThreads), smem, static_cast<cudaStream_t>(stream), attr);
   cudaError_t e = cudaLaunchKernelEx(&cfg, mlp_train_step_kernel, *a);
   if (e != cudaSuccess) return check_cuda(e, "mlp_train_step_kernel");
   return check_launch("mlp_train_step_kernel");
@@ -1061,16 +1053,9 @@ extern "C" int tqf_mlp_adam(const tqf_mlp_adam_args* a, void* stream) {
   TQF_REQUIRE(a && a->params && a->m && a->v && a->grad_partials && a->w1_bf16 && a->w2_bf16,
               "tqf_mlp_adam: null pointer");
   TQF_REQUIRE(a->num_partials >= 1, "tqf_mlp_adam: num_partials must be >= 1");
-  cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.gridDim = dim3((kNumParams + 1 + 31) / 32);
-  cfg.blockDim = dim3(32 * kAdamSlices);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = static_cast<cudaStream_t>(stream);
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cudaLaunchConfig_t cfg = pdl_config(dim3((kNumParams + 1 + 31) / 32), dim3(32 * kAdamSlices), 0,
+                                      static_cast<cudaStream_t>(stream), attr);
   cudaError_t e = cudaLaunchKernelEx(&cfg, mlp_adam_kernel, *a);
   if (e != cudaSuccess) return check_cuda(e, "mlp_adam_kernel");
   return check_launch("mlp_adam_kernel");
