@@ -634,6 +634,64 @@ def run_heston_sobol(n_paths=N_PATHS, n_steps=N_STEPS, reps=5):
             "atm_call_price": float(res.price[j]), "strike": float(k[j])}
 
 
+def run_euler_call_f64(reps=5):
+    """The workload of the reference's only published timing for this path: a
+    European call under Black-Scholes by the Euler scheme through
+    GenericItoProcess.sample_paths, float64, 200,000 paths (PSEUDO_ANTITHETIC)
+    x 100 steps to T = 1, priced at 3 strikes (synthetic parameters: S0 = 700,
+    sigma = 0.25, r = 0.01, strikes 600 / 650 / 680).  Timed through the
+    public API with CUDA events, sampling plus payoff reduction: once with the
+    drift and volatility as plain Python callables (one step kernel per time
+    step, the callables evaluated by torch), once with the structured GBM
+    coefficients (one fused kernel for the whole loop)."""
+    import torch
+    from tqf.math.random import RandomType
+    from tqf.models import GenericItoProcess, coefficients
+    from tqf.pricing import european_payoff_stats
+    s0, sigma, r, n = 700.0, 0.25, 0.01, 200_000
+    k = np.array([600.0, 650.0, 680.0])
+
+    def price(drift, vol):
+        proc = GenericItoProcess(1, drift, vol, dtype=np.float64)
+        paths = proc.sample_paths([1.0], num_samples=n, initial_state=np.array([s0]), time_step=0.01,
+                                  random_type=RandomType.PSEUDO_ANTITHETIC, seed=42)
+        return european_payoff_stats(paths[:, -1, 0], k, discount=float(np.exp(-r)))
+
+    callables = (lambda t, x: r * x, lambda t, x: (sigma * x)[..., None])
+    structured = coefficients.gbm([r], [sigma])
+    out = {"config": "GBM Euler f64, 200000 paths (antithetic) x 100 steps, 3 strikes; sample_paths + payoff"}
+    for name, (drift, vol) in (("callables", callables), ("structured", structured)):
+        res = price(drift, vol)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            res = price(drift, vol)
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        sec = sorted(ts)[len(ts) // 2]
+        out[name] = {"seconds": sec, "path_steps_per_s": n * 100 / sec,
+                     "prices": [float(x) for x in res.price.cpu()]}
+    bs = [float(closed_form_bs(s0, kk, r, sigma, 1.0)) for kk in k]
+    out["black_scholes"] = bs
+    # the reference's published wall times for this workload (TensorFlow on a
+    # Colab CPU, core count not stated): graph mode and with XLA
+    out["published_tf_cpu_seconds"] = {"graph": 2.162, "xla": 0.715}
+    for name in ("callables", "structured"):
+        out[name]["speedup_vs_published_tf_cpu"] = {m: t / out[name]["seconds"]
+                                                    for m, t in out["published_tf_cpu_seconds"].items()}
+    return out
+
+
+def closed_form_bs(s, k, r, v, t):
+    from math import erf, exp, log, sqrt
+    d1 = (log(s / k) + (r + 0.5 * v * v) * t) / (v * sqrt(t))
+    n = lambda x: 0.5 * (1.0 + erf(x / sqrt(2.0)))  # noqa: E731
+    return s * n(d1) - k * exp(-r * t) * n(d1 - v * sqrt(t))
+
+
 def run_greeks(n_paths=N_PATHS, n_steps=N_STEPS, reps=5):
     """Pathwise adjoint Greeks on the headline workload: the 7 sensitivities
     (spot, variance, mean reversion, theta, vol of vol, rho, rate) of the sum
@@ -697,6 +755,8 @@ def main():
     ap.add_argument("--no-lsm", action="store_true")
     ap.add_argument("--no-greeks", action="store_true")
     ap.add_argument("--no-heston-sobol", action="store_true")
+    ap.add_argument("--no-euler-call", action="store_true")
+    ap.add_argument("--euler-call-only", action="store_true", help="run only the float64 Euler call measurement")
     ap.add_argument("--no-stored-paths", action="store_true")
     ap.add_argument("--stored-paths-only", action="store_true", help="run only the stored-path measurement")
     ap.add_argument("--greeks-only", action="store_true", help="run only the adjoint-Greeks measurement")
@@ -727,6 +787,9 @@ def main():
 
     if args.lsm_only:
         print(json.dumps({"lsm": run_lsm(n_paths=args.lsm_paths)}))
+        return
+    if args.euler_call_only:
+        print(json.dumps({"euler_call_f64": run_euler_call_f64()}))
         return
     if args.stored_paths_only:
         print(json.dumps({"stored_paths": run_stored_paths(n_paths=args.paths)}))
@@ -769,6 +832,8 @@ def main():
         line["greeks"] = run_greeks(n_paths=args.paths)
     if rank == 0 and world == 1 and not args.no_heston_sobol:
         line["heston_sobol"] = run_heston_sobol(n_paths=args.paths)
+    if rank == 0 and world == 1 and not args.no_euler_call:
+        line["euler_call_f64"] = run_euler_call_f64()
     if rank == 0 and world == 1 and not args.no_stored_paths:
         line["stored_paths"] = run_stored_paths(n_paths=args.paths)
     if rank == 0:
