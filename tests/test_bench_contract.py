@@ -1,6 +1,6 @@
 """bench.py output contract on the CPU: the reference arm's JSON line (the
-oracle's NumPy sampler on the host cores) carries the keys the benchmark
-driver reads."""
+oracle's NumPy sampler on the host cores) carries every field of the
+benchmark line: metric, value, unit, steps, config, e2e and cpu_baseline."""
 
 import json
 import os
