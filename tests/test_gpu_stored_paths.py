@@ -3,8 +3,8 @@ given identical draws (GPU).
 
 The path kernels stage recorded states in shared memory and write them out
 as whole pieces of each path's output row once a path's row is long enough
-(Heston: always; Euler, GBM, Milstein, Hull-White: at least 64 bytes per
-path).  These cases record many times so that every stager runs several full
+(Heston: always; Euler, GBM, Milstein, Hull-White, Gaussian HJM: at least
+64 bytes per path).  These cases record many times so that every stager runs several full
 flushes and a partial one, with path counts that leave the last CTA round
 partly empty, and compare every stored state with the oracle.  Tolerances are
 those of the other path tests: 1e-5 relative in float32 and 1e-12 in float64.
@@ -17,6 +17,7 @@ import torch
 from oracle import euler as oeuler
 from oracle import grids as ogrids
 from oracle import heston as oheston
+from oracle import hjm as ohjm
 from oracle import hull_white as ohw
 from oracle import milstein as omil
 from oracle import mvgbm as omvgbm
@@ -163,3 +164,25 @@ def test_hull_white_every_time_recorded(cuda, dtype, rtol):
                                  dtype=dtype)
     assert got.shape == (N, len(times), 1)
     np.testing.assert_allclose(got, want, rtol=rtol, atol=rtol * 1e-2)
+
+
+@pytest.mark.parametrize("dtype,rtol", [(np.float32, 2e-5), (np.float64, 1e-12)])
+@pytest.mark.parametrize("dim", [1, 2])
+def test_gaussian_hjm_every_time_recorded(cuda, dtype, rtol, dim):
+    from tqf.models import utils
+    from tqf.models.hjm import GaussianHJM
+    mr = [0.03, 0.1][:dim]
+    vol = [0.005, 0.012][:dim]
+    corr = None if dim == 1 else [[1.0, 0.5], [0.5, 1.0]]
+    m = GaussianHJM(dim, mr, vol, lambda *args: [0.01], corr_matrix=corr, dtype=dtype)
+    times = (np.arange(1, 41) / 20).astype(dtype)  # 40 times to t = 2
+    all_times, _, ti = utils.prepare_grid(times=times, time_step=dtype(0.05), dtype=np.dtype(dtype))
+    N = 1000
+    draws = np.random.default_rng(11).standard_normal((N, len(all_times) - 1, dim)).astype(dtype)
+    rates, dfs, x, _ = m.sample_paths(times, N, time_step=0.05, normal_draws=draws)
+    om = ohjm.Model(dim, mr, None, np.asarray(vol)[:, None], corr, dtype)
+    wr, wd, wx = om.sample(all_times, ti, draws.transpose(1, 0, 2), lambda t: np.full(np.shape(t), 0.01, dtype))
+    assert tuple(rates.shape) == (N, len(times)) and tuple(x.shape) == (N, len(times), dim)
+    np.testing.assert_allclose(rates.cpu().numpy(), wr, rtol=rtol, atol=rtol * 1e-2)
+    np.testing.assert_allclose(dfs.cpu().numpy(), wd, rtol=rtol)
+    np.testing.assert_allclose(x.cpu().numpy(), wx, rtol=rtol, atol=rtol * 1e-2)

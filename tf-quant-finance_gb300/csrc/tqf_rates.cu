@@ -166,8 +166,14 @@ int dispatch(const tqf_hull_white_args& a, cudaStream_t s) {
 // Gaussian HJM: Euler for the factors with the short rate and discount factor
 // accumulated in registers (the reference stores every grid point and takes a
 // cumulative product afterwards).
-template <typename T, int DM>
+// STAGE: the recorded rates, discount factors and (when requested) factors go
+// through coalescing RowStagers (dynamic shared memory), chosen when a path's
+// rate row is at least 64 bytes; the three flush at the same slots.  Then
+// every thread runs every round and a thread past the last path simulates
+// that path again with its output dropped.
+template <typename T, int DM, bool STAGE>
 __global__ void __launch_bounds__(kBlock) hjm_kernel(tqf_hjm_args a) {
+  extern __shared__ __align__(16) unsigned char stage_smem[];
   const int d = a.dim;
   const int W = 2 + d + d * d;
   const T* tab = static_cast<const T*>(a.table);
@@ -177,24 +183,42 @@ __global__ void __launch_bounds__(kBlock) hjm_kernel(tqf_hjm_args a) {
   T* df_out = static_cast<T*>(a.df_out);
   T* x_out = static_cast<T*>(a.x_out);
   const int ns = a.num_slots;
+  const int64_t N = a.num_paths;
+  RowStager<T, 1, kBlock> st_rate(stage_smem, 1);
+  RowStager<T, 1, kBlock> st_df(stage_smem + RowStager<T, 1, kBlock>::kBytes, 1);
+  RowStager<T, DM, kBlock> st_x(stage_smem + 2 * RowStager<T, 1, kBlock>::kBytes, d);
   T k[DM];
 #pragma unroll
   for (int c = 0; c < DM; ++c) k[c] = c < d ? kk[c] : T(0);
-  for (int64_t path = (int64_t)blockIdx.x * kBlock + threadIdx.x; path < a.num_paths;
-       path += (int64_t)gridDim.x * kBlock) {
+  const int64_t per_round = (int64_t)gridDim.x * kBlock;
+  for (int64_t base = 0; base < N; base += per_round) {
+    const int64_t row0 = base + (int64_t)blockIdx.x * kBlock;
+    const int64_t path = row0 + threadIdx.x;
+    if (!STAGE && path >= N) break;
+    const int64_t pc = path < N ? path : N - 1;
     T x[DM];
 #pragma unroll
     for (int c = 0; c < DM; ++c) x[c] = T(0);
     T df = T(1);
     T rate = f0[0];  // sum of zero factors + f0(t_0)
+    auto record = [&](int slot) {
+      if constexpr (STAGE) {
+        st_rate.put(rate_out, ns, row0, N, slot, &rate);
+        st_df.put(df_out, ns, row0, N, slot, &df);
+        if (x_out) st_x.put(x_out, ns, row0, N, slot, x);
+      } else {
+        rate_out[path * ns + slot] = rate;
+        df_out[path * ns + slot] = df;
+        if (x_out) {
+#pragma unroll
+          for (int c = 0; c < DM; ++c)
+            if (c < d) x_out[(path * ns + slot) * d + c] = x[c];
+        }
+      }
+    };
     int slot = a.grid_slot[0];
-    if (slot >= 0) {
-      rate_out[path * ns + slot] = rate;
-      df_out[path * ns + slot] = df;
-      if (x_out)
-        for (int c = 0; c < d; ++c) x_out[(path * ns + slot) * d + c] = T(0);
-    }
-    DrawSource<T> src(a.draws, path, d);
+    if (slot >= 0) record(slot);
+    DrawSource<T> src(a.draws, pc, d);
     for (int i = 0; i < a.num_steps; ++i) {
       const T* row = tab + (size_t)i * W;
       const T dt = row[0], sdt = row[1];
@@ -222,25 +246,30 @@ __global__ void __launch_bounds__(kBlock) hjm_kernel(tqf_hjm_args a) {
       }
       rate = s + f0[i + 1];
       slot = a.grid_slot[i + 1];
-      if (slot >= 0) {
-        rate_out[path * ns + slot] = rate;
-        df_out[path * ns + slot] = df;
-        if (x_out)
-          for (int c = 0; c < d; ++c) x_out[(path * ns + slot) * d + c] = x[c];
-      }
+      if (slot >= 0) record(slot);
+    }
+    if (STAGE && st_rate.cnt > 0) {
+      st_rate.flush(rate_out, ns, row0, N);
+      st_df.flush(df_out, ns, row0, N);
+      if (x_out) st_x.flush(x_out, ns, row0, N);
     }
   }
 }
 
 template <typename T, int DM>
 int launch_hjm(const tqf_hjm_args& a, cudaStream_t s) {
+  // stage the outputs when a path's rate row is at least 64 bytes
+  const bool stage = (size_t)a.num_slots * sizeof(T) >= 64;
+  auto k = stage ? hjm_kernel<T, DM, true> : hjm_kernel<T, DM, false>;
+  const size_t smem = stage ? 2 * RowStager<T, 1, kBlock>::kBytes + (a.x_out ? RowStager<T, DM, kBlock>::kBytes : 0)
+                            : 0;
+  if (smem > 48 * 1024) set_smem_config(k, smem);
   int occ = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, hjm_kernel<T, DM>, kBlock, 0) != cudaSuccess || occ < 1)
-    occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem) != cudaSuccess || occ < 1) occ = 1;
   int64_t grid = (a.num_paths + kBlock - 1) / kBlock;
   const int64_t cap = (int64_t)num_sms() * occ;
   if (grid > cap) grid = cap;
-  hjm_kernel<T, DM><<<(unsigned)grid, kBlock, 0, s>>>(a);
+  k<<<(unsigned)grid, kBlock, smem, s>>>(a);
   return check_launch("hjm_kernel");
 }
 
