@@ -80,3 +80,51 @@ def test_entry_points_reject_null_arguments_without_a_gpu():
     eargs.dim = 40
     with pytest.raises(ValueError):
         L.call("tqf_euler_affine", eargs, None)
+
+
+# Entry points whose work is host-only (file parsing, sizes, version, error text).
+_HOST_ONLY = {"tqf_abi_version", "tqf_last_error", "tqf_launch_count", "tqf_sobol_direction_numbers",
+              "tqf_sobol_num_digits", "tqf_mlp_num_params", "tqf_heston_asian_occupancy"}
+
+
+def _compute_entry_points():
+    import ctypes
+    import tqf._lib as L
+    for name, (res, args) in L._SIGNATURES.items():
+        if name not in _HOST_ONLY and res is ctypes.c_int:
+            yield name, args
+
+
+def test_every_compute_entry_point_rejects_null_pointers_on_the_host():
+    # Every pointer null, every size 1: each entry point must answer
+    # TQF_E_INVALID with a message naming itself, before any CUDA call (this
+    # host has no GPU, so a call that reached CUDA would answer TQF_E_CUDA).
+    import ctypes
+    import tqf._lib as L
+    lib = L.load()
+    names = []
+    for name, args in _compute_entry_points():
+        vals = [1 if t in (L.c_i32, L.c_i64, L.c_u32, ctypes.c_uint64) else 1.0 if t is ctypes.c_double else None
+                for t in args]
+        assert getattr(lib, name)(*vals) == L.TQF_E_INVALID, name
+        assert L.last_error().startswith(name + ":"), (name, L.last_error())
+        names.append(name)
+    assert len(names) >= 30
+
+
+def test_every_args_struct_entry_point_rejects_a_zeroed_struct():
+    # A zero-initialised argument struct has no sizes and no buffers: each
+    # entry point taking one must reject it on the host.
+    import ctypes
+    import tqf._lib as L
+    lib = L.load()
+    count = 0
+    for name, args in _compute_entry_points():
+        target = getattr(args[0], "_type_", None)
+        if len(args) != 2 or not (isinstance(target, type) and issubclass(target, ctypes.Structure)):
+            continue
+        zero = args[0]._type_()
+        assert getattr(lib, name)(ctypes.byref(zero), None) == L.TQF_E_INVALID, name
+        assert L.last_error().startswith(name + ":"), (name, L.last_error())
+        count += 1
+    assert count >= 20

@@ -238,12 +238,12 @@ int launch_draws(const uint32_t* v, int d, int steps, int64_t N, uint32_t first,
   return check_launch("sobol_draws_kernel");
 }
 
-int check_sobol_common(const uint32_t* v, int64_t n, int64_t skip, int nd, void* out) {
-  TQF_REQUIRE(v != nullptr && out != nullptr, "sobol: null pointer");
-  TQF_REQUIRE(n >= 1, "sobol: num_results must be >= 1, got %lld", (long long)n);
-  TQF_REQUIRE(skip >= 0, "sobol: skip must be >= 0, got %lld", (long long)skip);
-  TQF_REQUIRE(skip + n <= 2147483647LL, "sobol: skip + num_results must be < 2^31");
-  TQF_REQUIRE(nd >= 1 && nd <= 32, "sobol: nd must be in [1, 32], got %d", nd);
+int check_sobol_common(const char* who, const uint32_t* v, int64_t n, int64_t skip, int nd, void* out) {
+  TQF_REQUIRE(v != nullptr && out != nullptr, "%s: null pointer", who);
+  TQF_REQUIRE(n >= 1, "%s: num_results must be >= 1, got %lld", who, (long long)n);
+  TQF_REQUIRE(skip >= 0, "%s: skip must be >= 0, got %lld", who, (long long)skip);
+  TQF_REQUIRE(skip + n <= 2147483647LL, "%s: skip + num_results must be < 2^31", who);
+  TQF_REQUIRE(nd >= 1 && nd <= 32, "%s: nd must be in [1, 32], got %d", who, nd);
   return TQF_OK;
 }
 
@@ -256,7 +256,7 @@ extern "C" int tqf_sobol_sample(const uint32_t* v_dev, int32_t dim, int64_t num_
                                 int64_t skip, int32_t nd, int32_t out_kind, void* out,
                                 void* stream) {
   clear_error();
-  int rc = check_sobol_common(v_dev, num_results, skip, nd, out);
+  int rc = check_sobol_common("tqf_sobol_sample", v_dev, num_results, skip, nd, out);
   if (rc) return rc;
   TQF_REQUIRE(dim >= 1, "tqf_sobol_sample: dim must be >= 1, got %d", dim);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -281,7 +281,7 @@ extern "C" int tqf_sobol_normal_draws(const uint32_t* v_dev, int32_t num_normal_
                                       int32_t num_steps, int64_t num_paths, int64_t skip,
                                       int32_t nd, int32_t out_kind, void* out, void* stream) {
   clear_error();
-  int rc = check_sobol_common(v_dev, num_paths, skip, nd, out);
+  int rc = check_sobol_common("tqf_sobol_normal_draws", v_dev, num_paths, skip, nd, out);
   if (rc) return rc;
   TQF_REQUIRE(num_normal_draws >= 1 && num_steps >= 1,
               "tqf_sobol_normal_draws: num_normal_draws and num_steps must be >= 1");
