@@ -113,15 +113,15 @@ def sample(dim, drift_fn, volatility_fn, times, time_step=None, num_time_steps=N
         draws = mvn.memory_draws(flat, path_axis=0, step_axis=1)
     else:
         rt = RandomType.PSEUDO if random_type is None else random_type
-        if rt in (RandomType.SOBOL, RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
-            if batch_shape:
-                raise NotImplementedError("low-discrepancy draws with a batch_shape are not supported")
-            sob = utils.generate_mc_normal_draws(dim, steps_total, num_samples, rt, skip=skip, seed=seed, dtype=td)
-            keep_alive.append(sob)
-            draws = mvn.memory_draws(sob, path_axis=1, step_axis=0)
+        quasi = rt in (RandomType.SOBOL, RandomType.HALTON, RandomType.HALTON_RANDOMIZED)
+        if quasi or (mvn.is_antithetic(rt) and batch_shape):
+            # materialised in the reference's layout, batch entries flattened
+            # into the path axis as the state is
+            mat = utils.generate_mc_normal_draws(dim, steps_total, num_samples, rt, batch_shape=batch_shape,
+                                                 skip=skip, seed=seed, dtype=td).reshape(steps_total, M, dim)
+            keep_alive.append(mat)
+            draws = mvn.memory_draws(mat, path_axis=1, step_axis=0)
         else:
-            if mvn.is_antithetic(rt) and batch_shape:
-                raise NotImplementedError("antithetic draws with a batch_shape are not supported")
             draws = mvn.philox_draws(rt, seed, M)
 
     out_shape = batch_shape + (num_samples, num_requested, dim)

@@ -13,6 +13,7 @@ import numpy as np
 import torch
 
 from tqf import _lib
+from tqf.errors import InvalidArgumentError
 from tqf.math.random import multivariate_normal as mvn
 from tqf.math.random.multivariate_normal import RandomType
 
@@ -142,24 +143,33 @@ def generate_mc_normal_draws(num_normal_draws, num_time_steps, num_sample_paths,
     total = nb * int(num_sample_paths)
     if random_type is None:
         random_type = RandomType.PSEUDO
+    shape = (int(num_time_steps),) + batch_shape + (int(num_sample_paths), int(num_normal_draws))
     if random_type == RandomType.SOBOL:
-        if batch_shape:
-            raise NotImplementedError("SOBOL draws with a batch_shape are not supported")
+        # The sample shape batch_shape + [num_sample_paths] is flattened in C
+        # order: point skip + 1 + b * num_sample_paths + n (utils.py:94-99).
         from tqf.math.random import sobol
-        return sobol.normal_draws(int(num_normal_draws), int(num_time_steps), int(num_sample_paths),
-                                  skip=int(skip or 0), dtype=dtype)
+        return sobol.normal_draws(int(num_normal_draws), int(num_time_steps), total,
+                                  skip=int(skip or 0), dtype=dtype).reshape(shape)
     if random_type in (RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
-        if batch_shape:
-            raise NotImplementedError("HALTON draws with a batch_shape are not supported")
         from tqf.math.random import halton
-        return halton.normal_draws(int(num_normal_draws), int(num_time_steps), int(num_sample_paths),
+        return halton.normal_draws(int(num_normal_draws), int(num_time_steps), total,
                                    randomized=random_type == RandomType.HALTON_RANDOMIZED, seed=seed,
-                                   skip=int(skip or 0), dtype=dtype)
+                                   skip=int(skip or 0), dtype=dtype).reshape(shape)
     if mvn.is_antithetic(random_type) and batch_shape:
-        raise NotImplementedError("antithetic draws with a batch_shape are not supported")
+        # Antithetic samples come first and the batch after (utils.py:98-107):
+        # path n of batch entry b is paired with path n + num_sample_paths / 2
+        # of the same entry.
+        n = int(num_sample_paths)
+        if n % 2:
+            raise InvalidArgumentError(
+                "First dimension of `sample_shape` should be even for PSEUDO_ANTITHETIC random type")
+        plain = RandomType.STATELESS if random_type == RandomType.STATELESS_ANTITHETIC else RandomType.PSEUDO
+        z = mvn.philox_normal_draws(plain, seed, int(num_normal_draws), int(num_time_steps), nb * (n // 2), dtype)
+        z = z.reshape(int(num_time_steps), nb, n // 2, int(num_normal_draws))
+        return torch.cat([z, -z], dim=2).reshape(shape)
     draws = mvn.philox_normal_draws(random_type, seed, int(num_normal_draws), int(num_time_steps),
                                     total, dtype)
-    return draws.reshape((int(num_time_steps),) + batch_shape + (int(num_sample_paths), int(num_normal_draws)))
+    return draws.reshape(shape)
 
 
 def step_table(rows: np.ndarray, dtype: torch.dtype, device) -> torch.Tensor:
