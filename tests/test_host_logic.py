@@ -137,3 +137,26 @@ def test_cv_pipeline_stage_marks():
     ti = np.round(np.arange(1, 53) * 252 / 52).astype(int)
     m = stage_marks(ti - 1)
     assert len(m) == 2 * 52 and np.all(np.diff(m) > 0)
+
+
+def test_reference_wrong_times_and_sample_shape_mismatch():
+    # euler_sampling_test.py:503-572: with validate_args, non-increasing times
+    # or times_grid and draws that do not match the grid raise
+    # InvalidArgumentError before anything runs.
+    from tqf import InvalidArgumentError
+    from tqf.models import euler_sampling
+
+    def drift_fn(_, x):
+        return x * 0
+
+    def vol_fn(_, x):
+        return (x * 0 + 1)[..., None]
+
+    kw = dict(dim=1, drift_fn=drift_fn, volatility_fn=vol_fn, seed=42, validate_args=True, dtype=np.float64)
+    with pytest.raises(InvalidArgumentError):  # draws for 5 steps on a 3-point grid
+        euler_sampling.sample(times=[0.1, 0.5, 1.0], normal_draws=np.zeros((100, 5, 1)),
+                              times_grid=[0.1, 0.5, 1.0], **kw)
+    with pytest.raises(InvalidArgumentError):  # times not increasing
+        euler_sampling.sample(times=[0.1, 0.5, 2.0, 1.0], time_step=0.01, **kw)
+    with pytest.raises(InvalidArgumentError):  # times_grid not increasing
+        euler_sampling.sample(times=[0.1, 0.5, 1.0], times_grid=[0.1, 0.5, 1.0, 1.0], **kw)
