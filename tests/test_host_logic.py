@@ -160,3 +160,20 @@ def test_reference_wrong_times_and_sample_shape_mismatch():
         euler_sampling.sample(times=[0.1, 0.5, 2.0, 1.0], time_step=0.01, **kw)
     with pytest.raises(InvalidArgumentError):  # times_grid not increasing
         euler_sampling.sample(times=[0.1, 0.5, 1.0], times_grid=[0.1, 0.5, 1.0, 1.0], **kw)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, None])
+def test_heston_model_drift_and_volatility_pinned(dtype):
+    # heston_model_test.py:175-219 on the model's own drift_fn / volatility_fn
+    # (host torch functions, piecewise-constant parameters read at t = 0.1).
+    import torch
+    from tqf.math.piecewise import PiecewiseConstantFunc
+    from tqf.models import HestonModel
+    process = HestonModel(mean_reversion=PiecewiseConstantFunc([0.5], [1, 1.1], dtype=dtype),
+                          theta=PiecewiseConstantFunc([0.5], [1, 0.9], dtype=dtype),
+                          volvol=PiecewiseConstantFunc([0.3], [0.1, 0.2], dtype=dtype),
+                          rho=PiecewiseConstantFunc([0.5], [0.4, 0.6], dtype=dtype), dtype=dtype)
+    x0 = torch.tensor([np.log(100), 0.045], dtype=torch.float64)
+    np.testing.assert_allclose(process.drift_fn()(0.1, x0).numpy(), [-0.0225, 0.955], rtol=1e-6)
+    np.testing.assert_allclose(process.volatility_fn()(0.1, x0).numpy(),
+                               [[0.21213203, 0.0], [0.00848528, 0.01944222]], rtol=1e-6)
