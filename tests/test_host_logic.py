@@ -177,3 +177,23 @@ def test_heston_model_drift_and_volatility_pinned(dtype):
     np.testing.assert_allclose(process.drift_fn()(0.1, x0).numpy(), [-0.0225, 0.955], rtol=1e-6)
     np.testing.assert_allclose(process.volatility_fn()(0.1, x0).numpy(),
                                [[0.21213203, 0.0], [0.00848528, 0.01944222]], rtol=1e-6)
+
+
+@pytest.mark.parametrize("sample_shape,batch_shape", [((7,), (3,)), ((5,), (4, 2)), ((2, 3, 5), (4, 2)),
+                                                      ((3,), (2, 3, 2)), ((), (3, 2))])
+def test_quasi_random_batch_layout_follows_the_reference(sample_shape, batch_shape):
+    # multivariate_normal.py:370-416 restated with NumPy: points [num, dim] ->
+    # transpose -> reshape(reverse(batch_shape) + sample_shape) -> sample axes
+    # first, batch axes back in order.
+    import torch
+    from tqf.math.random.multivariate_normal import quasi_layout
+    dim = batch_shape[-1]
+    num = int(np.prod(sample_shape + batch_shape)) // dim
+    points = np.arange(num * dim, dtype=np.float64).reshape(num, dim)
+    out_t = tuple(reversed(batch_shape)) + tuple(sample_shape)
+    nb, ns = len(batch_shape), len(sample_shape)
+    perm = list(range(nb, nb + ns)) + list(range(nb - 1, -1, -1))
+    want = np.transpose(points.T.reshape(out_t), perm)
+    got = quasi_layout(torch.from_numpy(points), sample_shape, batch_shape).numpy()
+    assert got.shape == tuple(sample_shape) + tuple(batch_shape)
+    np.testing.assert_array_equal(got, want)

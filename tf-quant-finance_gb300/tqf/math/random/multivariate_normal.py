@@ -122,6 +122,24 @@ def _resolve_dtype(dtype, *tensors):
     return torch.float32
 
 
+def quasi_layout(points, sample_shape, batch_shape):
+    """Arranges low-discrepancy points [n * prod(batch), dim] as sample_shape +
+    batch_shape (the last batch axis is the event dimension).
+
+    Element (s, b_1, ..., b_k, c) takes component c of point q, q the C-order
+    index of (b_k, ..., b_1, s): the reference reshapes the transposed points
+    to reverse(batch_shape) + sample_shape and moves the sample axes to the
+    front (multivariate_normal.py:370-416).
+    """
+    bax = tuple(int(b) for b in batch_shape[:-1])
+    dim = int(batch_shape[-1])
+    n = int(np.prod(sample_shape)) if len(sample_shape) else 1
+    k = len(bax)
+    z = points.reshape(tuple(reversed(bax)) + (n, dim))
+    z = z.permute((k,) + tuple(range(k - 1, -1, -1)) + (k + 1,))
+    return z.reshape(tuple(sample_shape) + tuple(batch_shape))
+
+
 def multivariate_normal(sample_shape, mean=None, covariance_matrix=None, scale_matrix=None,
                         random_type=None, validate_args=False, seed=None, dtype=None, name=None,
                         **kwargs):
@@ -153,22 +171,19 @@ def multivariate_normal(sample_shape, mean=None, covariance_matrix=None, scale_m
         # Antithetic rows [half, 2 half) are the negated rows [0, half), so
         # mean + scale z reproduces concat([m + s, 2 m - (m + s)]).
         z = z.reshape(sample_shape + batch_shape)
-    elif random_type == RandomType.SOBOL:
-        if len(batch_shape) != 1:
-            raise NotImplementedError("SOBOL draws with a batched mean/scale are not supported")
+    elif random_type in (RandomType.SOBOL, RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
         skip = int(kwargs.get("skip", 0) or 0)
-        from tqf.math.random import sobol
-        z = sobol.sample_normal(dim, n, skip=skip, dtype=dtype).reshape(sample_shape + (dim,))
-    elif random_type in (RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
-        if len(batch_shape) != 1:
-            raise NotImplementedError("HALTON draws with a batched mean/scale are not supported")
-        skip = int(kwargs.get("skip", 0) or 0)
-        from tqf.math.random import halton
-        z, _ = halton.sample(dim, sequence_indices=torch.arange(skip, skip + n),
-                             randomized=random_type == RandomType.HALTON_RANDOMIZED,
-                             randomization_params=kwargs.get("randomization_params"), seed=seed, dtype=dtype,
-                             normal=True)
-        z = z.reshape(sample_shape + (dim,))
+        total = n * int(np.prod(batch_shape[:-1]))
+        if random_type == RandomType.SOBOL:
+            from tqf.math.random import sobol
+            points = sobol.sample_normal(dim, total, skip=skip, dtype=dtype)
+        else:
+            from tqf.math.random import halton
+            points, _ = halton.sample(dim, sequence_indices=torch.arange(skip, skip + total),
+                                      randomized=random_type == RandomType.HALTON_RANDOMIZED,
+                                      randomization_params=kwargs.get("randomization_params"), seed=seed,
+                                      dtype=dtype, normal=True)
+        z = quasi_layout(points, sample_shape, batch_shape)
     else:
         raise NotImplementedError(f"unsupported random_type {random_type}")
     if scale is not None:
@@ -179,4 +194,4 @@ def multivariate_normal(sample_shape, mean=None, covariance_matrix=None, scale_m
 
 
 __all__ = ["RandomType", "multivariate_normal", "philox_key", "philox_draws", "memory_draws",
-           "philox_normal_draws", "is_antithetic"]
+           "philox_normal_draws", "is_antithetic", "quasi_layout"]
