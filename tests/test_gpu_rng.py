@@ -184,3 +184,27 @@ def test_draws_prefix_stability_and_moments(cuda):
     assert s.shape == (1000, 2) and abs(float(s.mean())) < 0.02
     z = mv_normal_sample([1000], mean=np.array([2.0, 3.0]), random_type=RandomType.PSEUDO_ANTITHETIC, seed=2)
     torch.testing.assert_close(z[:500] + z[500:], torch.tensor([4.0, 6.0], dtype=z.dtype, device=z.device).expand(500, 2))
+
+
+def test_sobol_normal_integral_mean_and_var(cuda):
+    # sobol_test.py:111-143: importance-sampled mean and standard deviation of
+    # N(mu_p, 0.5^2) from N(0, 1) quantiles of 1,000 Sobol points
+    from scipy.stats import norm
+    from tqf.math.random import sobol
+    mu_p, sigma_p = np.array([-1.0, 1.0]), np.array([0.5, 0.5])
+    cdf_sample = sobol.sample(2, 1000, dtype=torch.float64).cpu().numpy()
+    q_sample = norm.ppf(cdf_sample)
+    w = norm.pdf(q_sample, loc=mu_p, scale=sigma_p) / norm.pdf(q_sample)
+    e_x = np.mean(q_sample * w, 0)
+    stddev = np.sqrt(np.mean(q_sample ** 2 * w - e_x ** 2, 0))
+    np.testing.assert_allclose(e_x, mu_p, rtol=0.01)
+    np.testing.assert_allclose(stddev, sigma_p, rtol=0.02)
+
+
+def test_sobol_two_dimensional_projection(cuda):
+    # sobol_test.py:145-157: the last two of 170 dimensions are uncorrelated
+    from tqf.math.random import sobol
+    sample = sobol.sample(170, 1000).cpu().numpy()
+    x, y = sample[:, 168], sample[:, 169]
+    np.testing.assert_allclose(np.corrcoef(x, y)[1, 0], 0.0, atol=0.05)
+    np.testing.assert_allclose((x * y).mean(), 0.25, rtol=0.05)
