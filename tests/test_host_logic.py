@@ -197,3 +197,21 @@ def test_quasi_random_batch_layout_follows_the_reference(sample_shape, batch_sha
     got = quasi_layout(torch.from_numpy(points), sample_shape, batch_shape).numpy()
     assert got.shape == tuple(sample_shape) + tuple(batch_shape)
     np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("corr", [[[1, 0.1], [0.1, 1]], None])
+def test_multivariate_gbm_drift_and_volatility(dtype, corr):
+    # geometric_brownian_motion_test.py:174-245 (with and without a correlation matrix)
+    import torch
+    from tqf.models import ItoProcess, MultivariateGeometricBrownianMotion
+    means, vols = [0.05, 0.02], [0.1, 0.2]
+    process = MultivariateGeometricBrownianMotion(dim=2, means=means, volatilities=vols, corr_matrix=corr,
+                                                  dtype=torch.float64)
+    assert isinstance(process, ItoProcess)
+    state = np.array([[1.0, 2.0], [3.0, 4.0], [5.0, 6.0]], dtype=dtype)
+    np.testing.assert_allclose(process.drift_fn()(0.2, state).numpy(), np.array(means) * state,
+                               atol=1e-8, rtol=1e-8)
+    expected_vol = np.expand_dims(np.array(vols) * state, -1) * np.linalg.cholesky(
+        np.eye(2) if corr is None else np.array(corr, np.float64))
+    np.testing.assert_allclose(process.volatility_fn()(0.2, state).numpy(), expected_vol, atol=1e-8, rtol=1e-8)

@@ -22,9 +22,10 @@ from tqf.math import piecewise as pw
 from tqf.math.random import multivariate_normal as mvn
 from tqf.math.random.multivariate_normal import RandomType
 from tqf.models import utils
+from tqf.models.ito_process import ItoProcess
 
 
-class GeometricBrownianMotion:
+class GeometricBrownianMotion(ItoProcess):
     """GeometricBrownianMotion(mean, volatility, dtype=None, name=None)."""
 
     def __init__(self, mean, volatility, dtype=None, name=None):

@@ -17,6 +17,7 @@ from tqf import _lib
 from tqf.math.random import multivariate_normal as mvn
 from tqf.math.random.multivariate_normal import RandomType
 from tqf.models import utils
+from tqf.models.ito_process import ItoProcess
 
 
 def cholesky_f64(corr, device) -> torch.Tensor:
@@ -31,7 +32,7 @@ def cholesky_f64(corr, device) -> torch.Tensor:
     return L
 
 
-class MultivariateGeometricBrownianMotion:
+class MultivariateGeometricBrownianMotion(ItoProcess):
 
     def __init__(self, dim, means=0.0, volatilities=1.0, corr_matrix=None, dtype=None, name=None):
         self._name = name or "multivariate_geometric_brownian_motion"
@@ -56,6 +57,28 @@ class MultivariateGeometricBrownianMotion:
 
     def name(self):
         return self._name
+
+    def drift_fn(self):
+        """a(t, x) = means * x, in the process dtype
+        (multivariate_geometric_brownian_motion.py:127-133)."""
+        def _drift_fn(t, x):
+            del t
+            x = torch.as_tensor(x).to(self.dtype())
+            return torch.as_tensor(self._means, device=x.device) * x
+        return _drift_fn
+
+    def volatility_fn(self):
+        """b(t, x) = (volatilities * x)[:, None] * chol(corr_matrix), or
+        diag(volatilities * x) without a correlation matrix (:135-150)."""
+        def _vol_fn(t, x):
+            del t
+            x = torch.as_tensor(x).to(self.dtype())
+            vols = torch.as_tensor(self._vols, device=x.device) * x
+            if self._corr is None:
+                return torch.diag_embed(vols)
+            chol = torch.linalg.cholesky(torch.as_tensor(self._corr, dtype=torch.float64))
+            return vols[..., None] * chol.to(dtype=vols.dtype, device=vols.device)
+        return _vol_fn
 
     def sample_paths(self, times, initial_state=None, num_samples=1, random_type=None, seed=None, skip=0,
                      normal_draws=None, name=None, lz_mode=0):
