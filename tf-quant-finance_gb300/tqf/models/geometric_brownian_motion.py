@@ -30,6 +30,16 @@ class GeometricBrownianMotion(ItoProcess):
 
     def __init__(self, mean, volatility, dtype=None, name=None):
         self._name = name or "geometric_brownian_motion"
+        # Scalar torch tensors that require grad stay watched: sample_paths
+        # returns paths differentiable with respect to them.
+        self._watched = {}
+        for key, val in (("mean", mean), ("volatility", volatility)):
+            if isinstance(val, torch.Tensor) and val.requires_grad:
+                if val.numel() != 1:
+                    raise NotImplementedError("gradients are supported for scalar mean and volatility")
+                self._watched[key] = val
+        mean = mean.detach().cpu().numpy() if isinstance(mean, torch.Tensor) else mean
+        volatility = volatility.detach().cpu().numpy() if isinstance(volatility, torch.Tensor) else volatility
         self._mean, self._mean_is_constant = pw.convert_to_tensor_or_func(
             mean, dtype=None if dtype is None else utils.np_dtype(dtype))
         if dtype is None:
@@ -156,8 +166,29 @@ class GeometricBrownianMotion(ItoProcess):
                                      np.shape(self._volatility)[:-1] if np.ndim(self._volatility) > 0 else ())
             shape_b = tuple(sb)
         if not shape_b and B == 1:
-            return out[0]
+            return self._attach_gradient(out[0], times_np, float(x0[0])) if self._watched else out[0]
         return out.reshape(shape_b + (N, k, 1)) if shape_b else out
+
+    def _attach_gradient(self, paths, times_np, x0):
+        """Paths as a differentiable function of the watched scalar mean and
+        volatility: log x_k = log x0 + (mu - s^2 / 2) t_k + s W_k
+        (univariate_geometric_brownian_motion.py:261-318), with the Brownian
+        values W_k recovered from the sampled paths.  The values returned are
+        the kernel's; only the gradient comes from the expression."""
+        td, dev = paths.dtype, paths.device
+
+        def param(key, value):
+            if key in self._watched:
+                return self._watched[key].to(device=dev, dtype=td).reshape(())
+            return torch.tensor(float(np.asarray(value).reshape(-1)[0]), dtype=td, device=dev)
+
+        mu, s = param("mean", self._mean), param("volatility", self._volatility)
+        t = torch.as_tensor(times_np, dtype=td, device=dev)[:, None]
+        with torch.no_grad():
+            drift = (mu - s * s / 2) * t
+            w = torch.where(s != 0, (torch.log(paths / x0) - drift) / torch.where(s != 0, s, 1), 0)
+        expr = x0 * torch.exp((mu - s * s / 2) * t + s * w)
+        return paths + (expr - expr.detach())
 
 
 __all__ = ["GeometricBrownianMotion"]
