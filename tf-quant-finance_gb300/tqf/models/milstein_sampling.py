@@ -39,7 +39,7 @@ def sample(*, dim, drift_fn, volatility_fn, times, time_step=None, num_time_step
     del swap_memory, precompute_normal_draws, name
     if stratonovich_order <= 0:
         raise ValueError("`stratonovich_order` must be a positive integer.")
-    if watch_params is not None:
+    if watch_params:  # an empty list watches nothing: the paths are the same as without it
         raise NotImplementedError("watch_params (the custom for_loop gradient) is provided by "
                                   "euler_sampling.sample; the Milstein sampler is forward-only here")
     np_dt = utils.np_dtype(dtype) if dtype is not None else utils.infer_dtype(times)
