@@ -47,6 +47,17 @@ def main(ref_root):
                        "skip_expr": "2**31 - 5", "skip": 2 ** 31 - 5,
                        "expected": [[0.25], [0.75], [0.5]]},
     }
+    # generate_mc_normal_draws with SOBOL draws: [steps, paths, d] normals of
+    # the points skip + 1 ..., dimension step * d + component
+    utils_test = os.path.join(tff, "models", "utils_test.py")
+    usrc = open(utils_test).read()
+    for needle in ("num_draws = tf.constant(2", "steps_num = tf.constant(3", "num_samples = tf.constant(4",
+                   "skip = 10", "random_type = tff.math.random.RandomType.SOBOL"):
+        assert needle in usrc, needle
+    draws = _literal_assignments(utils_test, "test_sobol_numbers_generation")["expected_samples"]
+    golden["mc_normal_draws_sobol"] = {"source": "tf_quant_finance/models/utils_test.py:33-60",
+                                       "num_normal_draws": 2, "num_time_steps": 3, "num_sample_paths": 4,
+                                       "skip": 10, "expected": draws, "rtol": 1e-5, "atol": 1e-5}
     here = os.path.dirname(os.path.abspath(__file__))
     with open(os.path.join(here, "sobol_golden.json"), "w") as f:
         json.dump(golden, f, indent=1)

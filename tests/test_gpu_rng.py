@@ -208,3 +208,17 @@ def test_sobol_two_dimensional_projection(cuda):
     x, y = sample[:, 168], sample[:, 169]
     np.testing.assert_allclose(np.corrcoef(x, y)[1, 0], 0.0, atol=0.05)
     np.testing.assert_allclose((x * y).mean(), 0.25, rtol=0.05)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_mc_normal_draws_sobol_known_values(cuda, dtype):
+    # utils_test.py:33-60 on the device generator: [steps, paths, d]
+    import json, os
+    from tqf.math.random import RandomType
+    from tqf.models import utils
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "sobol_golden.json")))["mc_normal_draws_sobol"]
+    got = utils.generate_mc_normal_draws(num_normal_draws=g["num_normal_draws"], num_time_steps=g["num_time_steps"],
+                                         num_sample_paths=g["num_sample_paths"], random_type=RandomType.SOBOL,
+                                         dtype=dtype, skip=g["skip"])
+    assert tuple(got.shape) == (3, 4, 2) and got.dtype == dtype
+    np.testing.assert_allclose(got.cpu().numpy(), g["expected"], rtol=g["rtol"], atol=g["atol"])

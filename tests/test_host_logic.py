@@ -215,3 +215,17 @@ def test_multivariate_gbm_drift_and_volatility(dtype, corr):
     expected_vol = np.expand_dims(np.array(vols) * state, -1) * np.linalg.cholesky(
         np.eye(2) if corr is None else np.array(corr, np.float64))
     np.testing.assert_allclose(process.volatility_fn()(0.2, state).numpy(), expected_vol, atol=1e-8, rtol=1e-8)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_prepare_grid_reference_cases(dtype):
+    # utils_test.py:96-131 on the product's prepare_grid
+    from tqf.models import utils
+    times = np.linspace(dtype(0.02), dtype(1.0), 50).astype(dtype)
+    grid, _, idx = utils.prepare_grid(times=times, time_step=times[-1] / 100, dtype=dtype, num_time_steps=100)
+    np.testing.assert_allclose(grid, np.linspace(0, 1, 101, dtype=dtype), rtol=1e-6, atol=1e-6)
+    np.testing.assert_array_equal(idx, [2 * i for i in range(1, 51)])
+    times = np.array([0.1, 0.5, 1, 2], dtype=dtype)
+    grid, _, idx = utils.prepare_grid(times=times, time_step=np.float64(0.1), dtype=dtype)
+    np.testing.assert_allclose(grid, np.linspace(0, 2, 21, dtype=dtype), rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(grid[idx], times, rtol=1e-6, atol=1e-6)

@@ -248,3 +248,14 @@ def test_hjm_oracle_bond_prices():
         got = m.bond(g["state"] * np.ones((len(t), c["dim"])), t, t + g["maturity_offset"],
                      lambda x: np.full(np.shape(x), g["flat_rate"]))
         np.testing.assert_allclose(got, c["expected"], rtol=g["rtol"], atol=g["atol"])
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_mc_normal_draws_sobol_known_values(dtype):
+    # utils_test.py:33-60: generate_mc_normal_draws(2 draws, 3 steps, 4 paths,
+    # SOBOL, skip 10) -> [steps, paths, d], dimension step * d + component
+    g = SOBOL_GOLDEN["mc_normal_draws_sobol"]
+    d, steps, n = g["num_normal_draws"], g["num_time_steps"], g["num_sample_paths"]
+    u = sobol.sample(d * steps, n, skip=g["skip"], dtype=dtype)
+    z = sobol.normal_from_uniform(u).reshape(n, steps, d).transpose(1, 0, 2)
+    np.testing.assert_allclose(z, g["expected"], rtol=g["rtol"], atol=g["atol"])
