@@ -79,3 +79,40 @@ def test_compare_monte_carlo_to_european_option(cuda, case):
     ref = closed_form.heston_price(spot=np.exp(x0), strike=strike, expiry=maturity, rate=rate, v0=v0,
                                    kappa=kappa, theta=theta, xi=volvol, rho=rho)
     np.testing.assert_allclose(mc, ref, atol=0.1, rtol=0.1)
+
+
+def test_volatility(cuda):
+    # :32-49: with a tiny vol of vol the variance stays within 0.005 of theta
+    # after the first 50 requested times
+    from tqf.models import HestonModel
+    process = HestonModel(mean_reversion=1.0, theta=0.05, volvol=0.00001, rho=-0.0, dtype=np.float64)
+    times = np.linspace(0.0, 1.0, 365)
+    paths = process.sample_paths(times, time_step=0.01, num_samples=2, initial_state=np.array([np.log(100), 0.045]),
+                                 seed=None)
+    assert np.max(np.abs(paths.cpu().numpy()[..., 1][:, 50:] - 0.05)) < 0.005
+
+
+def test_state(cuda):
+    # :51-77: with a tiny vol of vol the spot is a GBM with volatility sqrt(theta)
+    from tqf.models import HestonModel
+    process = HestonModel(mean_reversion=1.0, theta=1.0, volvol=0.00001, rho=-0.0, dtype=np.float64)
+    times = [0.0, 0.5, 1.0]
+    state = process.sample_paths(times, time_step=0.001, num_samples=1000,
+                                 initial_state=np.array([np.log(100), 1.0]), seed=None).cpu().numpy()[..., 0]
+    np.testing.assert_allclose(state[:, 0], np.log(100), 1e-8)
+    for i in (1, 2):
+        np.testing.assert_allclose(np.mean(np.exp(state[:, i])), 100, 1.0)
+        np.testing.assert_allclose(np.std(np.exp(state[:, 1])), 100 * np.sqrt(np.exp(times[i]) - 1), 2.0)
+
+
+def test_expected_var_mc(cuda):
+    # :97-135: the Monte Carlo integral of the variance over [0, 1] against
+    # expected_total_variance within 1%
+    from tqf.models import HestonModel
+    process = HestonModel(mean_reversion=10.0, theta=0.04, volvol=1.0, rho=-0.5, dtype=np.float64)
+    times = np.linspace(0, 1.0, 252)
+    paths = process.sample_paths(times, np.array([1.0, 0.1]), time_step=0.1, num_samples=10000,
+                                 seed=123).cpu().numpy()
+    weights = np.concatenate([[times[0]], np.diff(times)])
+    mc = np.mean(np.sum(weights * paths[:, :, 1], axis=1))
+    np.testing.assert_allclose(float(process.expected_total_variance(1.0, 0.1)), mc, rtol=0.01)

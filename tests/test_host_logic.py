@@ -229,3 +229,23 @@ def test_prepare_grid_reference_cases(dtype):
     grid, _, idx = utils.prepare_grid(times=times, time_step=np.float64(0.1), dtype=dtype)
     np.testing.assert_allclose(grid, np.linspace(0, 2, 21, dtype=dtype), rtol=1e-6, atol=1e-6)
     np.testing.assert_allclose(grid[idx], times, rtol=1e-6, atol=1e-6)
+
+
+def test_heston_expected_total_variance():
+    # heston_model_test.py:79-96, 137-170: scalar and batched closed form;
+    # piecewise mean reversion / theta raise ValueError
+    from tqf.math.piecewise import PiecewiseConstantFunc
+    from tqf.models import HestonModel
+
+    def ground(v0, t, k=1.3, th=0.2):
+        return (v0 - th) * (1 - np.exp(-k * t)) / k + th * t
+
+    process = HestonModel(mean_reversion=1.3, theta=0.2, volvol=0.01, rho=0.1, dtype=np.float64)
+    np.testing.assert_allclose(process.expected_total_variance(1.2, 0.3).numpy(), ground(0.3, 1.2))
+    t, v0 = np.array([0.1, 1.0, 2.0]), np.array([0.1, 0.2, 0.3])
+    np.testing.assert_allclose(process.expected_total_variance(t, v0).numpy(), ground(v0, t))
+    pw = HestonModel(mean_reversion=PiecewiseConstantFunc([0.5], [1, 1.1], dtype=np.float64),
+                     theta=PiecewiseConstantFunc([0.5], [1, 0.9], dtype=np.float64), volvol=0.1, rho=0.5,
+                     dtype=np.float64)
+    with pytest.raises(ValueError):
+        pw.expected_total_variance(1.0, 1.0)
