@@ -445,18 +445,20 @@ typedef struct tqf_heston_args {
 TQF_API int tqf_heston_euler(const tqf_heston_args* args, void* stream);
 
 /* Allocation-free variant of tqf_heston_euler's fused pricing (no
- * counterpart in the reference).  Some callers cannot call cudaMalloc: code
- * running while a CUDA graph is being captured, hosts with a custom or
- * fixed-budget device allocator that forbids stray allocations, and plugins
- * whose host application owns all device memory.  They still pass inputs and
- * outputs (step table, strikes, payoff.out); the per-CTA partial sums go to a
- * 2 MiB array compiled into the library instead of payoff.workspace (ignored).
- * Limit: payoff.num_strikes <= 64.  The first call on each device looks up
- * that array's device address (cudaGetSymbolAddress), so make it before any
- * stream capture.  All calls share the array: two calls that overlap on the
- * GPU (different streams, or concurrent host threads) race; serialise them.
- * Nothing needs clearing between calls — every partial row the final
- * reduction reads is written by the same call. */
+ * counterpart in the reference).  Some callers cannot call cudaMalloc: hosts
+ * with a custom or fixed-budget device allocator that forbids stray
+ * allocations, and plugins whose host application owns all device memory and
+ * hands the library only its input and output buffers.  They still pass
+ * inputs and outputs (step table, strikes, payoff.out); the per-CTA partial
+ * sums go to a 2 MiB array compiled into the library instead of
+ * payoff.workspace (ignored).  Limit: payoff.num_strikes <= 64; more is
+ * rejected with TQF_E_INVALID.  The first call on each device (and the first
+ * after a cudaDeviceReset) looks up that array's device address
+ * (cudaGetSymbolAddress), so make it before any stream capture.  All calls
+ * share the array: two calls that overlap on the GPU (different streams, or
+ * concurrent host threads) race; serialise them.  Nothing needs clearing
+ * between calls — every partial row the final reduction reads is written by
+ * the same call. */
 TQF_API int tqf_heston_euler_price_noalloc(const tqf_heston_args* args, void* stream);
 
 /* Andersen QE scheme exactly as HestonModel.sample_paths runs it

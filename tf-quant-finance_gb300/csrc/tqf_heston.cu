@@ -691,24 +691,58 @@ static __device__ __align__(256) double g_noalloc_partials[kNoAllocDoubles];
 
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mutex;
-double* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+struct NoAllocSlot {
+  unsigned long long ctx_id;  // id of the context the address belongs to
+  double* ptr;
+};
+NoAllocSlot g_noalloc_slot[kNoAllocMaxDevices] = {};
 
-// Device address of g_noalloc_partials on the current device, looked up once
-// per device (the host-side symbol is only a stand-in, never a device pointer).
+// cuCtxGetId through the runtime's driver entry-point query, so the library
+// needs no link against libcuda.  nullptr when the driver lacks it.
+using CtxGetIdFn = int (*)(void* ctx, unsigned long long* id);
+CtxGetIdFn ctx_get_id_fn() {
+  static CtxGetIdFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    cudaGetLastError();
+    return reinterpret_cast<CtxGetIdFn>(p);
+  }();
+  return fn;
+}
+
+// Device address of g_noalloc_partials in the current device's context (the
+// host-side symbol is only a stand-in, never a device pointer).  The address
+// is looked up on the first call in each context and kept with that
+// context's unique id: after a cudaDeviceReset the runtime makes a new
+// primary context, the module loads again at another address, and the next
+// call sees a new id and looks the address up again.  Without cuCtxGetId
+// (drivers older than CUDA 12) it is looked up on every call.
 int noalloc_scratch(double** out) {
   int dev = 0;
   int rc = check_cuda(cudaGetDevice(&dev), "tqf_heston_euler_price_noalloc: cudaGetDevice");
   if (rc) return rc;
   TQF_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "tqf_heston_euler_price_noalloc: device %d out of range", dev);
+  // cudaSetDevice initialises the device's primary context (again, after a
+  // reset), so the id read next is the context the kernels will run in.
+  rc = check_cuda(cudaSetDevice(dev), "tqf_heston_euler_price_noalloc: cudaSetDevice");
+  if (rc) return rc;
+  unsigned long long id = 0;
+  const CtxGetIdFn get_id = ctx_get_id_fn();
+  const bool have_id = get_id != nullptr && get_id(nullptr, &id) == 0;
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (g_noalloc_ptr[dev] == nullptr) {
+  NoAllocSlot& slot = g_noalloc_slot[dev];
+  if (!have_id || slot.ptr == nullptr || slot.ctx_id != id) {
     void* p = nullptr;
     rc = check_cuda(cudaGetSymbolAddress(&p, g_noalloc_partials),
                     "tqf_heston_euler_price_noalloc: cudaGetSymbolAddress");
     if (rc) return rc;
-    g_noalloc_ptr[dev] = static_cast<double*>(p);
+    slot.ptr = static_cast<double*>(p);
+    slot.ctx_id = id;
   }
-  *out = g_noalloc_ptr[dev];
+  *out = slot.ptr;
   return TQF_OK;
 }
 
