@@ -606,31 +606,48 @@ def run_stored_paths(n_paths=N_PATHS, n_steps=N_STEPS, reps=5):
 
 def run_heston_sobol(n_paths=N_PATHS, n_steps=N_STEPS, reps=5):
     """The Heston pricing workload with Sobol draws (the quasi-random variant
-    of the headline config: dimension 2 x 252 = 504, points 1 .. 2^22): the
+    of the headline config: dimension 2 x 252 = 504, points 1 .. 2^22).
+    Fused: the normals are computed inside the pricing kernel from per-window
+    shared-memory tables (no draw buffer).  Materialised (for comparison): the
     draws are generated on the device ([252, 2^22, 2] float32, 8.5 GB) and
-    read in place by the fused kernel.  Median of `reps` calls through the
-    public API, CUDA events, draw generation included."""
+    read in place by the same kernel.  Median of `reps` calls through the
+    public API, CUDA events, draw generation included; the two prices agree
+    to the float64 summation order."""
     import torch
     from tqf.math.random import RandomType
+    from tqf.models import utils
     from tqf.pricing import heston_european_mc
     kw = dict(strikes=strikes(), expiry=1.0, spot=100.0, variance=0.04, mean_reversion=2.0, theta=0.04, volvol=0.3,
-              rho=-0.7, discount_rate=0.02, num_samples=n_paths, num_time_steps=n_steps,
-              random_type=RandomType.SOBOL)
-    res = heston_european_mc(**kw)
-    torch.cuda.synchronize()
-    ts = []
-    for _ in range(reps):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        res = heston_european_mc(**kw)
-        e1.record()
-        e1.synchronize()
-        ts.append(e0.elapsed_time(e1) * 1e-3)
-    sec = sorted(ts)[len(ts) // 2]
+              rho=-0.7, discount_rate=0.02, num_samples=n_paths, num_time_steps=n_steps)
+
+    def timed(fn):
+        res = fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            res = fn()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return sorted(ts)[len(ts) // 2], res
+
+    sec, res = timed(lambda: heston_european_mc(random_type=RandomType.SOBOL, **kw))
+
+    def materialised():
+        d = utils.generate_mc_normal_draws(2, n_steps, n_paths, RandomType.SOBOL, dtype=torch.float32)
+        return heston_european_mc(normal_draws=d.permute(1, 0, 2), **kw)
+
+    sec_m, res_m = timed(materialised)
+    torch.cuda.empty_cache()
     k = strikes()
     j = int(np.argmin(np.abs(k - 100.0)))
     return {"config": f"Heston FT-Euler FP32, {n_paths} paths x {n_steps} steps, 64 strikes, Sobol dim {2 * n_steps}",
-            "seconds": sec, "path_steps_per_s": n_paths * n_steps / sec, "draw_bytes": n_paths * n_steps * 2 * 4,
+            "seconds": sec, "path_steps_per_s": n_paths * n_steps / sec,
+            "materialised_seconds": sec_m, "materialised_draw_bytes": n_paths * n_steps * 2 * 4,
+            "max_rel_price_diff_fused_vs_materialised": float(
+                ((res.price - res_m.price).abs() / res_m.price.abs().clamp_min(1e-12)).max()),
             "atm_call_price": float(res.price[j]), "strike": float(k[j])}
 
 
@@ -755,6 +772,8 @@ def main():
     ap.add_argument("--no-lsm", action="store_true")
     ap.add_argument("--no-greeks", action="store_true")
     ap.add_argument("--no-heston-sobol", action="store_true")
+    ap.add_argument("--heston-sobol-only", action="store_true",
+                    help="run only the Heston pricing measurement with Sobol draws")
     ap.add_argument("--no-euler-call", action="store_true")
     ap.add_argument("--euler-call-only", action="store_true", help="run only the float64 Euler call measurement")
     ap.add_argument("--no-stored-paths", action="store_true")
@@ -799,6 +818,9 @@ def main():
         return
     if args.sobol_only:
         print(json.dumps({"sobol": run_sobol(chunk=args.sobol_chunk)}))
+        return
+    if args.heston_sobol_only:
+        print(json.dumps({"heston_sobol": run_heston_sobol(n_paths=args.paths)}))
         return
     if args.basket_only:
         print(json.dumps({"basket": run_basket(paths_n=args.basket_paths)}))

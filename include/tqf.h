@@ -44,6 +44,7 @@ extern "C" {
 
 #define TQF_DRAWS_MEMORY 0 /* read normals from `tqf_draws.ptr` with strides */
 #define TQF_DRAWS_PHILOX 1 /* generate them in-kernel (Philox4x32-10) */
+#define TQF_DRAWS_SOBOL 2  /* Sobol normals generated in-kernel (Heston kernels only) */
 
 /* Sobol output kinds (tqf_sobol_sample / tqf_sobol_normal_draws). */
 #define TQF_SOBOL_U32 0        /* integer at the reference's nd-digit scaling */
@@ -61,7 +62,14 @@ extern "C" {
  * layout and the caller-facing [N, steps, d] layout are read without a
  * transpose copy.  Philox draws use key (key0, key1) and the canonical
  * counter layout; `antithetic` makes paths [half, 2*half) the negation of
- * paths [0, half) (tff/math/random_ops/multivariate_normal.py:276-311). */
+ * paths [0, half) (tff/math/random_ops/multivariate_normal.py:276-311).
+ * Sobol draws (TQF_DRAWS_SOBOL) are the SOBOL branch of
+ * generate_mc_normal_draws (tff/models/utils.py:95-127) computed inside the
+ * path kernel: ptr = the device direction numbers [dims][32] of
+ * tqf_sobol_direction_numbers (dims >= key1 * num_steps), key0 = nd (the
+ * digit count of the whole request), key1 = normals per step, and path n
+ * takes point path_offset + 1 + n, step i component c dimension i*key1 + c;
+ * the values equal tqf_sobol_normal_draws's bit for bit. */
 typedef struct tqf_draws {
   int32_t source;
   int32_t antithetic;

@@ -88,8 +88,12 @@ def test_basket_price_sums_match_oracle_with_same_draws(cuda):
 
 
 def test_basket_adjoint_greeks_vs_finite_differences(cuda):
-    """Pathwise delta/vega within 1e-4 (relative to the price scale) of
-    central common-random-number bump-and-revalue."""
+    """Pathwise delta and vega of all 16 assets within 1e-4 (delta absolute,
+    vega relative to max(1, |bump|)) of central common-random-number
+    bump-and-revalue in float64.  The bumps (1e-5 relative in the spot, 1e-6
+    in the volatility) are small enough that few paths cross the strike
+    inside a bump, and large enough that the difference quotient's float64
+    rounding stays ~1e-9."""
     from tqf.math.random import RandomType
     from tqf.pricing import basket_european_mc
     d = 16
@@ -97,22 +101,21 @@ def test_basket_adjoint_greeks_vs_finite_differences(cuda):
     kw = dict(rate=0.02, corr=corr, strike=100.0, expiry=1.0, num_time_steps=64, num_samples=1 << 20,
               random_type=RandomType.STATELESS, seed=[3, 4], dtype=torch.float64)
     base = basket_european_mc(spots=np.full(d, 100.0), vols=vols, **kw)
-    for i in (0, 7, 15):
-        h = 1e-3 * 100.0
+    h, hv = 1e-3, 1e-6
+    for i in range(d):
         up = np.full(d, 100.0)
         up[i] += h
         dn = np.full(d, 100.0)
         dn[i] -= h
         fd = (basket_european_mc(spots=up, vols=vols, **kw).price - basket_european_mc(spots=dn, vols=vols, **kw).price) / (2 * h)
         assert abs(float(base.delta[i]) - fd) < 1e-4, (i, float(base.delta[i]), fd)
-        hv = 1e-4
         vu = vols.copy()
         vu[i] += hv
         vd = vols.copy()
         vd[i] -= hv
         fdv = (basket_european_mc(spots=np.full(d, 100.0), vols=vu, **kw).price
                - basket_european_mc(spots=np.full(d, 100.0), vols=vd, **kw).price) / (2 * hv)
-        assert abs(float(base.vega[i]) - fdv) < 1e-4 * max(1.0, abs(fdv)) * 10, (i, float(base.vega[i]), fdv)
+        assert abs(float(base.vega[i]) - fdv) < 1e-4 * max(1.0, abs(fdv)), (i, float(base.vega[i]), fdv)
 
 
 def test_basket_autograd_function(cuda):

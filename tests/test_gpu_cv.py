@@ -93,13 +93,20 @@ def test_train_step_gradient_matches_autograd(cuda):
     ref = params.grad
     got = grad.cpu()
     np.testing.assert_allclose(loss, float(L), rtol=2e-2)
+    # Elementwise, per parameter block: |got - ref| <= 0.04 rms(ref block) +
+    # 0.02 |ref|.  The kernels' SFU tanh differs from the exact tanh of the
+    # restatement by about one BF16 ulp in some activations, which moves
+    # elements by up to ~2 % of the block's rms (measured: W1 2.1 %, W2 1.6 %,
+    # b2 0.4 %, w3 0.2 %); an element of the wrong sign fails unless it is
+    # below ~2 % of the rms.
     blocks = {"W1": (0, 1024), "W2": (1024, 5120), "b2": (5120, 5184), "w3": (5184, 5248), "b3": (5248, 5249),
               "c": (5249, 5250)}
     for name, (a, b) in blocks.items():
-        r, gg = ref[a:b], got[a:b]
-        cos = float(torch.nn.functional.cosine_similarity(r, gg, dim=0)) if b - a > 1 else 1.0
-        assert cos > 0.98, (name, cos)
-        np.testing.assert_allclose(float(gg.norm()), float(r.norm()), rtol=5e-2, err_msg=name)
+        r, gg = ref[a:b].double(), got[a:b].double()
+        rms = float(r.pow(2).mean().sqrt())
+        bound = 0.04 * rms + 0.02 * r.abs()
+        bad = (gg - r).abs() > bound
+        assert not bool(bad.any()), (name, int(bad.sum()), float(((gg - r).abs() / rms).max()))
 
 
 def test_trained_control_variate_is_unbiased_and_reduces_variance(cuda):

@@ -106,6 +106,43 @@ def test_sobol_full_scale_permutation_property(cuda):
     assert torch.all((x * x).sum(dim=0) == n * (n + 1) * (2 * n + 1) // 6)
 
 
+@pytest.mark.parametrize("chunk_start", [0, 2 ** 25, 2 ** 26 - 2 ** 20])
+def test_sobol_dim1024_2pow26_chunks_bit_exact(cuda, chunk_start):
+    """Dimension 1024, 2^26 points (nd = 27 for the whole set), generated in
+    chunks of 2^20 points with the global nd, exactly as the throughput
+    measurement launches them: 4,096 rows of each chunk (its first, middle and
+    last 1,024 rows and 1,024 rows from a seeded random offset) checked bit for
+    bit against the oracle's integers, for the uint32 and float32 outputs;
+    the inverse-normal output within the float32 erfinv tolerance."""
+    import tqf._lib as L
+    from tqf.math.random import sobol
+    dim, total, chunk = 1024, 2 ** 26, 2 ** 20
+    nd = sobol.num_digits(total, 0)
+    assert nd == 27
+    v = sobol.device_direction_numbers(dim, cuda)
+    out = torch.empty((chunk, dim), dtype=torch.int32, device=cuda)
+    m = osobol.compute_direction_numbers(dim)
+    offs = [0, chunk // 2, chunk - 1024, int(np.random.default_rng(chunk_start + 1).integers(1024, chunk - 2048))]
+    want_int = {o: osobol.sample_int(dim, 1024, chunk_start + o, nd=nd, m=m) for o in offs}
+    rows = torch.cat([torch.arange(o, o + 1024) for o in offs]).to(cuda)
+    for kind in (L.SOBOL_U32, L.SOBOL_F32, L.SOBOL_NORMAL_F32):
+        out.fill_(-1)
+        L.call("tqf_sobol_sample", v.data_ptr(), dim, chunk, chunk_start, nd, kind, out.data_ptr(), L.stream_ptr())
+        got = out.index_select(0, rows).cpu().numpy()
+        for i, o in enumerate(offs):
+            g = got[i * 1024:(i + 1) * 1024]
+            w = want_int[o]
+            if kind == L.SOBOL_U32:
+                np.testing.assert_array_equal(g.view(np.uint32), w.astype(np.uint32))
+            else:
+                u = (w.astype(np.float32) / np.float32(2.0 ** nd)).astype(np.float32)
+                if kind == L.SOBOL_F32:
+                    np.testing.assert_array_equal(g.view(np.float32), u)
+                else:
+                    np.testing.assert_allclose(g.view(np.float32), osobol.normal_from_uniform(u), rtol=2e-6,
+                                               atol=2e-6)
+
+
 def test_sobol_2pow26_reference_rounding(cuda):
     # At 2^26 points the reference's float32 output reaches exactly 1.0.
     from tqf.math.random import sobol

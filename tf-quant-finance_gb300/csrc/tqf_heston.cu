@@ -23,8 +23,12 @@ constexpr int kQeCols = 12;
 constexpr size_t kMaxStagedTable = 96 * 1024;
 
 struct SmemLayout {
-  size_t bar, table, acc, spot, strike, call, stage, total;
+  size_t bar, table, acc, spot, strike, call, stage, sobol, total;
 };
+
+// In-kernel Sobol draws: tables for this many steps (two dimensions each)
+// are built per window (SobolTables).
+constexpr int kSobolWindow = 64;
 
 // Recorded states are staged in shared memory, kStage<T> consecutive slots
 // (128 bytes of a path's output row) per flush; see SlotStager.
@@ -32,7 +36,7 @@ template <typename T>
 constexpr int kStage = 128 / (2 * (int)sizeof(T));
 
 template <typename T>
-SmemLayout smem_layout(int steps, int cols, int ns, bool staged, bool store) {
+SmemLayout smem_layout(int steps, int cols, int ns, bool staged, bool store, bool sobol = false) {
   SmemLayout L;
   size_t off = 0;
   L.bar = off;
@@ -53,6 +57,9 @@ SmemLayout smem_layout(int steps, int cols, int ns, bool staged, bool store) {
   off = (off + 15) & ~(size_t)15;
   L.stage = off;
   if (store) off += (size_t)kStage<T> * (kBlock + 1) * 2 * sizeof(T);
+  off = (off + 15) & ~(size_t)15;
+  L.sobol = off;
+  if (sobol) off += (size_t)2 * kSobolWindow * SobolTables::kRow * sizeof(uint32_t);
   L.total = (off + 15) & ~(size_t)15;
   return L;
 }
@@ -267,7 +274,10 @@ __global__ void __launch_bounds__(kBlock)
     // its output is dropped
     const int64_t pc = valid ? path : N - 1;
     T x = x0, v = v0;
-    if (valid || STORE) {
+    // In-kernel Sobol draws build shared tables per window (CTA barriers),
+    // so every thread runs the steps; a thread past the last path takes the
+    // next point index and its result is dropped.
+    if (valid || STORE || SRC == TQF_DRAWS_SOBOL) {
       if (STORE && a.output.init_slot >= 0) stg.put(a.output, row0, N, a.output.init_slot, x, v);
       if (SRC == TQF_DRAWS_PHILOX && sizeof(T) == 4) {
         // Canonical stream, 2 normals per step: block b = steps 2b, 2b+1.
@@ -349,6 +359,37 @@ __global__ void __launch_bounds__(kBlock)
           float z0, z1;
           box_muller_f32(r.x, r.y, z0, z1);
           one_step(i, z0, z1);
+        }
+      } else if constexpr (SRC == TQF_DRAWS_SOBOL) {
+        const uint32_t* sv = static_cast<const uint32_t*>(a.draws.ptr);
+        const int nd = (int)a.draws.key0;
+        const uint32_t i0 = (uint32_t)(a.draws.path_offset + 1 + row0);
+        const uint32_t ip = i0 + threadIdx.x;
+        const int lo = (int)(ip & 15u), mid = 16 + (int)((ip >> 4) & 15u);
+        const int hi = 32 + (int)((ip >> 8) - (i0 >> 8));
+        uint32_t* tabs = reinterpret_cast<uint32_t*>(smem + L.sobol);
+        T sc;
+        if constexpr (sizeof(T) == 4) sc = __uint_as_float((uint32_t)(127 - nd) << 23);
+        else sc = ldexp(1.0, -nd);
+        for (int s0 = 0; s0 < steps; s0 += kSobolWindow) {
+          const int nw = steps - s0 < kSobolWindow ? steps - s0 : kSobolWindow;
+          __syncthreads();
+          SobolTables::build(tabs, sv, 2 * s0, 2 * nw, i0, nd);
+          __syncthreads();
+#pragma unroll 2
+          for (int s = 0; s < nw; ++s) {
+            const uint32_t* t0 = tabs + 2 * s * SobolTables::kRow;
+            const uint32_t* t1 = t0 + SobolTables::kRow;
+            const T z0 = sobol_normal(t0[lo] ^ t0[mid] ^ t0[hi], sc);
+            const T z1 = sobol_normal(t1[lo] ^ t1[mid] ^ t1[hi], sc);
+            const T* r0 = table + (size_t)(s0 + s) * COLS;
+            if (SCHEME == 0) ft_step<T>(r0, z0, z1, x, v);
+            else qe_step<T>(r0, z0, z1, x, v);
+            if (STORE) {
+              const int slot = (int)r0[COLS - 1];
+              if (slot >= 0) stg.put(a.output, row0, N, slot, x, v);
+            }
+          }
         }
       } else {
         DrawSource<T> src(a.draws, pc, 2);
@@ -606,6 +647,7 @@ KernelFn<T, SCHEME> pick(bool store, bool price) {
 
 template <typename T, int SCHEME>
 KernelFn<T, SCHEME> pick_kernel(int src, bool store, bool price, bool anti = false) {
+  if (src == TQF_DRAWS_SOBOL) return pick<T, SCHEME, TQF_DRAWS_SOBOL, false>(store, price);
   if (src != TQF_DRAWS_PHILOX) return pick<T, SCHEME, TQF_DRAWS_MEMORY, false>(store, price);
   return anti ? pick<T, SCHEME, TQF_DRAWS_PHILOX, true>(store, price)
               : pick<T, SCHEME, TQF_DRAWS_PHILOX, false>(store, price);
@@ -615,7 +657,7 @@ template <typename T, int SCHEME>
 int grid_for(int64_t N, int ns, int steps, bool staged, int src, bool store, bool price,
              SmemLayout* out_layout, bool anti = false) {
   const int cols = SCHEME == 0 ? kFtCols : kQeCols;
-  SmemLayout L = smem_layout<T>(steps, cols, price ? ns : 0, staged, store);
+  SmemLayout L = smem_layout<T>(steps, cols, price ? ns : 0, staged, store, src == TQF_DRAWS_SOBOL);
   if (out_layout) *out_layout = L;
   auto k = pick_kernel<T, SCHEME>(src, store, price, anti);
   set_smem_config(k, L.total);
@@ -664,8 +706,19 @@ int validate(const tqf_heston_args* a, const char* who) {
   TQF_REQUIRE(a->num_steps >= 0, "%s: num_steps must be >= 0", who);
   TQF_REQUIRE(a->num_steps == 0 || a->step_table != nullptr, "%s: null step_table", who);
   TQF_REQUIRE((reinterpret_cast<uintptr_t>(a->step_table) & 15u) == 0, "%s: step_table must be 16-byte aligned", who);
-  TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.source == TQF_DRAWS_MEMORY,
+  TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.source == TQF_DRAWS_MEMORY ||
+                  a->draws.source == TQF_DRAWS_SOBOL,
               "%s: bad draws.source %d", who, a->draws.source);
+  if (a->draws.source == TQF_DRAWS_SOBOL) {
+    TQF_REQUIRE(a->draws.ptr != nullptr, "%s: Sobol draws need the direction numbers in draws.ptr", who);
+    TQF_REQUIRE(a->draws.key1 == 2, "%s: Sobol draws need key1 = 2 normals per step, got %u", who, a->draws.key1);
+    TQF_REQUIRE(a->draws.key0 >= 1 && a->draws.key0 <= 32, "%s: Sobol nd (key0) must be in [1, 32]", who);
+    TQF_REQUIRE(!a->draws.antithetic, "%s: Sobol draws have no antithetic form", who);
+    TQF_REQUIRE(a->draws.path_offset >= 0 && a->draws.path_offset + a->num_paths <= 2147483647LL,
+                "%s: Sobol point indices must stay below 2^31", who);
+    TQF_REQUIRE(a->draws.path_offset + a->num_paths < (1LL << a->draws.key0),
+                "%s: Sobol point indices must fit in nd = %u digits", who, a->draws.key0);
+  }
   TQF_REQUIRE(a->draws.source != TQF_DRAWS_MEMORY || a->num_steps == 0 || a->draws.ptr != nullptr,
               "%s: memory draws need draws.ptr", who);
   TQF_REQUIRE(!a->draws.antithetic || 2 * a->draws.antithetic_half == a->num_paths,

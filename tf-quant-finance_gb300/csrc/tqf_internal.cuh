@@ -400,6 +400,69 @@ struct PhiloxReader<double> {
   }
 };
 
+// ---- Sobol normals ------------------------------------------------------------
+// Inverse-normal conversion of a Sobol integer x at nd digits (sc = 2^-nd):
+// u = float(x) sc, z = sqrt(2) erfinv((u - 1/2) 2) in the output's precision
+// (tff/math/random_ops/multivariate_normal.py:420).  The Sobol kernels and
+// the fused Sobol draws of the path kernels share these, so materialised and
+// fused draws agree bit for bit.
+__device__ __forceinline__ float sobol_normal_f32(uint32_t x, float sc) {
+  const float u = __fmul_rn(__uint2float_rn(x), sc);
+  return __fmul_rn(erfinvf(__fmul_rn(__fsub_rn(u, 0.5f), 2.0f)), 1.41421353816986083984375f);
+}
+__device__ __forceinline__ double sobol_normal_f64(uint32_t x, double sc) {
+  const double u = __dmul_rn((double)x, sc);
+  return __dmul_rn(erfinv(__dmul_rn(__dsub_rn(u, 0.5), 2.0)), 1.4142135623730951);
+}
+__device__ __forceinline__ float sobol_normal(uint32_t x, float sc) { return sobol_normal_f32(x, sc); }
+__device__ __forceinline__ double sobol_normal(uint32_t x, double sc) { return sobol_normal_f64(x, sc); }
+
+// Sobol integers of a CTA's tile of 256 consecutive point indices, for a
+// window of draw dimensions, from shared-memory tables.  Point i's integer in
+// dimension k is XOR_j bit_j(i) v_kj >> (32 - nd) (sobol_impl.py:128-157);
+// split i into bits 0-3, 4-7 and the rest: row k of the tables holds
+//   [0, 16):  XOR of v_kj, j in 0..3, over the set bits of each 4-bit value,
+//   [16, 32): the same for j in 4..7,
+//   32, 33:   the XOR over bits >= 8 of the two 256-blocks the tile touches
+// (its indices i0 .. i0 + 255 span at most two), so a thread reads three
+// words per draw: T[lo4] ^ T[16 + mid4] ^ T[32 + block].  Within a warp
+// the lo4 reads hit 16 consecutive words and the other two at most three
+// distinct words, so the reads are conflict-free.  The tables of a window
+// are rebuilt per tile (the high part depends on it); the build is ~2 jobs
+// per thread per window, against ~100 instructions per path-step.
+struct SobolTables {
+  static constexpr int kRow = 34;
+  // cooperative build of dimensions k0 .. k0 + nk - 1; the caller brackets it
+  // with __syncthreads (tables of the previous window may still be in use)
+  static __device__ __forceinline__ void build(uint32_t* tabs, const uint32_t* __restrict__ v, int k0, int nk,
+                                               uint32_t i0, int nd) {
+    const int sh = 32 - nd;
+    const uint32_t hA = i0 & ~255u, hB = hA + 256u;
+    for (int job = threadIdx.x; job < 3 * nk; job += blockDim.x) {
+      const int kk = job / 3, t = job - 3 * kk;
+      const uint32_t* vk = v + (size_t)(k0 + kk) * 32;
+      uint32_t* row = tabs + kk * kRow;
+      if (t < 2) {
+        const uint32_t b0 = vk[4 * t] >> sh, b1 = vk[4 * t + 1] >> sh;
+        const uint32_t b2 = vk[4 * t + 2] >> sh, b3 = vk[4 * t + 3] >> sh;
+        uint32_t* o = row + 16 * t;
+#pragma unroll
+        for (int e = 0; e < 16; ++e)
+          o[e] = ((e & 1) ? b0 : 0u) ^ ((e & 2) ? b1 : 0u) ^ ((e & 4) ? b2 : 0u) ^ ((e & 8) ? b3 : 0u);
+      } else {
+        uint32_t xa = 0u, xb = 0u;
+        for (int j = 8; j < nd; ++j) {
+          const uint32_t vj = vk[j] >> sh;
+          if ((hA >> j) & 1u) xa ^= vj;
+          if ((hB >> j) & 1u) xb ^= vj;
+        }
+        row[32] = xa;
+        row[33] = xb;
+      }
+    }
+  }
+};
+
 // Per-path view of a tqf_draws block: resolves antithetic pairing and the
 // global path index once, then serves draws by (step, component).
 template <typename T>

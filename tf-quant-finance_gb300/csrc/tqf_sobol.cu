@@ -35,18 +35,12 @@ struct SobolOut<TQF_SOBOL_F64> {
 template <>
 struct SobolOut<TQF_SOBOL_NORMAL_F32> {
   using T = float;
-  __device__ static T conv(uint32_t x, float sc, double) {
-    const float u = __fmul_rn(__uint2float_rn(x), sc);
-    return __fmul_rn(erfinvf(__fmul_rn(__fsub_rn(u, 0.5f), 2.0f)), 1.41421353816986083984375f);
-  }
+  __device__ static T conv(uint32_t x, float sc, double) { return sobol_normal_f32(x, sc); }
 };
 template <>
 struct SobolOut<TQF_SOBOL_NORMAL_F64> {
   using T = double;
-  __device__ static T conv(uint32_t x, float, double sc) {
-    const double u = (double)x * sc;
-    return erfinv((u - 0.5) * 2.0) * 1.4142135623730951;
-  }
+  __device__ static T conv(uint32_t x, float, double sc) { return sobol_normal_f64(x, sc); }
 };
 template <>
 struct SobolOut<TQF_SOBOL_F32_CENTERED> {

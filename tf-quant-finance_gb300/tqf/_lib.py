@@ -30,6 +30,7 @@ TQF_F32 = 0
 TQF_F64 = 1
 DRAWS_MEMORY = 0
 DRAWS_PHILOX = 1
+DRAWS_SOBOL = 2
 
 SOBOL_U32 = 0
 SOBOL_F32 = 1

@@ -78,6 +78,26 @@ def philox_draws(random_type, seed, num_paths: int, path_offset: int = 0) -> _li
     return d
 
 
+def sobol_draws(num_normal_draws: int, num_time_steps: int, num_paths: int, skip: int = 0,
+                device: torch.device | None = None):
+    """(tqf_draws, direction numbers to keep alive) for Sobol normals computed
+    inside the path kernel: the SOBOL branch of generate_mc_normal_draws
+    (tff/models/utils.py:95-127) for `num_paths` paths, point skip + 1 + n,
+    dimension step * num_normal_draws + c, nd digits of the whole request."""
+    from tqf.math.random import sobol
+    device = device or _lib.require_cuda()
+    dim = max(int(num_normal_draws) * int(num_time_steps), 1)
+    sobol._validate(dim, int(num_paths), int(skip), False)
+    v = sobol.device_direction_numbers(dim, device)
+    d = _lib.Draws()
+    d.source = _lib.DRAWS_SOBOL
+    d.ptr = v.data_ptr()
+    d.key0 = sobol.num_digits(int(num_paths), int(skip))
+    d.key1 = int(num_normal_draws)
+    d.path_offset = int(skip)
+    return d, v
+
+
 def memory_draws(draws: torch.Tensor, path_axis: int, step_axis: int) -> _lib.Draws:
     """tqf_draws block reading a 3-D tensor in place (any layout, any strides)."""
     d = _lib.Draws()

@@ -124,7 +124,12 @@ class HestonModel(GenericItoProcess):
                 raise InvalidArgumentError(
                     f"normal_draws cover {draws_t.shape[-2]} time steps, the grid needs {steps_exec}")
             draws = mvn.memory_draws(draws_t, path_axis=0, step_axis=1)
-        elif random_type in (RandomType.SOBOL, RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
+        elif random_type == RandomType.SOBOL:
+            # Sobol normals computed inside the kernel, equal to the
+            # materialised generate_mc_normal_draws(2, steps_total, ...) bit for bit
+            draws, v = mvn.sobol_draws(2, steps_total, int(num_samples), skip, device)
+            keep_alive.append(v)
+        elif random_type in (RandomType.HALTON, RandomType.HALTON_RANDOMIZED):
             sob = utils.generate_mc_normal_draws(2, steps_total, int(num_samples), random_type, skip=skip, seed=seed,
                                                  dtype=td)
             keep_alive.append(sob)

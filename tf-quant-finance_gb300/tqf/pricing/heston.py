@@ -36,14 +36,17 @@ def _table(key, build, td, device):
 _QUASI = (RandomType.SOBOL, RandomType.HALTON, RandomType.HALTON_RANDOMIZED)
 
 
-def _draws(random_type, seed, num_paths, num_steps, path_offset, normal_draws, td):
+def _draws(random_type, seed, num_paths, num_steps, path_offset, normal_draws, td, fused_sobol=True):
     """(tqf_draws, tensor to keep alive): caller draws [N, steps, 2] read in
-    place; SOBOL / HALTON* as [steps, N, 2] normal draws generated on the
-    device (dimension step * 2 + component, points path_offset + 1 ... as in
-    generate_mc_normal_draws with skip = path_offset); otherwise the Philox
-    stream generated inside the kernel."""
+    place; SOBOL computed inside the pricing kernel (dimension step * 2 +
+    component, points path_offset + 1 ..., the values of
+    generate_mc_normal_draws with skip = path_offset); HALTON* (and SOBOL
+    for the adjoint) as [steps, N, 2] normal draws generated on the device;
+    otherwise the Philox stream generated inside the kernel."""
     if normal_draws is not None:
         return mvn.memory_draws(normal_draws, path_axis=0, step_axis=1), normal_draws
+    if random_type == RandomType.SOBOL and fused_sobol:
+        return mvn.sobol_draws(2, num_steps, num_paths, int(path_offset))
     if random_type in _QUASI:
         q = utils.generate_mc_normal_draws(2, num_steps, num_paths, random_type, skip=int(path_offset), seed=seed,
                                            dtype=td)
@@ -142,7 +145,7 @@ def heston_european_vjp(grad_prices, *, strikes, expiry, spot, variance, mean_re
     calls = None
     if is_call_options is not None:
         calls = torch.as_tensor(np.broadcast_to(np.asarray(is_call_options, np.uint8), (ns,)).copy()).to(device)
-    draws, draws_keep = _draws(random_type, seed, N, steps, path_offset, normal_draws, td)
+    draws, draws_keep = _draws(random_type, seed, N, steps, path_offset, normal_draws, td, fused_sobol=False)
     out = torch.zeros(7, dtype=torch.float64, device=device)
     from tqf.pricing.european import workspace
     ws = workspace(int(_lib.load().tqf_heston_adjoint_workspace_bytes(N)), device, "heston_adjoint")
