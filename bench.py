@@ -546,6 +546,27 @@ def run_basket(paths_n=1 << 22, price_paths=1 << 22, n_steps=64, reps=10):
     sec = time.perf_counter() - t0
     res["basket_price"] = {"paths": price_paths, "price": b.price, "se": b.standard_error,
                            "wall_seconds_incl_host": sec, "path_steps_per_s": price_paths * n_steps / sec}
+    # 64 assets: L z on the tensor cores with K and N tiled in 16s (four
+    # K = 16 instructions per product) against the one-warp-per-path CUDA-core
+    # kernel; [2^20, 64, 64] float32 output (17.2 GB written per call).
+    d64, p64 = 64, paths_n // 4
+    rng = np.random.default_rng(64)
+    vols64 = rng.uniform(0.1, 0.4, d64)
+    q, _ = np.linalg.qr(rng.standard_normal((d64, d64)))
+    c = q @ np.diag(rng.uniform(0.1, 2.0, d64)) @ q.T
+    s = np.sqrt(np.diag(c))
+    proc64 = MultivariateGeometricBrownianMotion(d64, means=0.02, volatilities=vols64, corr_matrix=c / np.outer(s, s),
+                                                 dtype=np.float32)
+    bytes64 = p64 * n_steps * d64 * 4
+    res["assets64"] = {"config": f"64 assets, {p64} paths x {n_steps} dates, FP32, Philox"}
+    for mode, tag in [(0, "tensor_core_lz"), (1, "cuda_core_lz")]:
+        launch, out = proc64.paths_launcher(times, initial_state=np.full(d64, 100.0, np.float32), num_samples=p64,
+                                            random_type=RandomType.STATELESS, seed=[3, 4], lz_mode=mode)
+        sec = timed(launch)
+        res["assets64"][f"paths_{tag}"] = {"seconds": sec, "path_steps_per_s": p64 * n_steps / sec,
+                                           "store_gbs": bytes64 / sec / 1e9}
+        del out
+    torch.cuda.empty_cache()
     return res
 
 

@@ -539,12 +539,13 @@ typedef struct tqf_mvgbm_args {
   tqf_draws draws;
   tqf_path_output output;
   int32_t* dev_status;
-  int32_t lz_mode; /* 0: tensor-core split-BF16 L z when dim == 16 (float32), else CUDA cores; 1: CUDA cores */
+  int32_t lz_mode; /* 0: tensor-core split-BF16 L z for 16 <= dim <= 64 (float32), else CUDA cores; 1: CUDA cores */
   int32_t pad0;
 } tqf_mvgbm_args;
 
 /* FP64 Cholesky factor L (row-major, lower) of an n x n symmetric positive
- * definite matrix, n <= 64, on the GPU in one CTA (replaces
+ * definite matrix (any n; shared memory up to n = 64, global memory beyond),
+ * on the GPU in one CTA (replaces
  * tf.linalg.cholesky at multivariate_geometric_brownian_motion.py:264 and
  * multivariate_normal.py:436).  *info (device int) = 0 on success, k + 1
  * when the k-th pivot is not positive. */

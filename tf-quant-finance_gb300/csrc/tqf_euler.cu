@@ -161,6 +161,167 @@ __global__ void __launch_bounds__(kBlock) euler_update_kernel(tqf_euler_update_a
   }
 }
 
+// ---- any dimension: one warp per path ---------------------------------------
+// For dim > 16 the state no longer fits a thread's registers.  A warp carries
+// one path: lane l owns state rows r = l, l + 32, ...; each step the warp
+// writes its scaled draws dw = z sqrt(dt) and its state into per-warp shared
+// buffers, every lane forms its rows' drift m_r + sum_c M_rc x_c and
+// y_r = sum_c C_rc dw_c (M and C stored transposed, so the lanes of a warp
+// read consecutive words; summed in column order as the register kernel
+// does), and writes x'_r = x_r + dt drift + (s0_r + s1_r x_r) y_r into the
+// second state buffer.  Recorded rows are stored by consecutive lanes, i.e.
+// coalesced.  Coefficients sit in shared memory when they fit
+// (kWideCoefSmem), else they are read from global memory (L2-resident).
+constexpr int kWideWarps = kBlock / 32;
+constexpr size_t kWideCoefSmem = 96 * 1024;
+
+template <typename T>
+size_t wide_coef_bytes(int dim) {
+  return ((size_t)2 * dim * dim + 3 * (size_t)dim) * sizeof(T);
+}
+template <typename T>
+size_t wide_warp_bytes(int dim) {
+  return (size_t)3 * dim * sizeof(T);
+}
+
+// CS: coefficients copied (M and C transposed) into shared memory; else read
+// row-major from global memory.
+template <typename T, int SRC, bool CS>
+__global__ void __launch_bounds__(kBlock) euler_affine_wide_kernel(tqf_euler_affine_args a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int dim = a.dim;
+  const size_t dd = (size_t)dim * dim;
+  const T* gM = static_cast<const T*>(a.drift_M);
+  const T* gC = static_cast<const T*>(a.vol_C);
+  const T* m = static_cast<const T*>(a.drift_m);
+  const T* s0 = static_cast<const T*>(a.vol_s0);
+  const T* s1 = static_cast<const T*>(a.vol_s1);
+  T* cs = reinterpret_cast<T*>(smem);
+  size_t off = 0;
+  if (CS) {
+    // cs = Mt [dim][dim] (Mt[c][r] = M[r][c]), Ct, m, s0, s1
+    for (size_t i = threadIdx.x; i < dd; i += kBlock) {
+      const size_t r = i / dim, c = i - r * dim;
+      cs[c * dim + r] = gM[i];
+      cs[dd + c * dim + r] = gC[i];
+    }
+    for (int i = threadIdx.x; i < dim; i += kBlock) {
+      cs[2 * dd + i] = m[i];
+      cs[2 * dd + dim + i] = s0[i];
+      cs[2 * dd + 2 * dim + i] = s1[i];
+    }
+    m = cs + 2 * dd;
+    s0 = m + dim;
+    s1 = s0 + dim;
+    off = ((2 * dd + 3 * (size_t)dim) * sizeof(T) + 15) & ~(size_t)15;
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* xs = reinterpret_cast<T*>(smem + off) + (size_t)warp * 3 * dim;
+  T* xn = xs + dim;
+  T* dws = xn + dim;
+  __syncthreads();
+  const T* table = static_cast<const T*>(a.step_table);
+  T* out = static_cast<T*>(a.output.ptr);
+  const int ns = a.output.num_slots;
+  const int64_t N = a.num_paths;
+  const int64_t nwarps = (int64_t)gridDim.x * kWideWarps;
+  for (int64_t path = (int64_t)blockIdx.x * kWideWarps + warp; path < N; path += nwarps) {
+    const T* x0 = static_cast<const T*>(a.x0) + (a.x0_per_path ? path * dim : 0);
+    for (int r = lane; r < dim; r += 32) xs[r] = x0[r];
+    if (out && a.output.init_slot >= 0) {
+      T* o = out + (path * ns + a.output.init_slot) * dim;
+      for (int r = lane; r < dim; r += 32) o[r] = xs[r];
+    }
+    DrawSource<T> src(a.draws, path, dim);
+    for (int i = 0; i < a.num_steps; ++i) {
+      const T* row = table + (size_t)i * kCols;
+      const T dt = row[0], sdt = row[1];
+      const int slot = (int)row[2];
+      for (int c = lane; c < dim; c += 32) dws[c] = src.get(i, c) * sdt;
+      __syncwarp();
+      for (int r = lane; r < dim; r += 32) {
+        T drift = m[r];
+        T y = T(0);
+        for (int c = 0; c < dim; ++c) {
+          const T mv = CS ? cs[(size_t)c * dim + r] : gM[(size_t)r * dim + c];
+          const T cv = CS ? cs[dd + (size_t)c * dim + r] : gC[(size_t)r * dim + c];
+          drift += mv * xs[c];
+          y += cv * dws[c];
+        }
+        const T vol = s0[r] + s1[r] * xs[r];
+        xn[r] = xs[r] + dt * drift + vol * y;
+      }
+      __syncwarp();
+      T* t = xs;
+      xs = xn;
+      xn = t;
+      if (out && slot >= 0) {
+        T* o = out + (path * ns + slot) * dim;
+        for (int r = lane; r < dim; r += 32) o[r] = xs[r];
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// One Euler step, any dimension: one warp per path; the scaled draws go to a
+// per-warp shared buffer, then for each row r the warp reads B[r][:]
+// coalesced, reduces y_r = sum_c B_rc dw_c across its lanes and lane r % 32
+// writes x + dt a + y.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) euler_update_wide_kernel(tqf_euler_update_args a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int dim = a.dim;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* dws = reinterpret_cast<T*>(smem) + (size_t)warp * dim;
+  const int64_t path = (int64_t)blockIdx.x * kWideWarps + warp;
+  if (path >= a.num_paths) return;
+  const T* x = static_cast<const T*>(a.x) + path * dim;
+  const T* drift = static_cast<const T*>(a.drift) + path * dim;
+  const T* vol = static_cast<const T*>(a.vol) + path * (int64_t)dim * dim;
+  const T dt = (T)a.dt, sdt = (T)a.sqrt_dt;
+  DrawSource<T> src(a.draws, path, dim);
+  for (int c = lane; c < dim; c += 32) dws[c] = src.get(a.step, c) * sdt;
+  __syncwarp();
+  T* xn = static_cast<T*>(a.x_next) + path * dim;
+  T* po = a.paths_out && a.out_slot >= 0
+              ? static_cast<T*>(a.paths_out) + (path * a.num_slots + a.out_slot) * dim
+              : nullptr;
+  for (int r = 0; r < dim; ++r) {
+    T y = T(0);
+    for (int c = lane; c < dim; c += 32) y += vol[(size_t)r * dim + c] * dws[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+    if (lane == (r & 31)) {
+      const T v = x[r] + dt * drift[r] + y;
+      xn[r] = v;
+      if (po) po[r] = v;
+    }
+  }
+}
+
+template <typename T>
+int launch_affine_wide(const tqf_euler_affine_args& a, cudaStream_t s) {
+  const int dim = a.dim;
+  const size_t cbytes = (wide_coef_bytes<T>(dim) + 15) & ~(size_t)15;
+  const bool cs = cbytes <= kWideCoefSmem;
+  const size_t smem = (cs ? cbytes : 0) + kWideWarps * wide_warp_bytes<T>(dim);
+  TQF_REQUIRE(smem <= 200 * 1024, "tqf_euler_affine: dim %d needs %zu bytes of shared memory (max 200 KiB)", dim,
+              smem);
+  const bool philox = a.draws.source == TQF_DRAWS_PHILOX;
+  void (*k)(tqf_euler_affine_args) =
+      cs ? (philox ? euler_affine_wide_kernel<T, TQF_DRAWS_PHILOX, true> : euler_affine_wide_kernel<T, TQF_DRAWS_MEMORY, true>)
+         : (philox ? euler_affine_wide_kernel<T, TQF_DRAWS_PHILOX, false> : euler_affine_wide_kernel<T, TQF_DRAWS_MEMORY, false>);
+  set_smem_config(k, smem);
+  int occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem) != cudaSuccess || occ < 1) occ = 1;
+  int64_t grid = (a.num_paths + kWideWarps - 1) / kWideWarps;
+  const int64_t cap = (int64_t)num_sms() * occ;
+  if (grid > cap) grid = cap;
+  k<<<(unsigned)grid, kBlock, smem, s>>>(a);
+  return check_launch("euler_affine_wide_kernel");
+}
+
 template <typename T, int DM>
 int launch_affine(const tqf_euler_affine_args& a, cudaStream_t s) {
   const size_t tab_bytes = (size_t)a.num_steps * kCols * sizeof(T);
@@ -194,11 +355,22 @@ int dispatch_affine(const tqf_euler_affine_args& a, cudaStream_t s) {
   if (a.dim <= 2) return launch_affine<T, 2>(a, s);
   if (a.dim <= 4) return launch_affine<T, 4>(a, s);
   if (a.dim <= 8) return launch_affine<T, 8>(a, s);
-  return launch_affine<T, 16>(a, s);
+  if (a.dim <= 16) return launch_affine<T, 16>(a, s);
+  return launch_affine_wide<T>(a, s);
 }
 
 template <typename T>
 int dispatch_update(const tqf_euler_update_args& a, cudaStream_t s) {
+  if (a.dim > 16) {
+    const int64_t grid = (a.num_paths + kWideWarps - 1) / kWideWarps;
+    TQF_REQUIRE(grid <= 2147483647LL, "tqf_euler_update: too many paths");
+    const size_t smem = (size_t)kWideWarps * a.dim * sizeof(T);
+    TQF_REQUIRE(smem <= 200 * 1024, "tqf_euler_update: dim %d too large (max %d)", a.dim,
+                (int)(200 * 1024 / (kWideWarps * sizeof(T))));
+    set_smem_config(euler_update_wide_kernel<T>, smem);
+    euler_update_wide_kernel<T><<<(unsigned)grid, kBlock, smem, s>>>(a);
+    return check_launch("euler_update_wide_kernel");
+  }
   const int64_t grid = (a.num_paths + kBlock - 1) / kBlock;
   TQF_REQUIRE(grid <= 2147483647LL, "tqf_euler_update: too many paths");
   if (a.dim <= 1) euler_update_kernel<T, 1><<<(unsigned)grid, kBlock, 0, s>>>(a);
@@ -218,7 +390,7 @@ extern "C" int tqf_euler_affine(const tqf_euler_affine_args* a, void* stream) {
   clear_error();
   TQF_REQUIRE(a != nullptr, "tqf_euler_affine: null args");
   TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "tqf_euler_affine: bad dtype %d", a->dtype);
-  TQF_REQUIRE(a->dim >= 1 && a->dim <= 16, "tqf_euler_affine: dim must be in [1, 16], got %d", a->dim);
+  TQF_REQUIRE(a->dim >= 1, "tqf_euler_affine: dim must be >= 1, got %d", a->dim);
   TQF_REQUIRE(a->num_paths >= 1 && a->num_steps >= 0, "tqf_euler_affine: bad sizes");
   TQF_REQUIRE(a->x0 && a->drift_m && a->drift_M && a->vol_s0 && a->vol_s1 && a->vol_C,
               "tqf_euler_affine: null coefficient pointer");
@@ -237,7 +409,7 @@ extern "C" int tqf_euler_update(const tqf_euler_update_args* a, void* stream) {
   clear_error();
   TQF_REQUIRE(a != nullptr, "tqf_euler_update: null args");
   TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "tqf_euler_update: bad dtype %d", a->dtype);
-  TQF_REQUIRE(a->dim >= 1 && a->dim <= 16, "tqf_euler_update: dim must be in [1, 16], got %d", a->dim);
+  TQF_REQUIRE(a->dim >= 1, "tqf_euler_update: dim must be >= 1, got %d", a->dim);
   TQF_REQUIRE(a->num_paths >= 1, "tqf_euler_update: num_paths must be >= 1");
   TQF_REQUIRE(a->x && a->drift && a->vol && a->x_next, "tqf_euler_update: null pointer");
   TQF_REQUIRE(a->draws.source == TQF_DRAWS_PHILOX || a->draws.ptr,

@@ -243,6 +243,18 @@ __global__ void __launch_bounds__(kBlock)
   // Philox block in f32x2 arithmetic from the staged table's pair blocks.
   constexpr bool kPairable = SCHEME == 0 && SRC == TQF_DRAWS_PHILOX && sizeof(T) == 4;
   const bool paired = kPairable && staged;
+  // With in-kernel Sobol draws, a staged full-truncation table whose rows
+  // are all equal (a uniform grid with constant parameters and no recorded
+  // steps: the pricing calls) is read once into registers instead of once
+  // per step; rows are compared bit for bit, so the arithmetic is unchanged.
+  bool uniform = false;
+  if (SCHEME == 0 && SRC == TQF_DRAWS_SOBOL && staged && !STORE) {
+    int same = 1;
+    const uint32_t* tw = reinterpret_cast<const uint32_t*>(table);
+    constexpr int W = COLS * (int)sizeof(T) / 4;
+    for (int idx = threadIdx.x; idx < steps * W; idx += kBlock) same &= tw[idx] == tw[idx % W];
+    uniform = __syncthreads_and(same) != 0;
+  }
   if (kPairable && paired) {
     pair_ft_table(reinterpret_cast<float*>(smem + L.table), steps);
     __syncthreads();
@@ -339,6 +351,9 @@ __global__ void __launch_bounds__(kBlock)
                 }
               }
             };
+            // (the constants stay shared-memory operands even for a uniform
+            // table: holding them in registers costs this loop ~18 registers
+            // and two resident CTAs per SM, measured 15 % slower)
             const int full = steps >> 1;
 #pragma unroll 1
             for (int pb = 0; pb < full; ++pb) pair_steps(pb, true);
@@ -368,14 +383,26 @@ __global__ void __launch_bounds__(kBlock)
         const int lo = (int)(ip & 15u), mid = 16 + (int)((ip >> 4) & 15u);
         const int hi = 32 + (int)((ip >> 8) - (i0 >> 8));
         uint32_t* tabs = reinterpret_cast<uint32_t*>(smem + L.sobol);
-        T sc;
-        if constexpr (sizeof(T) == 4) sc = __uint_as_float((uint32_t)(127 - nd) << 23);
+        T sc;  // float32: 2^(1-nd) (sobol_normal_f32), float64: 2^-nd
+        if constexpr (sizeof(T) == 4) sc = __uint_as_float((uint32_t)(128 - nd) << 23);
         else sc = ldexp(1.0, -nd);
         for (int s0 = 0; s0 < steps; s0 += kSobolWindow) {
           const int nw = steps - s0 < kSobolWindow ? steps - s0 : kSobolWindow;
           __syncthreads();
           SobolTables::build(tabs, sv, 2 * s0, 2 * nw, i0, nd);
           __syncthreads();
+          if (SCHEME == 0 && uniform) {
+            const FtRow<T> row = load_ft_row<T>(table);
+#pragma unroll 2
+            for (int s = 0; s < nw; ++s) {
+              const uint32_t* t0 = tabs + 2 * s * SobolTables::kRow;
+              const uint32_t* t1 = t0 + SobolTables::kRow;
+              const T z0 = sobol_normal(t0[lo] ^ t0[mid] ^ t0[hi], sc);
+              const T z1 = sobol_normal(t1[lo] ^ t1[mid] ^ t1[hi], sc);
+              ft_step<T>(row, z0, z1, x, v);
+            }
+            continue;
+          }
 #pragma unroll 2
           for (int s = 0; s < nw; ++s) {
             const uint32_t* t0 = tabs + 2 * s * SobolTables::kRow;

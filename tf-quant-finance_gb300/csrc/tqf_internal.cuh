@@ -401,14 +401,17 @@ struct PhiloxReader<double> {
 };
 
 // ---- Sobol normals ------------------------------------------------------------
-// Inverse-normal conversion of a Sobol integer x at nd digits (sc = 2^-nd):
-// u = float(x) sc, z = sqrt(2) erfinv((u - 1/2) 2) in the output's precision
-// (tff/math/random_ops/multivariate_normal.py:420).  The Sobol kernels and
-// the fused Sobol draws of the path kernels share these, so materialised and
+// Inverse-normal conversion of a Sobol integer x at nd digits:
+// u = float(x) 2^-nd, z = sqrt(2) erfinv((u - 1/2) 2)
+// (tff/math/random_ops/multivariate_normal.py:420).  In float32,
+// (u - 1/2) 2 = fma(float(x), 2^(1-nd), -1) exactly: the product is a power-
+// of-two scaling (exact) and scaling by 2 commutes with rounding, so the one
+// rounding of the fma equals the reference's rounding of u - 1/2, doubled.
+// sc2 = 2^(1-nd) (float32), sc = 2^-nd (float64).  The Sobol kernels and the
+// fused Sobol draws of the path kernels share these, so materialised and
 // fused draws agree bit for bit.
-__device__ __forceinline__ float sobol_normal_f32(uint32_t x, float sc) {
-  const float u = __fmul_rn(__uint2float_rn(x), sc);
-  return __fmul_rn(erfinvf(__fmul_rn(__fsub_rn(u, 0.5f), 2.0f)), 1.41421353816986083984375f);
+__device__ __forceinline__ float sobol_normal_f32(uint32_t x, float sc2) {
+  return __fmul_rn(erfinvf(fmaf(__uint2float_rn(x), sc2, -1.0f)), 1.41421353816986083984375f);
 }
 __device__ __forceinline__ double sobol_normal_f64(uint32_t x, double sc) {
   const double u = __dmul_rn((double)x, sc);
@@ -451,10 +454,13 @@ struct SobolTables {
           o[e] = ((e & 1) ? b0 : 0u) ^ ((e & 2) ? b1 : 0u) ^ ((e & 4) ? b2 : 0u) ^ ((e & 8) ? b3 : 0u);
       } else {
         uint32_t xa = 0u, xb = 0u;
-        for (int j = 8; j < nd; ++j) {
-          const uint32_t vj = vk[j] >> sh;
-          if ((hA >> j) & 1u) xa ^= vj;
-          if ((hB >> j) & 1u) xb ^= vj;
+#pragma unroll
+        for (int j = 8; j < 32; ++j) {  // independent loads, predicated on j < nd
+          if (j < nd) {
+            const uint32_t vj = vk[j] >> sh;
+            xa ^= ((hA >> j) & 1u) ? vj : 0u;
+            xb ^= ((hB >> j) & 1u) ? vj : 0u;
+          }
         }
         row[32] = xa;
         row[33] = xb;

@@ -258,6 +258,189 @@ __global__ void __launch_bounds__(kBlock) milstein_update_kernel(tqf_milstein_up
     }
 }
 
+// ---- any dimension: one warp per path -----------------------------------------
+// For dim > 8 a warp carries one path.  Per step the warp writes the step's
+// normals into per-warp shared buffers (dW, xi = dW / sqrt(dt), the last mu
+// term, zeta, w = sqrt2 xi + eta), builds the Stratonovich integrals J (lane
+// l owns rows i = l, l + 32, ...; stored transposed, Jt[m][i] = J_im, so the
+// lanes of a warp touch consecutive words) with the arithmetic of
+// stratonovich_J, then each lane updates its state rows.  Coefficients are
+// read from global memory (L1/L2-resident).  Per-warp shared memory:
+// 6 d + 2 d order + 2 d^2 values.
+template <typename T>
+__host__ __device__ inline size_t mil_wide_warp_elems(int d, int order) {
+  return (size_t)6 * d + (size_t)2 * d * order + (size_t)2 * d * d;
+}
+
+template <typename T>
+struct MilWarpBufs {
+  T *x, *xn, *lev, *dw, *xi, *mu, *zeta, *w, *Jt, *Rt;
+  __device__ MilWarpBufs(T* base, int d, int order) {
+    x = base;
+    xn = x + d;
+    lev = xn + d;
+    dw = lev + d;
+    xi = dw + d;
+    mu = xi + d;
+    zeta = mu + d;
+    w = zeta + (size_t)d * order;
+    Jt = w + (size_t)d * order;
+    Rt = Jt + (size_t)d * d;
+  }
+};
+
+// Normals of `step` and the transposed J for this warp's path.
+template <typename T>
+__device__ __forceinline__ void mil_wide_draws_and_J(MilWarpBufs<T>& b, DrawSource<T>& src, int step, int d,
+                                                     int order, T dt, T sdt, T sqrt_rho, int lane) {
+  const T s2 = (T)1.4142135623730951;
+  const int p = order - 1;
+  for (int c = lane; c < d; c += 32) {
+    const T dwc = src.get(step, c) * sdt;
+    b.dw[c] = dwc;
+    b.xi[c] = dwc / sdt;
+    b.mu[c] = src.get(step, d + c * order + p);
+    for (int r = 0; r < order; ++r) {
+      b.zeta[c * order + r] = src.get(step, d + d * order + c * order + r);
+      b.w[c * order + r] = s2 * b.xi[c] + src.get(step, d + 2 * d * order + c * order + r);
+    }
+  }
+  __syncwarp();
+  const T two_pi = (T)6.283185307179586;
+  for (int i = lane; i < d; i += 32) {
+    for (int m = 0; m < d; ++m) {
+      T v;
+      if (m == i) {
+        v = b.dw[i] * b.dw[i] / T(2);
+      } else {
+        v = dt * (b.dw[i] * b.dw[m] / T(2) + sqrt_rho * (b.mu[i] * b.xi[m] - b.xi[i] * b.mu[m]));
+        T acc = T(0);
+        for (int r = 0; r < order; ++r) {
+          const T inv = T(1) / T(r + 1);
+          acc += (b.zeta[i * order + r] * b.w[m * order + r] - b.w[i * order + r] * b.zeta[m * order + r]) * inv;
+        }
+        v = v + dt * acc / two_pi;
+      }
+      b.Jt[(size_t)m * d + i] = v;
+    }
+  }
+  __syncwarp();
+}
+
+template <typename T, int SRC>
+__global__ void milstein_affine_wide_kernel(tqf_milstein_affine_args a, double rho_c) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int d = a.dim, order = a.order;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  MilWarpBufs<T> b(reinterpret_cast<T*>(smem) + (size_t)warp * mil_wide_warp_elems<T>(d, order), d, order);
+  const T* m = static_cast<const T*>(a.drift_m);
+  const T* M = static_cast<const T*>(a.drift_M);
+  const T* s0 = static_cast<const T*>(a.vol_s0);
+  const T* s1 = static_cast<const T*>(a.vol_s1);
+  const T* C = static_cast<const T*>(a.vol_C);
+  const T* table = static_cast<const T*>(a.step_table);
+  const T sqrt_rho = sqrt((T)rho_c);
+  const int K = d + 3 * d * order;
+  T* out = static_cast<T*>(a.output.ptr);
+  const int ns = a.output.num_slots;
+  const int64_t N = a.num_paths;
+  const int64_t nwarps = (int64_t)gridDim.x * wpb;
+  for (int64_t path = (int64_t)blockIdx.x * wpb + warp; path < N; path += nwarps) {
+    const T* x0 = static_cast<const T*>(a.x0) + (a.x0_per_path ? path * d : 0);
+    for (int k = lane; k < d; k += 32) b.x[k] = x0[k];
+    if (a.output.init_slot >= 0) {
+      T* o = out + (path * ns + a.output.init_slot) * d;
+      for (int k = lane; k < d; k += 32) o[k] = x0[k];
+    }
+    DrawSource<T> src(a.draws, path, K);
+    for (int i = 0; i < a.num_steps; ++i) {
+      const T dt = table[i * 4], sdt = table[i * 4 + 1];
+      const int slot = (int)table[i * 4 + 2];
+      __syncwarp();
+      for (int k = lane; k < d; k += 32) b.lev[k] = s0[k] + s1[k] * b.x[k];
+      mil_wide_draws_and_J<T>(b, src, i, d, order, dt, sdt, sqrt_rho, lane);
+      for (int k = lane; k < d; k += 32) {
+        T drift = m[k];
+        for (int c = 0; c < d; ++c) drift += M[(size_t)k * d + c] * b.x[c];
+        T u = T(0), dwi = T(0), h = T(0);
+        for (int j = 0; j < d; ++j) {
+          const T ckj = C[(size_t)k * d + j];
+          const T Bkj = b.lev[k] * ckj;
+          u += s1[k] * ckj * Bkj;
+          dwi += Bkj * b.dw[j];
+        }
+        for (int mm = 0; mm < d; ++mm) {
+          T l = T(0);  // sum_j dB_kj/dx_k B_jm
+          for (int j = 0; j < d; ++j) l += s1[k] * C[(size_t)k * d + j] * (b.lev[j] * C[(size_t)j * d + mm]);
+          h += l * b.Jt[(size_t)mm * d + k];
+        }
+        b.xn[k] = b.x[k] + dt * (drift - u) + dwi + h;
+      }
+      __syncwarp();
+      for (int k = lane; k < d; k += 32) b.x[k] = b.xn[k];
+      if (slot >= 0) {
+        T* o = out + (path * ns + slot) * d;
+        for (int k = lane; k < d; k += 32) o[k] = b.x[k];
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// One step for caller-evaluated drift, B and dB/dx (any dimension):
+// u_k = sum_{i,j} G_ikj B_ij and h_k = sum_{i,j} G_ikj R_ji with
+// R_ji = sum_m B_jm J_im (the reference's sums, regrouped so that R is formed
+// once per path-step).
+template <typename T>
+__global__ void milstein_update_wide_kernel(tqf_milstein_update_args a, double rho_c) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int d = a.dim, order = a.order;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  const int64_t path = (int64_t)blockIdx.x * wpb + warp;
+  if (path >= a.num_paths) return;
+  MilWarpBufs<T> b(reinterpret_cast<T*>(smem) + (size_t)warp * mil_wide_warp_elems<T>(d, order), d, order);
+  const int K = d + 3 * d * order;
+  const T* x = static_cast<const T*>(a.x) + path * d;
+  const T* A = static_cast<const T*>(a.drift) + path * d;
+  const T* B = static_cast<const T*>(a.vol) + path * (int64_t)d * d;
+  const T* G = static_cast<const T*>(a.grad) + path * (int64_t)d * d * d;  // [i][k][j]
+  DrawSource<T> src(a.draws, path, K);
+  const T dt = (T)a.dt, sdt = (T)a.sqrt_dt;
+  mil_wide_draws_and_J<T>(b, src, a.step, d, order, dt, sdt, sqrt((T)rho_c), lane);
+  // Rt[i][j] = R_ji = sum_m B_jm J_im, lane-owned rows i
+  for (int i = lane; i < d; i += 32)
+    for (int j = 0; j < d; ++j) {
+      T r = T(0);
+      for (int mm = 0; mm < d; ++mm) r += B[(size_t)j * d + mm] * b.Jt[(size_t)mm * d + i];
+      b.Rt[(size_t)i * d + j] = r;
+    }
+  __syncwarp();
+  T* xo = static_cast<T*>(a.x_next) + path * d;
+  T* po = a.paths_out && a.out_slot >= 0 ? static_cast<T*>(a.paths_out) + (path * a.num_slots + a.out_slot) * d
+                                          : nullptr;
+  for (int k = lane; k < d; k += 32) {
+    T u = T(0), dwi = T(0), h = T(0);
+    for (int i = 0; i < d; ++i)
+      for (int j = 0; j < d; ++j) {
+        const T g = G[((size_t)i * d + k) * d + j];
+        u += g * B[(size_t)i * d + j];
+        h += g * b.Rt[(size_t)i * d + j];
+      }
+    for (int j = 0; j < d; ++j) dwi += B[(size_t)k * d + j] * b.dw[j];
+    const T v = x[k] + dt * (A[k] - u) + dwi + h;
+    xo[k] = v;
+    if (po) po[k] = v;
+  }
+}
+
+// Warps per CTA for the wide kernels: up to 4, as shared memory allows.
+template <typename T>
+int mil_wide_warps(int d, int order) {
+  const size_t per = mil_wide_warp_elems<T>(d, order) * sizeof(T);
+  int w = (int)((200 * 1024) / (per > 0 ? per : 1));
+  return w > 4 ? 4 : w;
+}
+
 // 1/12 - sum_{r=1}^{order} r^-2 / (2 pi^2), the variance factor rho_p of the
 // truncated Fourier expansion (milstein_sampling.py:500-503).
 double rho_constant(int order) {
@@ -292,15 +475,45 @@ int launch_affine(const tqf_milstein_affine_args& a, cudaStream_t s) {
 }
 
 template <typename T>
+int launch_affine_wide(const tqf_milstein_affine_args& a, cudaStream_t s) {
+  const int wpb = mil_wide_warps<T>(a.dim, a.order);
+  TQF_REQUIRE(wpb >= 1, "tqf_milstein_affine: dim %d with order %d needs more than 200 KiB of shared memory", a.dim,
+              a.order);
+  const size_t smem = (size_t)wpb * mil_wide_warp_elems<T>(a.dim, a.order) * sizeof(T);
+  auto k = a.draws.source == TQF_DRAWS_PHILOX ? milstein_affine_wide_kernel<T, TQF_DRAWS_PHILOX>
+                                              : milstein_affine_wide_kernel<T, TQF_DRAWS_MEMORY>;
+  set_smem_config(k, smem);
+  int occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 32 * wpb, smem) != cudaSuccess || occ < 1) occ = 1;
+  int64_t grid = (a.num_paths + wpb - 1) / wpb;
+  const int64_t cap = (int64_t)num_sms() * occ;
+  if (grid > cap) grid = cap;
+  k<<<(unsigned)grid, 32 * wpb, smem, s>>>(a, rho_constant(a.order));
+  return check_launch("milstein_affine_wide_kernel");
+}
+
+template <typename T>
 int dispatch_affine(const tqf_milstein_affine_args& a, cudaStream_t s) {
   if (a.dim == 1) return launch_affine<T, 1>(a, s);
   if (a.dim <= 2) return launch_affine<T, 2>(a, s);
   if (a.dim <= 4) return launch_affine<T, 4>(a, s);
-  return launch_affine<T, 8>(a, s);
+  if (a.dim <= 8) return launch_affine<T, 8>(a, s);
+  return launch_affine_wide<T>(a, s);
 }
 
 template <typename T>
 int dispatch_update(const tqf_milstein_update_args& a, cudaStream_t s) {
+  if (a.dim > kMaxDimMil) {
+    const int wpb = mil_wide_warps<T>(a.dim, a.order);
+    TQF_REQUIRE(wpb >= 1, "tqf_milstein_update: dim %d with order %d needs more than 200 KiB of shared memory",
+                a.dim, a.order);
+    const size_t smem = (size_t)wpb * mil_wide_warp_elems<T>(a.dim, a.order) * sizeof(T);
+    const int64_t grid = (a.num_paths + wpb - 1) / wpb;
+    TQF_REQUIRE(grid <= 2147483647LL, "tqf_milstein_update: too many paths");
+    set_smem_config(milstein_update_wide_kernel<T>, smem);
+    milstein_update_wide_kernel<T><<<(unsigned)grid, 32 * wpb, smem, s>>>(a, rho_constant(a.order));
+    return check_launch("milstein_update_wide_kernel");
+  }
   const int64_t grid = (a.num_paths + kBlock - 1) / kBlock;
   TQF_REQUIRE(grid <= 2147483647LL, "tqf_milstein_update: too many paths");
   const double rc = rho_constant(a.order);
@@ -320,7 +533,7 @@ extern "C" int tqf_milstein_affine(const tqf_milstein_affine_args* a, void* stre
   clear_error();
   TQF_REQUIRE(a != nullptr, "tqf_milstein_affine: null args");
   TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "tqf_milstein_affine: bad dtype %d", a->dtype);
-  TQF_REQUIRE(a->dim >= 1 && a->dim <= kMaxDimMil, "tqf_milstein_affine: dim must be in [1, 8], got %d", a->dim);
+  TQF_REQUIRE(a->dim >= 1, "tqf_milstein_affine: dim must be >= 1, got %d", a->dim);
   TQF_REQUIRE(a->order >= 1 && a->order <= 64, "tqf_milstein_affine: order must be in [1, 64], got %d", a->order);
   TQF_REQUIRE(a->num_paths >= 1 && a->num_steps >= 0, "tqf_milstein_affine: bad sizes");
   TQF_REQUIRE(a->x0 && a->drift_m && a->drift_M && a->vol_s0 && a->vol_s1 && a->vol_C,
@@ -340,7 +553,7 @@ extern "C" int tqf_milstein_update(const tqf_milstein_update_args* a, void* stre
   clear_error();
   TQF_REQUIRE(a != nullptr, "tqf_milstein_update: null args");
   TQF_REQUIRE(a->dtype == TQF_F32 || a->dtype == TQF_F64, "tqf_milstein_update: bad dtype %d", a->dtype);
-  TQF_REQUIRE(a->dim >= 1 && a->dim <= kMaxDimMil, "tqf_milstein_update: dim must be in [1, 8], got %d", a->dim);
+  TQF_REQUIRE(a->dim >= 1, "tqf_milstein_update: dim must be >= 1, got %d", a->dim);
   TQF_REQUIRE(a->order >= 1 && a->order <= 64, "tqf_milstein_update: bad order %d", a->order);
   TQF_REQUIRE(a->num_paths >= 1, "tqf_milstein_update: num_paths must be >= 1");
   TQF_REQUIRE(a->x && a->drift && a->vol && a->grad && a->x_next, "tqf_milstein_update: null pointer");

@@ -35,7 +35,7 @@ struct SobolOut<TQF_SOBOL_F64> {
 template <>
 struct SobolOut<TQF_SOBOL_NORMAL_F32> {
   using T = float;
-  __device__ static T conv(uint32_t x, float sc, double) { return sobol_normal_f32(x, sc); }
+  __device__ static T conv(uint32_t x, float sc, double) { return sobol_normal_f32(x, 2.0f * sc); }
 };
 template <>
 struct SobolOut<TQF_SOBOL_NORMAL_F64> {

@@ -87,7 +87,7 @@ def sample(*, dim, drift_fn, volatility_fn, times, time_step=None, num_time_step
     alloc = torch.zeros if unwritten else torch.empty
     paths = alloc((N, num_requested, dim), dtype=td, device=device)
     if isinstance(drift_fn, coef.AffineDrift) and isinstance(volatility_fn, coef.ScaledVolatility) \
-            and grad_volatility_fn is None and dim <= 8:
+            and grad_volatility_fn is None:
         if drift_fn.dim != dim or volatility_fn.dim != dim:
             raise ValueError(f"structured coefficients have dimension {drift_fn.dim}, sample() got dim={dim}")
         x0v = torch.broadcast_to(x0, (N, dim)).contiguous() if x0.dim() > 1 else x0.reshape(dim).contiguous()

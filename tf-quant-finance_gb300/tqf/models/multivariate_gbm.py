@@ -85,7 +85,8 @@ class MultivariateGeometricBrownianMotion(ItoProcess):
         """Returns [num_samples, k, dim] (multivariate_geometric_brownian_motion.py:153-227).
 
         ``lz_mode`` (extension): 0 computes L z on the tensor cores (split BF16,
-        three products) when there are 16 float32 factors, 1 forces CUDA cores."""
+        three products) for 16 to 64 correlated float32 factors, 1 forces CUDA
+        cores."""
         del name
         launch, out = self.paths_launcher(times, initial_state, num_samples, random_type, seed, skip,
                                           normal_draws, lz_mode)
@@ -155,7 +156,7 @@ class MultivariateGeometricBrownianMotion(ItoProcess):
         a.output.num_slots = k
         a.output.init_slot = -1
         a.dev_status = _lib.status_buffer(device).data_ptr()
-        a.lz_mode = int(lz_mode)  # 0: tensor cores for 16 float32 factors, 1: CUDA cores
+        a.lz_mode = int(lz_mode)  # 0: tensor cores for 16-64 float32 factors, 1: CUDA cores
         keep_alive += [x0, table, drift, vol, chol]
 
         def launch():
