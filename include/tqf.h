@@ -88,11 +88,20 @@ typedef struct tqf_draws {
  * -1 = none) in the last column of row i of the kernel's step table, and the
  * initial state to init_slot (-1 = none).  The host derives the slots from
  * the reference's written_count/keep_mask recursion
- * (tff/models/euler_sampling.py:424-455). */
+ * (tff/models/euler_sampling.py:424-455).  every_step = 1 declares that step
+ * i records slot base + i for every step (base = 1 after an initial state at
+ * slot 0, else 0) and num_slots = base + num_steps: path rows then fill front
+ * to back, and the Euler (tqf_euler_affine) and GBM (tqf_mvgbm_paths) kernels
+ * write rows that are a multiple of 16 bytes with bulk shared -> global
+ * copies (4, 8 or 16 bytes per slot).  Such a kernel that finds the
+ * declaration false writes no states and sets *dev_status to TQF_E_INVALID;
+ * the other kernels ignore the field. */
 typedef struct tqf_path_output {
   void* ptr;
   int32_t num_slots;
   int32_t init_slot;
+  int32_t every_step;
+  int32_t pad0;
 } tqf_path_output;
 
 /* Fused European payoff over the final state: for each strike j the kernel

@@ -186,3 +186,94 @@ def test_gaussian_hjm_every_time_recorded(cuda, dtype, rtol, dim):
     np.testing.assert_allclose(rates.cpu().numpy(), wr, rtol=rtol, atol=rtol * 1e-2)
     np.testing.assert_allclose(dfs.cpu().numpy(), wd, rtol=rtol)
     np.testing.assert_allclose(x.cpu().numpy(), wx, rtol=rtol, atol=rtol * 1e-2)
+
+
+@pytest.mark.parametrize("dtype,rtol", DTYPES)
+@pytest.mark.parametrize("d", [1, 2, 4])
+def test_euler_bulk_rows_every_step(cuda, dtype, rtol, d):
+    """Every grid time recorded (times = times_grid, t = 0 included): rows of
+    72 slots x d values are a multiple of 16 bytes, so the kernel writes them
+    with bulk shared -> global copies in 128-byte pieces (2 full pieces and a
+    partial one per path for d = 1); 1000 paths leave the last CTA round
+    partly empty.  d = 4 in float64 (32 bytes per slot) takes the RowStager."""
+    from tqf.models import coefficients, euler_sampling
+    N, steps = 1000, 71
+    rng = np.random.default_rng(20 + d)
+    mu = rng.uniform(-0.05, 0.05, d)
+    sig = rng.uniform(0.1, 0.3, d)
+    corr = 0.6 * np.eye(d) + 0.4
+    drift, vol = coefficients.gbm(mu, sig, corr)
+    grid = np.linspace(0.0, 1.0, steps + 1).astype(dtype)
+    draws = rng.standard_normal((N, steps, d)).astype(dtype)
+    x0 = np.linspace(1.0, 2.0, d).astype(dtype)
+    got = euler_sampling.sample(d, drift, vol, grid, times_grid=grid, initial_state=x0,
+                                normal_draws=draws).cpu().numpy()
+    all_t, keep, _ = ogrids.prepare_grid(grid, None, dtype, times_grid=grid)
+    L = np.linalg.cholesky(corr).astype(dtype)
+    want = oeuler.sample_with_draws(lambda t, x: (x * mu.astype(dtype)).astype(dtype),
+                                    lambda t, x: ((x * sig.astype(dtype))[..., None] * L).astype(dtype),
+                                    all_t, keep, len(grid), np.broadcast_to(x0, (N, d)), draws.transpose(1, 0, 2),
+                                    dtype)
+    assert got.shape == (N, steps + 1, d)
+    _close(got, want, rtol, 1.0)
+
+
+def test_heston_every_step_of_times_grid(cuda):
+    """QE (HestonModel.sample_paths) and full truncation (euler_sampling with
+    the Heston coefficients) with every step of a 72-step times_grid recorded
+    (the every-step declaration is set; the Heston kernels keep their
+    CTA-cooperative SlotStager), against the oracle."""
+    import tqf
+    N, steps = 1000, 72
+    grid = np.linspace(0.0, 1.0, steps + 1).astype(np.float32)
+    x0 = np.array([np.log(100.0), 0.04], np.float32)
+    draws = np.random.default_rng(9).standard_normal((N, steps, 2)).astype(np.float32)
+    model = tqf.models.HestonModel(2.0, 0.04, 0.3, -0.7)
+    got = model.sample_paths(grid[1:], x0, times_grid=grid, normal_draws=draws).cpu().numpy()
+    all_t, keep, _ = ogrids.prepare_grid(grid[1:], None, np.float32, times_grid=grid)
+    want, near = oheston.qe_sample_with_draws(2.0, 0.04, 0.3, -0.7, all_t, keep, steps, x0[0], x0[1],
+                                              draws.transpose(1, 0, 2), np.float32, near=1e-4)
+    assert got.shape == want.shape == (N, steps, 2)
+    ok = ~near
+    err = np.abs(got[ok] - want[ok]) / (np.abs(want[ok]) + np.array([1.0, 0.04]))
+    assert err.max() < 1e-5, err.max()
+    drift, vol = tqf.models.coefficients.heston_full_truncation(0.02, 2.0, 0.04, 0.3, -0.7)
+    p2 = tqf.models.euler_sampling.sample(2, drift, vol, grid[1:], times_grid=grid, initial_state=x0,
+                                          normal_draws=draws).cpu().numpy()
+    fd, fv = oeuler.heston_ft_coefficients(0.02, 2.0, 0.04, 0.3, -0.7, np.float32)
+    want2 = oeuler.sample_with_draws(fd, fv, all_t, keep, steps, np.broadcast_to(x0, (N, 2)),
+                                     draws.transpose(1, 0, 2), np.float32)
+    err = np.abs(p2 - want2) / (np.abs(want2) + np.array([1.0, 0.04]))
+    assert np.quantile(err.max(axis=(1, 2)), 0.99) < 1e-5
+
+
+def test_every_step_declaration_is_checked(cuda):
+    """A path kernel told that every step is recorded in order (the bulk-row
+    layout) verifies it on its step table: here one date records nothing, so
+    the kernel writes no state and reports TQF_E_INVALID in the status word."""
+    import tqf._lib as L
+    from tqf.math.random import RandomType
+    from tqf.math.random import multivariate_normal as mvn
+    from tqf.models import utils
+    k, N = 8, 300
+    rows = np.zeros((k, 4))
+    rows[:, 0] = 1.0 / k
+    rows[:, 1] = np.sqrt(1.0 / k)
+    rows[:, 2] = np.arange(k)
+    rows[3, 2] = -1
+    table = utils.step_table(rows, torch.float32, cuda)
+    one = torch.ones(1, device=cuda)
+    out = torch.full((N, k, 1), float("nan"), device=cuda)
+    a = L.MvgbmArgs()
+    a.dtype, a.dim, a.num_paths, a.num_steps = L.TQF_F32, 1, N, k
+    a.step_table = table.data_ptr()
+    a.x0 = a.drift = a.vol = one.data_ptr()
+    a.chol = None
+    a.draws = mvn.philox_draws(RandomType.STATELESS, [1, 2], N)
+    a.output.ptr, a.output.num_slots, a.output.init_slot, a.output.every_step = out.data_ptr(), k, -1, 1
+    a.dev_status = L.status_buffer(cuda).data_ptr()
+    a.lz_mode = 1
+    L.call("tqf_mvgbm_paths", a, L.stream_ptr())
+    with pytest.raises(RuntimeError):
+        L.check_device_status(cuda)
+    assert bool(torch.isnan(out).all())

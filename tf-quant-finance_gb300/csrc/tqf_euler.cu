@@ -29,10 +29,12 @@ __host__ __device__ inline size_t affine_stage_offset(int steps, bool staged) {
   return (head + (staged ? (size_t)steps * kCols * sizeof(T) : 0) + 15) & ~(size_t)15;
 }
 
-// STAGE: recorded states go through the coalescing RowStager (chosen when a
-// path's output row is long enough for scattered stores to cost more than
-// the stager's registers and shared memory).
-template <typename T, int DM, int SRC, bool STAGE>
+// STAGE: 0 = each thread stores its own recorded states; 1 = through the
+// coalescing RowStager (chosen when a path's output row is long enough for
+// scattered stores to cost more than the stager's registers and shared
+// memory); 2 = BulkRowStager (every step declared recorded in order, dim ==
+// DM, DM * sizeof(T) in {4, 8, 16}, 16-byte rows and alignment).
+template <typename T, int DM, int SRC, int STAGE>
 __global__ void __launch_bounds__(kBlock)
     euler_affine_kernel(tqf_euler_affine_args a, int staged) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -68,10 +70,23 @@ __global__ void __launch_bounds__(kBlock)
   const int64_t N = a.num_paths;
   T* out = static_cast<T*>(a.output.ptr);
   const int ns = a.output.num_slots;
-  // with the stager every thread runs every round (a thread past the last
+  if constexpr (STAGE == 2) {
+    // verify the every-step declaration on the table (see tqf_path_output)
+    const int base = a.output.init_slot >= 0 ? 1 : 0;
+    int ok = (a.output.init_slot < 0 || a.output.init_slot == 0) && base + steps == ns;
+    for (int i = threadIdx.x; i < steps; i += kBlock) ok &= (int)table[(size_t)i * kCols + 2] == base + i;
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0 && a.dev_status) atomicExch(a.dev_status, TQF_E_INVALID);
+      return;
+    }
+  }
+  // with the RowStager every thread runs every round (a thread past the last
   // path simulates that path again and its output is dropped)
-  const bool stage_out = STAGE && out != nullptr;
+  const bool stage_out = STAGE == 1 && out != nullptr;
   RowStager<T, DM, kBlock> stg(smem + affine_stage_offset<T, DM>(steps, staged != 0), dim);
+  BulkRowStager bst(smem + affine_stage_offset<T, DM>(steps, staged != 0));
+  unsigned char* out_bytes = reinterpret_cast<unsigned char*>(out);
+  const int64_t row_bytes = (int64_t)ns * DM * (int64_t)sizeof(T);
   const int64_t per_round = (int64_t)gridDim.x * kBlock;
   for (int64_t base = 0; base < N; base += per_round) {
     const int64_t row0 = base + (int64_t)blockIdx.x * kBlock;
@@ -83,7 +98,9 @@ __global__ void __launch_bounds__(kBlock)
 #pragma unroll
     for (int j = 0; j < DM; ++j) x[j] = j < dim ? x0[j] : T(0);
     if (out && a.output.init_slot >= 0) {
-      if (stage_out) {
+      if constexpr (STAGE == 2) {
+        bst.put<T, DM>(out_bytes, row_bytes, path, a.output.init_slot, x);
+      } else if (stage_out) {
         stg.put(out, ns, row0, N, a.output.init_slot, x);
       } else {
         T* o = out + (path * ns + a.output.init_slot) * dim;
@@ -116,7 +133,9 @@ __global__ void __launch_bounds__(kBlock)
       for (int r = 0; r < DM; ++r) x[r] = xn[r];
       const int slot = (int)row[2];
       if (out && slot >= 0) {
-        if (stage_out) {
+        if constexpr (STAGE == 2) {
+          bst.put<T, DM>(out_bytes, row_bytes, path, slot, x);
+        } else if (stage_out) {
           stg.put(out, ns, row0, N, slot, x);
         } else {
           T* o = out + (path * ns + slot) * dim;
@@ -127,7 +146,9 @@ __global__ void __launch_bounds__(kBlock)
       }
     }
     if (stage_out && stg.cnt > 0) stg.flush(out, ns, row0, N);
+    if (STAGE == 2) bst.flush(out_bytes);
   }
+  if (STAGE == 2) bst.finish(out_bytes);
 }
 
 template <typename T, int DM>
@@ -327,17 +348,26 @@ int launch_affine(const tqf_euler_affine_args& a, cudaStream_t s) {
   const size_t tab_bytes = (size_t)a.num_steps * kCols * sizeof(T);
   const bool staged = tab_bytes > 0 && tab_bytes <= 96 * 1024 &&
                       (reinterpret_cast<uintptr_t>(a.step_table) & 15u) == 0;
+  // bulk rows for every-step outputs of 4, 8 or 16 bytes per slot; else
   // stage the output when a path's row is at least 64 bytes
-  const bool stage_out =
-      a.output.ptr != nullptr && (size_t)a.output.num_slots * a.dim * sizeof(T) >= 64;
-  const size_t smem =
-      affine_stage_offset<T, DM>(a.num_steps, staged) + (stage_out ? RowStager<T, DM, kBlock>::kBytes : 0);
+  constexpr bool kBulkable = DM * sizeof(T) == 4 || DM * sizeof(T) == 8 || DM * sizeof(T) == 16;
+  const size_t row = (size_t)a.output.num_slots * a.dim * sizeof(T);
+  const bool bulk = kBulkable && a.output.ptr != nullptr && a.output.every_step && a.dim == DM &&
+                    (reinterpret_cast<uintptr_t>(a.output.ptr) & 15u) == 0 && row % 16 == 0;
+  const bool stage_out = !bulk && a.output.ptr != nullptr && row >= 64;
+  const size_t smem = affine_stage_offset<T, DM>(a.num_steps, staged) +
+                      (bulk ? (size_t)kBlock * BulkRowStager::kRowBytes
+                            : (stage_out ? RowStager<T, DM, kBlock>::kBytes : 0));
   const bool philox = a.draws.source == TQF_DRAWS_PHILOX;
   void (*k)(tqf_euler_affine_args, int) =
-      stage_out ? (philox ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX, true>
-                          : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY, true>)
-                : (philox ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX, false>
-                          : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY, false>);
+      stage_out ? (philox ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX, 1>
+                          : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY, 1>)
+                : (philox ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX, 0>
+                          : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY, 0>);
+  if constexpr (kBulkable) {
+    if (bulk)
+      k = philox ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX, 2> : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY, 2>;
+  }
   if (smem > 48 * 1024) set_smem_config(k, smem);
   int occ = 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem) != cudaSuccess || occ < 1)

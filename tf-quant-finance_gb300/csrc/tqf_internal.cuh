@@ -598,6 +598,96 @@ __device__ __forceinline__ bool stage_to_smem(void* dst, const void* src, uint32
   return true;
 }
 
+// ---- every-step output by bulk stores --------------------------------------------
+// When every output slot is recorded once, in increasing order from slot 0,
+// and a path's output row is a multiple of 16 bytes long (and the output
+// 16-byte aligned), a path's recorded values fill its row front to back.
+// Then each thread gathers its own row in 128-byte pieces in a private
+// shared-memory row (16-byte vector stores of packed values) and writes each
+// full piece with one cp.async.bulk shared -> global copy: no CTA barrier, no
+// per-value global store, and threads past the last path simply stop.  The
+// row stride of 144 bytes (an odd multiple of 16 modulo 128) keeps the
+// quarter-warp phases of the 16-byte shared stores conflict-free.  Before a
+// row is refilled the thread waits (cp.async.bulk.wait_group.read 0) for its
+// previous copy to have read it; finish() waits for every copy to complete.
+// Values per slot (W) times sizeof(T) must be 4, 8 or 16 bytes.
+struct BulkRowStager {
+  static constexpr int kPiece = 128;
+  static constexpr int kRowBytes = kPiece + 16;
+  uint32_t row;         // shared-memory address of this thread's row
+  uint32_t h0, h1, h2;  // pending words of the next 16-byte store
+  int pk, nb;           // pending words, bytes gathered in the row
+  int64_t gofs;
+  __device__ explicit BulkRowStager(void* smem)
+      : row(smem_addr(smem) + threadIdx.x * (uint32_t)kRowBytes), h0(0), h1(0), h2(0), pk(0), nb(0), gofs(0) {}
+  __device__ __forceinline__ void store16(uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+    asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(row + (uint32_t)nb), "r"(a), "r"(b), "r"(c),
+                 "r"(d)
+                 : "memory");
+    nb += 16;
+  }
+  // Appends the W values x[0..W) of `slot` of path `path` (row_bytes = the
+  // output row length in bytes); W * sizeof(T) is 4, 8 or 16.
+  template <typename T, int W>
+  __device__ __forceinline__ void put(unsigned char* out, int64_t row_bytes, int64_t path, int slot, const T* x) {
+    constexpr int B = W * (int)sizeof(T);
+    static_assert(B == 4 || B == 8 || B == 16, "bulk rows take 4, 8 or 16 bytes per slot");
+    if (nb == 0 && pk == 0) {
+      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+      gofs = path * row_bytes + (int64_t)slot * B;
+    }
+    uint32_t w[B / 4];
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+      for (int c = 0; c < W; ++c) w[c] = __float_as_uint(x[c]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        const unsigned long long u = __double_as_longlong(x[c]);
+        w[2 * c] = (uint32_t)u;
+        w[2 * c + 1] = (uint32_t)(u >> 32);
+      }
+    }
+    if constexpr (B == 16) {
+      store16(w[0], w[1], w[2], w[3]);
+    } else if constexpr (B == 8) {
+      if (pk == 0) {
+        h0 = w[0];
+        h1 = w[1];
+        pk = 2;
+      } else {
+        store16(h0, h1, w[0], w[1]);
+        pk = 0;
+      }
+    } else {
+      if (pk == 0) h0 = w[0];
+      else if (pk == 1) h1 = w[0];
+      else if (pk == 2) h2 = w[0];
+      if (pk == 3) {
+        store16(h0, h1, h2, w[0]);
+        pk = 0;
+      } else {
+        ++pk;
+      }
+    }
+    if (nb == kPiece) flush(out);
+  }
+  // Writes the gathered bytes (whole 16-byte groups under the layout contract).
+  __device__ __forceinline__ void flush(unsigned char* out) {
+    if (nb == 0) return;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(out + gofs), "r"(row),
+                 "r"(nb)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    nb = 0;
+  }
+  __device__ __forceinline__ void finish(unsigned char* out) {
+    flush(out);
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  }
+};
+
 // ---- FP64 European payoff accumulation --------------------------------------
 // Each round, the CTA's BLOCK threads have one terminal spot each in
 // s_spot[] (NaN for no path).  Work item w = (strike j, quarter q) sums

@@ -49,11 +49,13 @@ __device__ __forceinline__ void load_coef(GbmCoef<T, DM>* c, int dim, const void
   }
 }
 
-// STAGE: recorded states go through the coalescing RowStager (dynamic
+// STAGE: 1 = recorded states go through the coalescing RowStager (dynamic
 // shared memory), chosen when a path's output row is at least 64 bytes; then
 // every thread runs every round and a thread past the last path simulates
-// that path again with its output dropped.
-template <typename T, int DM, bool STAGE>
+// that path again with its output dropped.  2 = BulkRowStager (every date
+// declared recorded in order, dim == DM, DM * sizeof(T) in {4, 8, 16},
+// 16-byte rows and alignment).  0 = direct stores.
+template <typename T, int DM, int STAGE>
 __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
   __shared__ GbmCoef<T, DM> coef;
   extern __shared__ __align__(16) unsigned char stage_smem[];
@@ -64,12 +66,25 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
   T* out = static_cast<T*>(a.output.ptr);
   const int ns = a.output.num_slots;
   const int64_t N = a.num_paths;
+  if constexpr (STAGE == 2) {
+    // verify the every-step declaration on the table (see tqf_path_output)
+    const int base = a.output.init_slot >= 0 ? 1 : 0;
+    int ok = (a.output.init_slot < 0 || a.output.init_slot == 0) && base + a.num_steps == ns;
+    for (int i = threadIdx.x; i < a.num_steps; i += kBlock) ok &= (int)table[i * 4 + 2] == base + i;
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0 && a.dev_status) atomicExch(a.dev_status, TQF_E_INVALID);
+      return;
+    }
+  }
   RowStager<T, DM, kBlock> stg(stage_smem, dim);
+  BulkRowStager bst(stage_smem);
+  unsigned char* out_bytes = reinterpret_cast<unsigned char*>(out);
+  const int64_t row_bytes = (int64_t)ns * DM * (int64_t)sizeof(T);
   const int64_t per_round = (int64_t)gridDim.x * kBlock;
   for (int64_t base = 0; base < N; base += per_round) {
     const int64_t row0 = base + (int64_t)blockIdx.x * kBlock;
     const int64_t path = row0 + threadIdx.x;
-    if (!STAGE && path >= N) break;
+    if (STAGE != 1 && path >= N) break;
     const int64_t pc = path < N ? path : N - 1;
     const T* x0p = static_cast<const T*>(a.x0) + (a.x0_per_path ? pc * dim : 0);
     T x0[DM], cs[DM];
@@ -79,7 +94,9 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
       cs[j] = T(0);
     }
     if (a.output.init_slot >= 0) {
-      if (STAGE) {
+      if constexpr (STAGE == 2) {
+        bst.put<T, DM>(out_bytes, row_bytes, path, a.output.init_slot, x0);
+      } else if constexpr (STAGE == 1) {
         stg.put(out, ns, row0, N, a.output.init_slot, x0);
       } else {
         T* o = out + (path * ns + a.output.init_slot) * dim;
@@ -103,7 +120,12 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
         cs[r] += coef.drift[r] * dt + sdt * coef.sigma[r] * y;
       }
       if (slot >= 0) {
-        if constexpr (STAGE) {
+        if constexpr (STAGE == 2) {
+          T xs[DM];
+#pragma unroll
+          for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
+          bst.put<T, DM>(out_bytes, row_bytes, path, slot, xs);
+        } else if constexpr (STAGE == 1) {
           T xs[DM];
 #pragma unroll
           for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
@@ -116,8 +138,10 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
         }
       }
     }
-    if (STAGE && stg.cnt > 0) stg.flush(out, ns, row0, N);
+    if (STAGE == 1 && stg.cnt > 0) stg.flush(out, ns, row0, N);
+    if (STAGE == 2) bst.flush(out_bytes);
   }
+  if (STAGE == 2) bst.finish(out_bytes);
 }
 
 // ---- tensor-core L z (split BF16, three products) ------------------------------
@@ -637,10 +661,19 @@ __global__ void __launch_bounds__(256) cholesky_f64_global_kernel(const double* 
 
 template <typename T, int DM>
 int launch_paths(const tqf_mvgbm_args& a, cudaStream_t s) {
+  // bulk rows for every-date outputs of 4, 8 or 16 bytes per date; else
   // stage the output when a path's row is at least 64 bytes
-  const bool stage = (size_t)a.output.num_slots * a.dim * sizeof(T) >= 64;
-  auto k = stage ? mvgbm_paths_kernel<T, DM, true> : mvgbm_paths_kernel<T, DM, false>;
-  const size_t smem = stage ? RowStager<T, DM, kBlock>::kBytes : 0;
+  constexpr bool kBulkable = DM * sizeof(T) == 4 || DM * sizeof(T) == 8 || DM * sizeof(T) == 16;
+  const size_t row = (size_t)a.output.num_slots * a.dim * sizeof(T);
+  const bool bulk = kBulkable && a.output.every_step && a.dim == DM &&
+                    (reinterpret_cast<uintptr_t>(a.output.ptr) & 15u) == 0 && row % 16 == 0;
+  const bool stage = !bulk && row >= 64;
+  auto k = stage ? mvgbm_paths_kernel<T, DM, 1> : mvgbm_paths_kernel<T, DM, 0>;
+  if constexpr (kBulkable) {
+    if (bulk) k = mvgbm_paths_kernel<T, DM, 2>;
+  }
+  const size_t smem =
+      bulk ? (size_t)kBlock * BulkRowStager::kRowBytes : (stage ? RowStager<T, DM, kBlock>::kBytes : 0);
   if (smem > 48 * 1024) set_smem_config(k, smem);
   int occ = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem);

@@ -61,7 +61,7 @@ class Draws(ctypes.Structure):
 
 
 class PathOutput(ctypes.Structure):
-    _fields_ = [("ptr", c_vp), ("num_slots", c_i32), ("init_slot", c_i32)]
+    _fields_ = [("ptr", c_vp), ("num_slots", c_i32), ("init_slot", c_i32), ("every_step", c_i32), ("pad0", c_i32)]
 
 
 class Payoff(ctypes.Structure):
@@ -586,9 +586,13 @@ def status_buffer(device: torch.device) -> torch.Tensor:
 
 
 def check_device_status(device: torch.device) -> None:
-    """Raises if a kernel recorded a timed-out wait (synchronises)."""
+    """Raises if a kernel recorded a device-side error (synchronises): a
+    timed-out bounded wait (TQF_E_TIMEOUT), or an every-step output layout
+    declared by the caller that the step table contradicts (TQF_E_INVALID)."""
     buf = status_buffer(device)
     v = int(buf.item())
     if v != 0:
         buf.zero_()
-        raise RuntimeError(f"tqf kernel reported device status {v} (bounded wait timed out)")
+        why = {TQF_E_TIMEOUT: "bounded wait timed out",
+               TQF_E_INVALID: "the every-step output declaration does not match the step table"}.get(v, "error")
+        raise RuntimeError(f"tqf kernel reported device status {v} ({why})")

@@ -159,6 +159,7 @@ def sample(dim, drift_fn, volatility_fn, times, time_step=None, num_time_steps=N
         args.output.ptr = paths.data_ptr()
         args.output.num_slots = num_requested
         args.output.init_slot = init_slot
+        args.output.every_step = utils.every_step_layout(step_slot, init_slot, steps_exec, num_requested)
         args.dev_status = _lib.status_buffer(device).data_ptr()
         _lib.call("tqf_euler_affine", args, _lib.stream_ptr(device))
         return paths

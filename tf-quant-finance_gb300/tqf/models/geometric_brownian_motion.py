@@ -155,6 +155,7 @@ class GeometricBrownianMotion(ItoProcess):
             a.output.ptr = out[b].data_ptr()
             a.output.num_slots = k
             a.output.init_slot = -1
+            a.output.every_step = 1  # date j records slot j
             a.dev_status = _lib.status_buffer(device).data_ptr()
             a.lz_mode = 1
             _lib.call("tqf_mvgbm_paths", a, _lib.stream_ptr(device))

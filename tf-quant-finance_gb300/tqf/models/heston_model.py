@@ -149,6 +149,7 @@ class HestonModel(GenericItoProcess):
         args.output.ptr = paths.data_ptr()
         args.output.num_slots = num_requested
         args.output.init_slot = init_slot
+        args.output.every_step = utils.every_step_layout(step_slot, init_slot, steps_exec, num_requested)
         args.dev_status = _lib.status_buffer(device).data_ptr()
         _lib.call("tqf_heston_qe", args, _lib.stream_ptr(device))
         return paths
@@ -250,6 +251,7 @@ def run_full_truncation(heston, all_times, dt, sqrt_dt, step_slot, init_slot, st
     args.output.ptr = paths.data_ptr()
     args.output.num_slots = num_slots
     args.output.init_slot = init_slot
+    args.output.every_step = utils.every_step_layout(step_slot, init_slot, steps_exec, num_slots)
     args.dev_status = _lib.status_buffer(device).data_ptr()
     _lib.call("tqf_heston_euler", args, _lib.stream_ptr(device))
 

@@ -155,6 +155,7 @@ class MultivariateGeometricBrownianMotion(ItoProcess):
         a.output.ptr = out.data_ptr()
         a.output.num_slots = k
         a.output.init_slot = -1
+        a.output.every_step = 1  # date j records slot j
         a.dev_status = _lib.status_buffer(device).data_ptr()
         a.lz_mode = int(lz_mode)  # 0: tensor cores for 16-64 float32 factors, 1: CUDA cores
         keep_alive += [x0, table, drift, vol, chol]

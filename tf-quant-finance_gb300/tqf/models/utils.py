@@ -103,6 +103,18 @@ def prepare_grid(*, times, time_step, dtype, tolerance=None, num_time_steps=None
     return all_times, mask, ti
 
 
+def every_step_layout(step_slot, init_slot: int, steps_exec: int, num_slots: int) -> int:
+    """1 if step i records slot base + i for every executed step (base = 1
+    after an initial state at slot 0) and the slots end at num_slots: the
+    tqf_path_output.every_step declaration that lets the path kernels write
+    whole rows with bulk copies."""
+    base = 1 if init_slot >= 0 else 0
+    if init_slot not in (-1, 0) or base + int(steps_exec) != int(num_slots):
+        return 0
+    s = np.asarray(step_slot[:steps_exec]).astype(np.int64)
+    return int(bool(np.array_equal(s, base + np.arange(int(steps_exec)))))
+
+
 def plan_output_slots(keep_mask, num_requested: int, initial_written_count: int):
     """Replays the reference's written_count recursion (euler_sampling.py:424-455;
     heston_model.py:441-446 starts it at 0) on the host.
