@@ -457,9 +457,10 @@ def run_sobol(dim=1024, total_points=1 << 26, chunk=1 << 20, timed_chunks=8):
 def run_lsm(n_paths=1 << 20, n_dates=50, degree=3, reps=5, cpu_paths=1 << 15):
     """Longstaff–Schwartz American put (K = 1.1, r = 6 %, sigma = 0.2, T = 1)
     on GBM paths from this engine's sampler: N paths x 50 exercise dates,
-    float32, centred cubic basis.  Device time of least_square_mc (all
-    passes, reductions and solves, paths resident) from CUDA events; the
-    oracle's NumPy restatement timed on a path sample beside it."""
+    float32, centred cubic basis.  Time of least_square_mc through the public
+    API (the gather, then the whole backward loop in one cooperative kernel;
+    paths resident) from CUDA events; the oracle's NumPy restatement timed on
+    a path sample beside it."""
     import torch
     from tqf.math.random import RandomType
     from tqf.models import MultivariateGeometricBrownianMotion
@@ -483,6 +484,11 @@ def run_lsm(n_paths=1 << 20, n_dates=50, degree=3, reps=5, cpu_paths=1 << 15):
     e1.record()
     torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) / reps / 1e3
+    from tqf import _lib
+    c0 = _lib.launch_count()
+    L.least_square_mc(paths, ex, pay, basis, discount_factors=df, dtype=np.float32)
+    launches = _lib.launch_count() - c0
+    torch.cuda.synchronize()
     sample = paths[:cpu_paths].cpu().numpy()
     t0 = time.perf_counter()
     cpu_price = olsm.least_square_mc(sample, ex, [1.1], degree, discount_factors=df, dtype=np.float32)
@@ -491,7 +497,7 @@ def run_lsm(n_paths=1 << 20, n_dates=50, degree=3, reps=5, cpu_paths=1 << 15):
                       f"float32, degree-{degree} basis",
             "price": float(price.cpu().numpy()[0]), "seconds": sec,
             "path_dates_per_s": n_paths * n_dates / sec,
-            "launches_per_call": 3 * (n_dates - 1) + 4,
+            "launches_per_call": launches,
             "cpu_baseline": {"path_dates_per_s": cpu_paths * n_dates / cpu_sec, "cores": 1, "kind": "port",
                              "sample": f"oracle NumPy restatement, {cpu_paths} paths, price {float(cpu_price[0]):.5f}"}}
 

@@ -134,8 +134,11 @@ __host__ inline int lsm_gather_grid(const tqf_lsm_args& a) {
 }
 
 struct WsLayout {
-  size_t partials, sums, beta, means, mean_partials, eig_v, xt, total;
+  size_t partials, sums, beta, means, mean_partials, eig_v, xt, sync, total;
 };
+
+// Grid of the one-launch date loop (0 when the call does not qualify).
+__host__ int lsm_loop_grid(const tqf_lsm_args& a);
 
 __host__ inline WsLayout lsm_layout(const tqf_lsm_args& a) {
   const int G = a.num_basis, B = a.batch, E = a.num_exercise;
@@ -143,12 +146,13 @@ __host__ inline WsLayout lsm_layout(const tqf_lsm_args& a) {
   const int gx = a.dtype == TQF_F32 ? lsm_pass_grid<float>(a, nullptr, nullptr)
                                     : lsm_pass_grid<double>(a, nullptr, nullptr);
   const int gg = lsm_gather_grid(a);
+  const int gl = lsm_loop_grid(a);
   const size_t es = a.dtype == TQF_F32 ? 4 : 8;
   auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
   WsLayout w{};
   size_t off = 0;
   w.partials = off;
-  off += up((size_t)gx * B * (En > 1 ? En : 1) * 8);
+  off += up((size_t)(gx > gl ? gx : gl) * B * (En > 1 ? En : 1) * 8);
   w.sums = off;
   off += up((size_t)B * En * 8);
   w.beta = off;
@@ -161,6 +165,8 @@ __host__ inline WsLayout lsm_layout(const tqf_lsm_args& a) {
   off += up((size_t)B * G * G * 8);
   w.xt = off;
   if (a.degree >= 0) off += up((size_t)a.paths_batch * E * a.num_paths * a.dim * es);
+  w.sync = off;
+  off += 256;
   w.total = off;
   return w;
 }
@@ -836,6 +842,622 @@ __global__ void __launch_bounds__(kSolveThreads)
     for (int i = tid; i < G * G; i += nt) Vb[i] = V[i];
 }
 
+// ---- the whole backward loop in one cooperative kernel --------------------------
+// For the common structured case (one payoff, one path set, d <= 2 and 2..5
+// basis functions) tqf_lsm_price runs every exercise date in one cooperative
+// launch instead of three launches per date.  Per date all CTAs run the pass
+// (the register-mode arithmetic of lsm_pass_kernel) and store their partial
+// sums; a grid barrier; CTA 0 reduces the partials in a fixed order and its
+// first warp solves the 2..5-function system (below); a second barrier
+// releases the next date.  Both barriers are bounded waits: after
+// kLoopSpinLimit polls the CTA sets the abort word and TQF_E_TIMEOUT in
+// dev_status and every CTA leaves.  Data crossing CTAs (partials, beta) is
+// written and read with L2-only accesses (__stcg / __ldcg).
+constexpr int kLoopThreads = 256;
+constexpr unsigned kLoopSpinLimit = 1u << 24;
+constexpr int kLoopMaxG = 5;
+constexpr int kLoopMaxEn = kLoopMaxG * (kLoopMaxG + 1) / 2 + kLoopMaxG;
+
+struct LoopSync {
+  unsigned int count;
+  unsigned int abort;
+};
+
+__device__ __forceinline__ unsigned ld_volatile(const unsigned* p) {
+  return *reinterpret_cast<const volatile unsigned*>(p);
+}
+
+// Grid barrier number `gen` (1, 2, ...): returns false when it was aborted.
+__device__ bool loop_barrier(LoopSync* sy, unsigned gen, int32_t* status) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(&sy->count, 1u);
+    const unsigned target = gen * gridDim.x;
+    int ok = 1;
+    for (unsigned it = 0;; ++it) {
+      if (ld_volatile(&sy->count) >= target) break;
+      if (ld_volatile(&sy->abort)) {
+        ok = 0;
+        break;
+      }
+      if (it > kLoopSpinLimit) {
+        ok = 0;
+        atomicExch(&sy->abort, 1u);
+        if (status) atomicExch(status, TQF_E_TIMEOUT);
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+__device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+// The rotation (c, s) of the pair (x, xp) of the current round, from the
+// lanes holding A_pp, A_qq and A_pq (Golub & Van Loan, sym.schur2); identity
+// when x has no partner.  Kept out of line: the solver runs in one warp once
+// per date, so its code is cold in the instruction cache and small code is
+// what makes it fast.
+template <int G>
+__device__ __noinline__ float2 jacobi_rot_f32(float af, int x, int xp) {
+  const int p = xp < 0 ? x : (x < xp ? x : xp), q = xp < 0 ? x : (x < xp ? xp : x);
+  const float app = __shfl_sync(0xffffffffu, af, p * G + p);
+  const float aqq = __shfl_sync(0xffffffffu, af, q * G + q);
+  const float apq = __shfl_sync(0xffffffffu, af, p * G + q);
+  float c = 1.f, sn = 0.f;
+  // |apq| below 2^-100 of the diagonal gap needs no rotation (and keeps the
+  // fast approximate division away from overflow); the angle only has to be
+  // FP32-accurate, so the SFU division and square root serve
+  const float gap = aqq - app;
+  if (xp >= 0 && fabsf(apq) > 7.9e-31f * fabsf(gap) && apq != 0.f) {
+    const float th = __fdividef(gap, 2.f * apq);
+    const float ath = fabsf(th);
+    const float t = ath > 1e18f ? __fdividef(0.5f, th)
+                                : __fdividef(copysignf(1.f, th), ath + sqrt_approx(fmaf(th, th, 1.f)));
+    c = rsqrtf(fmaf(t, t, 1.f));
+    sn = t * c;
+  }
+  return make_float2(c, sn);
+}
+
+// Pseudo-inverse solve of a G x G system (G <= 5) by one warp.  FP64 is a
+// narrow pipe on this GPU (a warp-wide FP64 instruction occupies it for ~64
+// cycles, measured, whatever the active lanes), so the eigenvectors come
+// from cyclic Jacobi in FP32 and only a fixed, short FP64 stage follows:
+//   1. lane i*G + j holds A_ij (and V_ij); A scaled by a power of two to
+//      O(1), warm-started by V^T A V from the previous date's V; FP32 Jacobi
+//      sweeps (round-robin pairing over G rounded up to even, partner of x in
+//      round r = 2r - x mod (Pe - 1), the last index with r; the rotation of
+//      Golub & Van Loan's sym.schur2) until the off-diagonal is below 1e-12
+//      of the total or stops shrinking; skipped on a warm start whose
+//      Gershgorin discs keep every direction far above the cutoff;
+//   2. FP64: B = V^T A V and u = V^T X'y with the FP32 V (any invertible V
+//      gives A^-1 = V B^-1 V^T exactly, and B is diagonal to ~1e-7, so its
+//      diagonal holds the eigenvalues to FP64 accuracy);
+//   3. tf.linalg.pinv's cutoff (rcond x max |B_kk|) drops directions; the
+//      kept block B_KK x = u_K is solved by Gaussian elimination in FP64 (one
+//      row per lane, pivots on the diagonal; reciprocals from the FP32
+//      reciprocal refined by two Newton steps), beta = V x.
+// sums: packed upper triangle then X'y (FP64, shared); Vs (shared) keeps V
+// for the next date; Ws, Bs: shared scratch [G*G + G].
+template <int G>
+__device__ __noinline__ void warp_pinv_solve(const double* sums, double rcond, bool warm, float* Vs, float* Fs,
+                                             double* Ws, double* Bs, double* beta_out) {
+  const int lane = threadIdx.x & 31;
+  const bool in = lane < G * G;
+  const int i = in ? lane / G : 0, j = in ? lane % G : 0;
+  auto packed = [](int r, int c) {
+    const int p = r < c ? r : c, q = r < c ? c : r;
+    return p * G - p * (p - 1) / 2 + (q - p);
+  };
+  const double a = in ? sums[packed(i, j)] : 0.0;
+  // 1. FP32 Jacobi on A scaled by 2^-e (e from the largest diagonal entry)
+  float af = (float)a;
+  float dm = in && i == j ? fabsf(af) : 0.f;
+  for (int o = 16; o > 0; o >>= 1) dm = fmaxf(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+  int e2 = 0;
+  frexpf(dm > 0.f ? dm : 1.f, &e2);
+  const float scf = ldexpf(1.f, -e2);
+  af *= scf;
+  float vf = in ? (warm ? Vs[lane] : (i == j ? 1.f : 0.f)) : 0.f;
+  if (warm) {
+    if (in) Fs[lane] = af;
+    __syncwarp();
+    float x = 0.f;
+    if (in)
+      for (int k = 0; k < G; ++k) {
+        float t = 0.f;
+        for (int l = 0; l < G; ++l) t = fmaf(Fs[k * G + l], Vs[l * G + j], t);
+        x = fmaf(Vs[k * G + i], t, x);
+      }
+    __syncwarp();
+    if (in) Fs[lane] = x;
+    __syncwarp();
+    af = in ? 0.5f * (x + Fs[j * G + i]) : 0.f;
+    __syncwarp();
+  }
+  constexpr int Pe = G + (G & 1);
+  auto partner = [](int x, int r) {
+    constexpr int m = Pe - 1;
+    int p;
+    if (x == m) p = r;
+    else if (x == r) p = m;
+    else p = ((2 * r - x) % m + m) % m;
+    return p < G ? p : -1;
+  };
+  // With the previous date's V, V^T A V is usually close to diagonal.  When
+  // Gershgorin's bound puts every eigenvalue far above the cutoff (64 x
+  // rcond x the largest diagonal entry, plus 1e-5 of it for the FP32
+  // rounding of V^T A V), no direction is dropped and the FP64 stage below
+  // solves with that V exactly (any invertible V), so the sweeps are skipped.
+  bool sweep_needed = !warm;
+  if (warm) {
+    if (in) Fs[lane] = af;
+    __syncwarp();
+    float lo = 3.0e38f, hi = 0.f;
+    if (lane < G) {
+      float rad = 0.f;
+      for (int c = 0; c < G; ++c)
+        if (c != lane) rad += fabsf(Fs[lane * G + c]);
+      const float dg = Fs[lane * G + lane];
+      lo = dg - rad;
+      hi = fabsf(dg);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    sweep_needed = !(lo > (64.f * (float)rcond + 1e-5f) * hi);
+    __syncwarp();
+  }
+  float prev = 0.f;
+#pragma unroll 1
+  for (int sweep = 0; sweep < 30 && G > 1 && sweep_needed; ++sweep) {
+    float off = in && i != j ? af * af : 0.f, tot = in ? af * af : 0.f;
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    }
+    if (off <= 1e-12f * tot || off == 0.f) break;
+    if (sweep > 0 && off > 0.25f * prev) break;  // at the FP32 rounding floor
+    prev = off;
+#pragma unroll 1
+    for (int r = 0; r < Pe - 1; ++r) {
+      const int ip = partner(i, r), jp = partner(j, r);
+      const float2 rr = jacobi_rot_f32<G>(af, i, ip);
+      const float2 rc = jacobi_rot_f32<G>(af, j, jp);
+      const float cr = rr.x, sr = rr.y, cc = rc.x, sc2 = rc.y;
+      const int jj = jp < 0 ? j : jp, ii = ip < 0 ? i : ip;
+      const float a_ijp = __shfl_sync(0xffffffffu, af, i * G + jj);
+      const float a_ipj = __shfl_sync(0xffffffffu, af, ii * G + j);
+      const float a_ipjp = __shfl_sync(0xffffffffu, af, ii * G + jj);
+      const float v_ijp = __shfl_sync(0xffffffffu, vf, i * G + jj);
+      auto colr = [&](float self, float other) {
+        if (jp < 0) return self;
+        return j < jp ? cc * self - sc2 * other : sc2 * other + cc * self;
+      };
+      const float b_ij = colr(af, a_ijp), b_ipj = colr(a_ipj, a_ipjp);
+      float an = b_ij;
+      if (ip >= 0) an = i < ip ? cr * b_ij - sr * b_ipj : sr * b_ipj + cr * b_ij;
+      const float vn = colr(vf, v_ijp);
+      af = in ? an : 0.f;
+      vf = in ? vn : 0.f;
+    }
+  }
+  // 2. FP64: B = V^T A V (W = A V first) and u = V^T X'y, same instruction
+  //    stream for all lanes (per-lane operand pointers)
+  double* As = Ws + G * G;  // [G*G] A, then [G] u
+  if (in) {
+    Vs[lane] = vf;
+    As[lane] = a;
+  }
+  __syncwarp();
+  const double* rhs = sums + G * (G + 1) / 2;
+  {
+    double w = 0.0;
+    if (in)
+      for (int l = 0; l < G; ++l) w = fma(As[i * G + l], (double)Vs[l * G + j], w);
+    __syncwarp();
+    if (in) Ws[lane] = w;
+    __syncwarp();
+  }
+  const bool ul = lane >= G * G && lane < G * G + G;  // lanes computing u
+  {
+    double bsum = 0.0;
+    if (in || ul) {
+      const int col = in ? i : lane - G * G;
+      for (int k = 0; k < G; ++k)
+        bsum = fma((double)Vs[k * G + col], in ? Ws[k * G + j] : rhs[k], bsum);
+    }
+    if (in) Bs[lane] = bsum;
+    if (ul) Bs[lane] = bsum;  // u at Bs[G*G + k]
+    __syncwarp();
+  }
+  // 3. cutoff on the diagonal, kept block by elimination (row i in lane i)
+  double lmax = 0.0;
+  for (int k = 0; k < G; ++k) lmax = fmax(lmax, fabs(Bs[k * G + k]));
+  const double cutoff = rcond * lmax;
+  auto kept = [&](int k) { const double l = Bs[k * G + k]; return fabs(l) > cutoff && l != 0.0; };
+  double row[G + 1];
+  const int ri = lane < G ? lane : 0;
+  const bool kr = kept(ri);
+#pragma unroll
+  for (int c = 0; c < G; ++c) row[c] = kr && kept(c) ? Bs[ri * G + c] : (c == ri ? 1.0 : 0.0);
+  row[G] = kr ? Bs[G * G + ri] : 0.0;
+  double rcp[G];
+#pragma unroll
+  for (int p = 0; p < G; ++p) {
+    const double d = __shfl_sync(0xffffffffu, row[p], p);
+    double r0 = (double)__frcp_rn((float)d);
+    r0 = r0 * fma(-d, r0, 2.0);
+    r0 = r0 * fma(-d, r0, 2.0);
+    rcp[p] = r0;
+    const double f = row[p] * r0;
+#pragma unroll
+    for (int c = p + 1; c <= G; ++c) {
+      const double pc = __shfl_sync(0xffffffffu, row[c], p);
+      if (lane > p) row[c] = fma(-f, pc, row[c]);
+    }
+  }
+  // back substitution: x_i = (rhs_i - sum_{c > i} U_ic x_c) / U_ii
+  double x[G];
+#pragma unroll
+  for (int p = G - 1; p >= 0; --p) {
+    double t = __shfl_sync(0xffffffffu, row[G], p);
+#pragma unroll
+    for (int c = p + 1; c < G; ++c) t = fma(-__shfl_sync(0xffffffffu, row[c], p), x[c], t);
+    x[p] = t * rcp[p];
+  }
+  if (lane < G) {
+    double bt = 0.0;
+#pragma unroll
+    for (int k = 0; k < G; ++k) bt = fma((double)Vs[lane * G + k], x[k], bt);
+    __stcg(beta_out + lane, bt);
+  }
+  __syncwarp();
+}
+
+// Per-thread path state of the loop kernel lives in shared memory for the
+// whole loop: the K paths n = (blockIdx.x + k gridDim.x) C + tid of thread
+// tid keep cashflow, value and the states at the last accumulated date
+// (which the next date's update reads), [K][C] each, so a date reads only
+// its new exercise date from the gathered states.
+template <typename T, int DM>
+__host__ __device__ inline size_t lsm_loop_smem(int K) {
+  return (size_t)K * kLoopThreads * (2 + DM) * sizeof(T);
+}
+
+template <typename T, int DM, int GN>
+__global__ void __launch_bounds__(kLoopThreads, 2)
+    lsm_loop_kernel(tqf_lsm_args a, const T* __restrict__ xt, typename Acc<T>::S* __restrict__ partials,
+                    double* __restrict__ beta, const double* __restrict__ means, LoopSync* sy, int K) {
+  using A = Acc<T>;
+  using S = typename A::S;
+  constexpr int EN = GN * (GN + 1) / 2 + GN;
+  constexpr int C = kLoopThreads;
+  constexpr int KB = 8;  // paths per batch of loads
+  extern __shared__ __align__(16) unsigned char dsm[];
+  T* cs_ = reinterpret_cast<T*>(dsm);  // [K][C] cashflow
+  T* vs_ = cs_ + (size_t)K * C;        // [K][C] value
+  T* xs_ = vs_ + (size_t)K * C;        // [K][DM][C] states at the last accumulated date
+  __shared__ T beta_s[GN];
+  __shared__ T mu_s[2][kMaxDimLsm];
+  __shared__ S red[C / 32][EN];
+  __shared__ double sums_s[kLoopMaxEn];
+  __shared__ float Vs[kLoopMaxG * kLoopMaxG], Fs[kLoopMaxG * kLoopMaxG];
+  __shared__ double Ws[2 * kLoopMaxG * kLoopMaxG], Bs[kLoopMaxG * kLoopMaxG + kLoopMaxG];
+  __shared__ S rsum[16][16];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int d = a.dim, E = a.num_exercise;
+  const int64_t N = a.num_paths;
+  const T K_strike = static_cast<const T*>(a.strikes)[0];
+  const int64_t n_cal = a.num_calibration > 0 ? a.num_calibration : N;
+  const int64_t price_from = a.num_calibration > 0 ? a.num_calibration : 0;
+  const double eps = sizeof(T) == 4 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
+  const double rcond = 10.0 * GN * eps;
+  LsmCtx<T, DM> ctx{a, xt, 0, 0, GN, d, nullptr};
+  // basket put on the states (make_basket_put_payoff: relu(K - mean_d S))
+  auto pay = [&](const T* x) {
+    T sm = T(0);
+#pragma unroll
+    for (int c = 0; c < DM; ++c) sm += x[c];
+    const T v = K_strike - (DM == 1 ? sm : sm / (T)d);
+    return v > T(0) ? v : T(0);
+  };
+  auto load_x = [&](int date, int64_t n, T* x) {
+    const T* p = xt + ((int64_t)date * N + n) * d;
+#pragma unroll
+    for (int c = 0; c < DM; ++c) x[c] = p[c];
+  };
+  // centred basis: DM = 1 the powers of x; DM = 2 the exponent grid
+  // (g / (degree + 1), g % (degree + 1)) of make_polynomial_basis
+  const int deg = a.degree;
+  auto basis = [&](const T* xc, T* phi) {
+    if constexpr (DM == 1) {
+      phi[0] = T(1);
+#pragma unroll
+      for (int g = 1; g < GN; ++g) phi[g] = phi[g - 1] * xc[0];
+    } else {
+#pragma unroll
+      for (int g = 0; g < GN; ++g)
+        phi[g] = ipow(xc[0], (int)a.exponents[g * 2]) * ipow(xc[1], (int)a.exponents[g * 2 + 1]);
+    }
+  };
+  (void)deg;
+  unsigned gen = 0;
+  for (int step = 0;; ++step) {
+    const int init = step == 0;
+    const int upd = step == 0 ? 0 : E - step;
+    const int acc = E - 1 - step;
+    const int fin = acc < 1;
+    __syncthreads();
+    if (upd >= 1)
+      for (int g = tid; g < GN; g += C) beta_s[g] = (T)__ldcg(beta + g);
+    for (int i = tid; i < 2 * kMaxDimLsm; i += C) {
+      const int which = i / kMaxDimLsm, c = i % kMaxDimLsm;
+      const int idx = which == 0 ? upd : acc;
+      mu_s[which][c] = idx >= 1 ? (T)means[(size_t)(idx - 1) * kMaxDimLsm + c] : T(0);
+    }
+    __syncthreads();
+    const T r_upd = upd >= 1 && a.disc_stride_n == 0 ? ctx.ratio(upd, 0) : T(0);
+    const T r_acc = acc >= 1 && a.disc_stride_n == 0 ? ctx.ratio(acc, 0) : T(0);
+    const T r_fin = fin && a.disc_stride_n == 0 ? ctx.ratio(0, 0) : T(0);
+    T part[EN];
+    S acc2[EN];
+    int cnt = 0;
+#pragma unroll
+    for (int e = 0; e < EN; ++e) {
+      part[e] = T(0);
+      acc2[e] = A::zero();
+    }
+    S final_acc = A::zero();
+    for (int kb = 0; kb < K; kb += KB) {
+      // the batch's loads first (the new accumulation date, and at the start
+      // the last exercise date), so that they are in flight together
+      T xa[KB][DM], xi[KB][DM];
+#pragma unroll
+      for (int q = 0; q < KB; ++q) {
+        const int64_t n = ((int64_t)blockIdx.x + (int64_t)(kb + q) * gridDim.x) * C + tid;
+        const bool ok = kb + q < K && n < N;
+#pragma unroll
+        for (int c = 0; c < DM; ++c) xa[q][c] = xi[q][c] = T(0);
+        if (ok && acc >= 1) load_x(acc - 1, n, xa[q]);
+        if (ok && init) load_x(E - 1, n, xi[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < KB; ++q) {
+        const int k = kb + q;
+        const int64_t n = ((int64_t)blockIdx.x + (int64_t)k * gridDim.x) * C + tid;
+        if (k >= K || n >= N) continue;
+        const size_t o = (size_t)k * C + tid;
+        T c, v;
+        if (init) {
+          c = pay(xi[q]);
+          v = T(0);
+        } else {
+          c = cs_[o];
+          v = vs_[o];
+        }
+        if (upd >= 1) {
+          // continuation = relu(design . beta), exercise where payoff > continuation (lsm.py:380-400)
+          T xu[DM], xc[DM], phi[GN];
+#pragma unroll
+          for (int cc = 0; cc < DM; ++cc) {
+            xu[cc] = xs_[((size_t)k * DM + cc) * C + tid];
+            xc[cc] = xu[cc] - mu_s[0][cc];
+          }
+          const T evu = pay(xu);
+          basis(xc, phi);
+          T cont = T(0);
+#pragma unroll
+          for (int g = 0; g < GN; ++g) cont += phi[g] * beta_s[g];
+          cont = cont > T(0) ? cont : T(0);
+          const bool ex_now = evu > cont;
+          const T vn = ex_now ? T(0) : c + v;
+          c = ex_now ? evu : T(0);
+          v = ctx.ratio_at(upd, n, r_upd) * vn;
+        }
+        if (fin) {
+          if (n >= price_from) final_acc = A::add(final_acc, ctx.ratio_at(0, n, r_fin) * (c + v));
+          continue;
+        }
+        cs_[o] = c;
+        vs_[o] = v;
+#pragma unroll
+        for (int cc = 0; cc < DM; ++cc) xs_[((size_t)k * DM + cc) * C + tid] = xa[q][cc];
+        if (n < n_cal) {
+          // masked normal equations of exercise index acc (lsm.py:355-379)
+          const T cv = ctx.ratio_at(acc, n, r_acc) * (v + c);
+          const T eva = pay(xa[q]);
+          T xc[DM], phi[GN];
+#pragma unroll
+          for (int cc = 0; cc < DM; ++cc) xc[cc] = xa[q][cc] - mu_s[1][cc];
+          basis(xc, phi);
+          const bool use = eva > T(0);
+#pragma unroll
+          for (int g = 0; g < GN; ++g) phi[g] = use ? phi[g] : T(0);
+          int e = 0;
+#pragma unroll
+          for (int jj = 0; jj < GN; ++jj)
+#pragma unroll
+            for (int kk = jj; kk < GN; ++kk) part[e++] += phi[jj] * phi[kk];
+#pragma unroll
+          for (int jj = 0; jj < GN; ++jj) part[e++] += phi[jj] * cv;
+          if (++cnt == kSubSum) {
+#pragma unroll
+            for (int qq = 0; qq < EN; ++qq) {
+              acc2[qq] = A::add(acc2[qq], part[qq]);
+              part[qq] = T(0);
+            }
+            cnt = 0;
+          }
+        }
+      }
+    }
+    const int width = fin ? 1 : EN;
+    double* pout = reinterpret_cast<double*>(partials);
+    if (!fin) {
+      // the block reduction of lsm_pass_kernel's register mode
+#pragma unroll
+      for (int q = 0; q < EN; ++q) {
+        T t = (T)A::value(A::add(acc2[q], part[q]));
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) red[warp][q] = A::add(A::zero(), t);
+      }
+      __syncthreads();
+      for (int q = tid; q < EN; q += C) {
+        S t = A::zero();
+        for (int w = 0; w < C / 32; ++w) t = A::sum(t, red[w][q]);
+        __stcg(pout + (size_t)blockIdx.x * EN + q, *reinterpret_cast<double*>(&t));
+      }
+    } else {
+      for (int o = 16; o > 0; o >>= 1) final_acc = A::sum(final_acc, A::shfl_down(final_acc, o));
+      if (lane == 0) red[warp][0] = final_acc;
+      __syncthreads();
+      if (tid == 0) {
+        S t = A::zero();
+        for (int w = 0; w < C / 32; ++w) t = A::sum(t, red[w][0]);
+        __stcg(pout + blockIdx.x, *reinterpret_cast<double*>(&t));
+      }
+    }
+    if (!loop_barrier(sy, ++gen, a.dev_status)) return;
+    if (blockIdx.x == 0) {
+      // fixed-order reduction: thread (r, e), r < 16, sums rows r, r + 16, ...
+      // of entry e (eight loads in flight), then the 16 groups in order
+      const int e = tid & 15, r = tid >> 4;
+      S t = A::zero();
+      if (e < width) {
+        const int rows = (int)gridDim.x;
+        for (int row0 = r; row0 < rows; row0 += 128) {
+          double raw[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int row = row0 + 16 * q;
+            raw[q] = row < rows ? __ldcg(pout + (size_t)row * width + e) : 0.0;
+          }
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            if (row0 + 16 * q < rows) t = A::sum(t, *reinterpret_cast<const S*>(&raw[q]));
+        }
+      }
+      rsum[r][e] = t;
+      __syncthreads();
+      if (tid < width) {
+        S u = A::zero();
+        for (int q = 0; q < 16; ++q) u = A::sum(u, rsum[q][tid]);
+        sums_s[tid] = A::value(u);
+      }
+      __syncthreads();
+      if (fin) {
+        if (tid == 0) {
+          const int64_t count = a.num_calibration > 0 ? N - a.num_calibration : N;
+          a.out[0] = sums_s[0] * (1.0 / (double)count);
+        }
+      } else if (warp == 0) {
+        warp_pinv_solve<GN>(sums_s, rcond, acc < E - 1, Vs, Fs, Ws, Bs, beta);
+      }
+    }
+    if (fin) return;
+    if (!loop_barrier(sy, ++gen, a.dev_status)) return;
+  }
+}
+
+// The one-launch loop applies to structured calls with one payoff, one path
+// set, d <= 2 and 2..5 basis functions.
+__host__ inline bool lsm_loop_eligible(const tqf_lsm_args& a) {
+  return a.degree >= 0 && a.batch == 1 && a.paths_batch == 1 && a.dim >= 1 && a.dim <= 2 && a.num_basis >= 2 &&
+         a.num_basis <= kLoopMaxG && a.num_exercise >= 1;
+}
+
+template <typename T>
+__host__ void* loop_kernel_for(int d, int G) {
+  if (d == 1) {
+    switch (G) {
+      case 2: return reinterpret_cast<void*>(&lsm_loop_kernel<T, 1, 2>);
+      case 3: return reinterpret_cast<void*>(&lsm_loop_kernel<T, 1, 3>);
+      case 4: return reinterpret_cast<void*>(&lsm_loop_kernel<T, 1, 4>);
+      default: return reinterpret_cast<void*>(&lsm_loop_kernel<T, 1, 5>);
+    }
+  }
+  switch (G) {
+    case 2: return reinterpret_cast<void*>(&lsm_loop_kernel<T, 2, 2>);
+    case 3: return reinterpret_cast<void*>(&lsm_loop_kernel<T, 2, 3>);
+    case 4: return reinterpret_cast<void*>(&lsm_loop_kernel<T, 2, 4>);
+    default: return reinterpret_cast<void*>(&lsm_loop_kernel<T, 2, 5>);
+  }
+}
+
+// Grid and paths per thread (K) of the loop kernel: the largest resident
+// grid (2 or 1 CTAs per SM) whose per-thread path state fits
+// kLoopStateSmem of shared memory; 0 when none does (the per-date kernels
+// run instead).
+constexpr size_t kLoopStateSmem = 64 * 1024;
+
+__host__ int lsm_loop_config(const tqf_lsm_args& a, int* K_out, size_t* smem_out) {
+  if (!lsm_loop_eligible(a)) return 0;
+  const bool f32 = a.dtype == TQF_F32;
+  const void* k = f32 ? loop_kernel_for<float>(a.dim, a.num_basis) : loop_kernel_for<double>(a.dim, a.num_basis);
+  const int64_t chunks = (a.num_paths + kLoopThreads - 1) / kLoopThreads;
+  const size_t per_k = f32 ? (a.dim == 1 ? lsm_loop_smem<float, 1>(1) : lsm_loop_smem<float, 2>(1))
+                           : (a.dim == 1 ? lsm_loop_smem<double, 1>(1) : lsm_loop_smem<double, 2>(1));
+  for (int occ_try = 2; occ_try >= 1; --occ_try) {
+    int64_t g = (int64_t)num_sms() * occ_try;
+    if (g > chunks) g = chunks;
+    if (g < 1) g = 1;
+    const int64_t K = (chunks + g - 1) / g;
+    const size_t smem = (size_t)K * per_k;
+    if (smem > kLoopStateSmem) continue;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLoopStateSmem) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kLoopThreads, smem) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    if ((int64_t)occ * num_sms() < g) continue;  // cooperative launch needs every CTA resident
+    if (K_out) *K_out = (int)K;
+    if (smem_out) *smem_out = smem;
+    return (int)g;
+  }
+  return 0;
+}
+
+__host__ int lsm_loop_grid(const tqf_lsm_args& a) { return lsm_loop_config(a, nullptr, nullptr); }
+
+// Cooperative launch of the whole date loop (all CTAs resident).
+int launch_loop(const tqf_lsm_args& a, cudaStream_t s) {
+  const WsLayout L = lsm_layout(a);
+  unsigned char* ws = static_cast<unsigned char*>(a.workspace);
+  int K = 0;
+  size_t smem = 0;
+  const int grid = lsm_loop_config(a, &K, &smem);
+  TQF_REQUIRE(grid >= 1, "tqf_lsm_price: the one-launch loop does not apply");
+  LoopSync* sy = reinterpret_cast<LoopSync*>(ws + L.sync);
+  int rc = check_cuda(cudaMemsetAsync(sy, 0, sizeof(LoopSync), s), "tqf_lsm_price: cudaMemsetAsync");
+  if (rc) return rc;
+  const bool f32 = a.dtype == TQF_F32;
+  void* k = f32 ? loop_kernel_for<float>(a.dim, a.num_basis) : loop_kernel_for<double>(a.dim, a.num_basis);
+  tqf_lsm_args args = a;
+  const void* xt = ws + L.xt;
+  void* partials = ws + L.partials;
+  double* beta = reinterpret_cast<double*>(ws + L.beta);
+  const double* means = reinterpret_cast<const double*>(ws + L.means);
+  void* params[] = {&args, const_cast<void**>(&xt), &partials, &beta, const_cast<double**>(&means), &sy, &K};
+  rc = check_cuda(cudaLaunchCooperativeKernel(k, dim3((unsigned)grid), dim3(kLoopThreads), params, smem, s),
+                  "lsm_loop_kernel cooperative launch");
+  if (rc) return rc;
+  note_launch();
+  return TQF_OK;
+}
+
 constexpr int kMaxWarmBasis = 64;  // warm start needs a second [G][G+1] buffer
 
 size_t solve_smem(int G) {
@@ -1018,8 +1640,13 @@ extern "C" int tqf_lsm_price(const tqf_lsm_args* args, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   tqf_lsm_args a = *args;
   const bool f32 = a.dtype == TQF_F32;
+  {
+    const int64_t count = a.num_calibration > 0 ? a.num_paths - a.num_calibration : a.num_paths;
+    TQF_REQUIRE(count >= 1, "tqf_lsm_price: no paths left to price after calibration");
+  }
   rc = f32 ? launch_gather<float>(a, s) : launch_gather<double>(a, s);
   if (rc) return rc;
+  if (lsm_loop_grid(a) >= 1) return launch_loop(a, s);
   auto pass = [&](int init, int upd, int acc, int fin) {
     a.init = init;
     a.upd_index = upd;

@@ -372,7 +372,7 @@ constexpr size_t kWideLSmem = 96 * 1024;
 
 template <typename T, bool LS>
 __global__ void __launch_bounds__(kBlock) mvgbm_paths_wide_kernel(tqf_mvgbm_args a) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(1024) unsigned char smem[];
   const int dim = a.dim;
   const size_t dd = (size_t)dim * dim;
   const T* gL = static_cast<const T*>(a.chol);
@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_wide_kernel(tqf_mvgbm_args
 // accumulators in shared memory hold [P, P^2, g_i, g_i (y_i - sigma_i T)].
 template <typename T, bool LS>
 __global__ void __launch_bounds__(kBlock) basket_price_wide_kernel(tqf_basket_args a) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(1024) unsigned char smem[];
   const int dim = a.dim;
   const size_t dd = (size_t)dim * dim;
   const T* gL = static_cast<const T*>(a.chol);
