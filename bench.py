@@ -105,11 +105,14 @@ def run_cpu_baseline(steps, warmup, budget_s=12.0):
     ctx = mp.get_context("spawn")
     paths_per_core = 4096
     with ctx.Pool(cores) as pool:
-        # calibrate the sample so that one step takes about budget_s / steps
-        units, wall = cpu_reference_step(pool, cores, 512, N_STEPS, 0)
+        # calibrate the sample so that one step takes about budget_s / steps,
+        # on a warm pool (the first round pays the workers' imports), and
+        # never below 8192 paths per worker (pool dispatch stays a small share)
+        cpu_reference_step(pool, cores, 512, N_STEPS, 0)
+        units, wall = cpu_reference_step(pool, cores, 2048, N_STEPS, 0)
         rate = units / wall
         target = max(budget_s / max(steps + warmup, 1), 0.5)
-        paths_per_core = int(max(256, min(1 << 16, rate * target / (cores * N_STEPS))))
+        paths_per_core = int(max(8192, min(1 << 16, rate * target / (cores * N_STEPS))))
         for w in range(warmup):
             cpu_reference_step(pool, cores, paths_per_core, N_STEPS, 1 + w)
         tot_units, tot_wall = 0, 0.0
