@@ -363,19 +363,22 @@ def run_gpu(args, rank, world, local_rank):
     return line
 
 
-def run_neural_cv(pilot_paths=1 << 20, train_steps=2000, eval_paths=1 << 26, batch_paths=512):
+def run_neural_cv(pilot_paths=1 << 20, train_steps=600, eval_paths=1 << 26, batch_paths=1024, lr=3e-3,
+                  control_every=2):
     """Config C5: Heston arithmetic-Asian call (52 dates, K=100) — pilot paths,
-    2,000 Adam steps (lr 1e-3) on the tcgen05 training kernels, then fused CV
-    pricing vs plain MC on the same evaluation paths; time to a 1e-4 relative
-    95% CI for both (GPU seconds, CUDA events), with and without training."""
+    600 Adam steps (lr 3e-3, 1,024-path minibatches) on the tcgen05 training
+    kernels, then fused CV pricing vs plain MC on the same evaluation paths;
+    the network's position is rebalanced at every second monitoring date
+    (26 evaluations per path).  Time to a 1e-4 relative 95% CI for both (GPU
+    seconds, CUDA events), with and without pilot and training."""
     import torch
     from tqf.pricing import HestonAsianCV, time_to_ci
     cv = HestonAsianCV(spot=100.0, variance=0.04, mean_reversion=2.0, theta=0.04, volvol=0.3, rho=-0.7, rate=0.02,
-                       expiry=1.0, strike=100.0, num_dates=52, num_time_steps=252)
+                       expiry=1.0, strike=100.0, num_dates=52, num_time_steps=252, control_every=control_every)
     cv.pilot(pilot_paths, seed=(977, 5))
     cv.price(1 << 16, control_variate=False, seed=(1, 1))  # warm-up of both pricing kernels
     cv.price(1 << 16, control_variate=True, seed=(1, 1))
-    losses = cv.train(steps=train_steps, batch_paths=batch_paths)
+    losses = cv.train(steps=train_steps, batch_paths=batch_paths, lr=lr)
     plain = cv.price(eval_paths, control_variate=False, seed=(31, 41))
     est = cv.price(eval_paths, control_variate=True, seed=(31, 41))
     t_plain = time_to_ci(plain)
@@ -384,7 +387,9 @@ def run_neural_cv(pilot_paths=1 << 20, train_steps=2000, eval_paths=1 << 26, bat
     torch.cuda.synchronize()
     return {
         "config": "Heston FT-Euler FP32, 252 steps, arithmetic Asian 52 dates, K=100; MLP 3-64-64-1 SiLU BF16, "
-                  f"{pilot_paths} pilot paths, {train_steps} Adam steps x {batch_paths} paths, {eval_paths} eval paths",
+                  f"control rebalanced every {control_every} dates ({cv.num_control} evaluations per path), "
+                  f"{pilot_paths} pilot paths, {train_steps} Adam steps (lr {lr}) x {batch_paths} paths, "
+                  f"{eval_paths} eval paths",
         "price_cv": est.price, "se_cv": est.standard_error, "price_plain": plain.price, "se_plain": plain.standard_error,
         "vrf": est.vrf, "bias_in_se": (est.price - plain.price) / plain.standard_error,
         "mean_control_in_se": est.mean_control / est.se_control,
@@ -793,8 +798,10 @@ def main():
     ap.add_argument("--no-neural-cv", action="store_true")
     ap.add_argument("--cv-only", action="store_true", help="run only the neural-CV measurement (small sizes ok)")
     ap.add_argument("--cv-eval-paths", type=int, default=1 << 26)
-    ap.add_argument("--cv-train-steps", type=int, default=2000)
-    ap.add_argument("--cv-batch", type=int, default=512, help="pilot paths per Adam step")
+    ap.add_argument("--cv-train-steps", type=int, default=600)
+    ap.add_argument("--cv-batch", type=int, default=1024, help="pilot paths per Adam step")
+    ap.add_argument("--cv-lr", type=float, default=3e-3, help="Adam learning rate of the control-variate network")
+    ap.add_argument("--cv-every", type=int, default=2, help="rebalance the control every n-th monitoring date")
     ap.add_argument("--no-basket", action="store_true")
     ap.add_argument("--basket-only", action="store_true", help="run only the 16-asset basket measurement")
     ap.add_argument("--basket-paths", type=int, default=1 << 22)
@@ -857,7 +864,8 @@ def main():
         return
     if args.cv_only:
         print(json.dumps({"neural_cv": run_neural_cv(eval_paths=args.cv_eval_paths, train_steps=args.cv_train_steps,
-                                                  batch_paths=args.cv_batch)}))
+                                                  batch_paths=args.cv_batch, lr=args.cv_lr,
+                                                  control_every=args.cv_every)}))
         return
     if world > 1:
         import torch
@@ -873,7 +881,8 @@ def main():
     line = run_gpu(args, rank, world, local_rank)
     if rank == 0 and world == 1 and not args.no_neural_cv:
         line["neural_cv"] = run_neural_cv(eval_paths=args.cv_eval_paths, train_steps=args.cv_train_steps,
-                                                  batch_paths=args.cv_batch)
+                                                  batch_paths=args.cv_batch, lr=args.cv_lr,
+                                                  control_every=args.cv_every)
     if rank == 0 and world == 1 and not args.no_basket:
         line["basket"] = run_basket(paths_n=args.basket_paths)
     if rank == 0 and world == 1 and not args.no_sobol:

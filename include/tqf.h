@@ -623,15 +623,22 @@ typedef struct tqf_mlp_weights {
  * slot -2 as "advance the network pipeline one stage here"; two such steps
  * between consecutive dates let the tensor-core work overlap the stepping
  * (without them every stage runs at the date).  date_table
- * [num_dates][4] = (t_k, exp(-r t_k), 0, 0).
+ * [num_dates][4] = (t_k, exp(-r t_k), hold_k, 0).  The control's intervals
+ * run between the control dates: the monitoring dates with hold_k = 0, and
+ * always the last date.  At a date with hold_k != 0 the network's position
+ * carries over (no evaluation ends or starts there); with every hold_k = 0
+ * the network is evaluated at every monitoring interval.  D_c below is the
+ * number of control dates.
  *  mode 0: out[5] (device, FP64) = sums of (Y, Y^2, 0, 0, 0);
  *  mode 1: pilot data, date-major so that the stores coalesce:
- *          pilot_feats [num_dates][N][4] = (t, log S, v, 0) at each interval
- *          start, pilot_dS [num_dates][N] discounted-spot increments,
- *          pilot_Y [N];
- *  mode 2: out[5] = sums of (Y, Y^2, C, C^2, Y C), C = sum_k g_k dS~_k the
+ *          pilot_feats [D_c][N][4] = (t, log S, v, 0) at each control
+ *          interval start, pilot_dS [D_c][N] discounted-spot increments over
+ *          the control intervals, pilot_Y [N];
+ *  mode 2: out[5] = sums of (Y, Y^2, C, C^2, Y C), C = sum_j g_j dS~_j the
  *          martingale control variate with the network evaluated on the
- *          tensor cores at every interval start.
+ *          tensor cores at every control interval start.
+ * Modes 0 and 2 also write, when path_values is non-null (8-byte aligned),
+ * each path's (Y, C) as float pairs [N][2] (C = 0 in mode 0).
  * Estimator of the price: mean(Y - C). */
 typedef struct tqf_heston_asian_args {
   int32_t mode;
@@ -654,6 +661,7 @@ typedef struct tqf_heston_asian_args {
   void* workspace;
   size_t workspace_bytes;
   int32_t* dev_status;
+  float* path_values; /* optional [N][2] per-path (Y, C), modes 0 and 2 */
 } tqf_heston_asian_args;
 
 TQF_API int tqf_heston_asian(const tqf_heston_asian_args* args, void* stream);

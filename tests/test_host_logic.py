@@ -139,6 +139,24 @@ def test_cv_pipeline_stage_marks():
     assert len(m) == 2 * 52 and np.all(np.diff(m) > 0)
 
 
+def test_cv_control_dates_and_marks_around_held_dates():
+    """Control dates: every n-th monitoring date counted back from the last;
+    the pipeline marks of the longer control intervals avoid the held dates."""
+    from tqf.pricing.neural_cv import control_dates, stage_marks
+    assert control_dates(52, 1).tolist() == list(range(52))
+    assert control_dates(52, 2).tolist() == list(range(1, 52, 2))
+    assert control_dates(5, 3).tolist() == [1, 4]
+    with pytest.raises(ValueError):
+        control_dates(4, 0)
+    ti = np.round(np.arange(1, 53) * 252 / 52).astype(int)
+    cd = control_dates(52, 2)
+    m = stage_marks(ti[cd] - 1, busy=ti - 1)
+    assert len(m) == 2 * 26 and np.all(np.diff(m) > 0)
+    assert not set(m.tolist()) & set((ti - 1).tolist())
+    # a held date at the natural mark moves the mark to the nearest free step
+    assert stage_marks([6], busy=[1, 4]).tolist() == [2, 3]
+
+
 def test_reference_wrong_times_and_sample_shape_mismatch():
     # euler_sampling_test.py:503-572: with validate_args, non-increasing times
     # or times_grid and draws that do not match the grid raise

@@ -11,13 +11,16 @@
 // The backward GEMMs (Q2 W2, dW2, db2, dw3, dW1) are tcgen05 MMAs as well.
 //
 // heston_asian_kernel<MODE>: full-truncation Euler paths (Philox in-kernel),
-//   num_dates monitoring dates marked in the step table's slot column.
+//   num_dates monitoring dates marked in the step table's slot column; the
+//   control dates are the monitoring dates the date table does not mark
+//   "hold", and the last date.
 //   MODE 0: plain estimator sums of Y = e^{-rT} max(mean_k S_k - K, 0).
-//   MODE 1: pilot data — per path and interval k the start features
-//           (t_k, log S_k, v_k), the discounted-spot increment
-//           dS~_k = e^{-r t_{k+1}} S_{k+1} - e^{-r t_k} S_k, and Y.
-//   MODE 2: fused control variate C = sum_k g(t_k, X_k, V_k) dS~_k with the
-//           network evaluated per warpgroup tile at every interval start.
+//   MODE 1: pilot data — per path and control interval j the start features
+//           (t_j, log S_j, v_j), the discounted-spot increment
+//           dS~_j = e^{-r t_{j+1}} S_{j+1} - e^{-r t_j} S_j, and Y.
+//   MODE 2: fused control variate C = sum_j g(t_j, X_j, V_j) dS~_j with the
+//           network evaluated per warpgroup tile at every control interval
+//           start (held over the monitoring dates in between).
 //   Modes 0/2 accumulate (Y, Y^2, C, C^2, Y C) in FP64 (fixed order).
 //   Under the log-Euler step E[S~_{i+1} | F_i] = S~_i, so E[C] = 0 exactly.
 // mlp_train_step_kernel: one Adam step's gradient for a minibatch of paths,
@@ -79,6 +82,17 @@ __device__ __forceinline__ uint32_t silu_bf16x2(float a, float b) {
   const uint32_t x2 = pack_bf16x2(a, b);
   uint32_t h2, t2, s2;
   asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(h2) : "r"(x2), "r"(0x3F003F00u));
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t2) : "r"(h2));
+  asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(s2) : "r"(h2), "r"(t2), "r"(h2));
+  return s2;
+}
+
+// The same SiLU from the halved pre-activations h = x/2 (the inference tiles
+// hold W1, W2 and b2 scaled by 1/2, which is exact in BF16 and in the FP32
+// accumulation, so bf16(x/2) = bf16(x)/2 bit for bit): one multiply fewer.
+__device__ __forceinline__ uint32_t silu_half_bf16x2(float ha, float hb) {
+  const uint32_t h2 = pack_bf16x2(ha, hb);
+  uint32_t t2, s2;
   asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t2) : "r"(h2));
   asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(s2) : "r"(h2), "r"(t2), "r"(h2));
   return s2;
@@ -195,9 +209,10 @@ __device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t* r) {
       : "r"(taddr));
 }
 
-// SiLU of this row's 64 TMEM accumulators (packed BF16) into row r of sH,
-// 16 columns per TMEM round trip (fewer live registers than 32 at a time,
-// which measured faster at this kernel's 64-register budget).
+// SiLU of this row's 64 TMEM accumulators (halved pre-activations, packed
+// BF16) into row r of sH, 16 columns per TMEM round trip (fewer live
+// registers than 32 at a time, which measured faster at this kernel's
+// 64-register budget).
 __device__ __forceinline__ void silu_row_from_tmem(uint32_t taddr, unsigned char* sH, int r) {
 #pragma unroll
   for (int c = 0; c < kH; c += 16) {
@@ -210,8 +225,8 @@ __device__ __forceinline__ void silu_row_from_tmem(uint32_t taddr, unsigned char
 #pragma unroll
     for (int h = 0; h < 16; h += 8)
       *reinterpret_cast<uint4*>(sH + tc::kmajor_off(r, c + h, kHLbo, kHSbo)) =
-          make_uint4(silu_bf16x2(acc[h], acc[h + 1]), silu_bf16x2(acc[h + 2], acc[h + 3]),
-                     silu_bf16x2(acc[h + 4], acc[h + 5]), silu_bf16x2(acc[h + 6], acc[h + 7]));
+          make_uint4(silu_half_bf16x2(acc[h], acc[h + 1]), silu_half_bf16x2(acc[h + 2], acc[h + 3]),
+                     silu_half_bf16x2(acc[h + 4], acc[h + 5]), silu_half_bf16x2(acc[h + 6], acc[h + 7]));
   }
 }
 
@@ -278,15 +293,16 @@ __device__ __forceinline__ float eval_finish(int wg, int tid, const MlpConst& wc
   return __uint_as_float(r0) + __uint_as_float(r1) + wc.b3;
 }
 
-// Weight tiles of the inference pipeline from the constant-bank copy.
+// Weight tiles of the inference pipeline from the constant-bank copy; W1
+// (with b1) and b2 halved, so that layers 1 and 2 produce x/2 for the SiLU.
 __device__ __forceinline__ void build_eval_tiles(const MlpConst& wc, unsigned char* sW1, unsigned char* sB2,
                                                  unsigned char* sW3) {
   for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x) {
     const int n = i >> 4, k = i & 15;
     const float4 l = wc.l1[n];
-    const float w = k == 0 ? l.x : k == 1 ? l.y : k == 2 ? l.z : k == 3 ? l.w : 0.f;
+    const float w = 0.5f * (k == 0 ? l.x : k == 1 ? l.y : k == 2 ? l.z : k == 3 ? l.w : 0.f);
     const float hi = round_bf16(wc.b2[n]);
-    const float b = k == 3 ? hi : k == 4 ? wc.b2[n] - hi : 0.f;
+    const float b = 0.5f * (k == 3 ? hi : k == 4 ? wc.b2[n] - hi : 0.f);
     __nv_bfloat16 wb = __float2bfloat16_rn(w), bb = __float2bfloat16_rn(b);
     *reinterpret_cast<__nv_bfloat16*>(sW1 + tc::kmajor_off(n, k, kW1Lbo, kW1Sbo)) = wb;
     *reinterpret_cast<__nv_bfloat16*>(sB2 + tc::kmajor_off(n, k, kW1Lbo, kW1Sbo)) = bb;
@@ -306,6 +322,8 @@ struct AsianSmem {
   uint32_t pad;
   double acc[kPathThreads / 32][5];
   float date_t[kMaxDates], date_disc[kMaxDates];
+  int date_cv[kMaxDates];  // control interval ending at date k, or -1 (held)
+  int num_cv;              // control dates
 };
 
 // Mode 2 pipelines the network with the simulation: the evaluation for
@@ -333,6 +351,11 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : kPlai
     S->date_t[i] = a.date_table[4 * i];
     S->date_disc[i] = a.date_table[4 * i + 1];
   }
+  if (threadIdx.x == 0) {
+    int j = 0;
+    for (int k = 0; k < D; ++k) S->date_cv[k] = (k + 1 < D && a.date_table[4 * k + 2] != 0.f) ? -1 : j++;
+    S->num_cv = j;
+  }
   for (int i = threadIdx.x; i < (kPathThreads / 32) * 5; i += blockDim.x) (&S->acc[0][0])[i] = 0.0;
   if (MODE != 2)
     for (int p = threadIdx.x; p < (a.num_steps + 1) / 2; p += blockDim.x)
@@ -340,8 +363,11 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : kPlai
   EvalPipe P;
   if (MODE == 2) {
     const uint4* w2 = static_cast<const uint4*>(a.mlp.w2_bf16);
-    for (int i = threadIdx.x; i < kH * kH / 8; i += blockDim.x)
-      *reinterpret_cast<uint4*>(sW2 + tc::kmajor_off(i >> 3, 8 * (i & 7), kW2Lbo, kW2Sbo)) = w2[i];
+    for (int i = threadIdx.x; i < kH * kH / 8; i += blockDim.x) {
+      const uint4 q = w2[i];  // halved (exact in BF16)
+      *reinterpret_cast<uint4*>(sW2 + tc::kmajor_off(i >> 3, 8 * (i & 7), kW2Lbo, kW2Sbo)) =
+          make_uint4(bf2_mul(q.x, kBf2Half), bf2_mul(q.y, kBf2Half), bf2_mul(q.z, kBf2Half), bf2_mul(q.w, kBf2Half));
+    }
     build_eval_tiles(wc, sW1, sB2, sW3);
     for (int i = threadIdx.x; i < 2 * (kXBytes + kHBytes) / 16; i += blockDim.x)
       reinterpret_cast<uint4*>(sWg)[i] = make_uint4(0u, 0u, 0u, 0u);
@@ -368,6 +394,7 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : kPlai
   const float K = (float)a.strike, discT = (float)a.discount_T, x0 = (float)a.x0, v0 = (float)a.v0;
   const float S0 = __expf(x0);
   const float inv_D = 1.f / (float)D;
+  const int Dc = S->num_cv;
   const int64_t N = a.num_paths;
   const int64_t per_round = (int64_t)gridDim.x * kPathThreads;
   for (int64_t base = 0; base < N; base += per_round) {
@@ -387,19 +414,22 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : kPlai
       }
       if (k >= 0) {
         const float Sk = __expf(x);
-        const float dsk = S->date_disc[k] * Sk - prev;
         avg += Sk;
-        if (MODE == 2) {
-          const float g = eval_finish(wg, tid, wc, P, sW2, sB2, sW3, a.dev_status);
-          cv = fmaf(g, dsk, cv);
+        const int j = MODE == 0 ? -1 : S->date_cv[k];
+        if (j >= 0) {
+          const float dsk = S->date_disc[k] * Sk - prev;
+          if (MODE == 2) {
+            const float g = eval_finish(wg, tid, wc, P, sW2, sB2, sW3, a.dev_status);
+            cv = fmaf(g, dsk, cv);
+          }
+          if (MODE == 1 && valid) {
+            a.pilot_dS[j * N + path] = dsk;
+            if (j + 1 < Dc)
+              reinterpret_cast<float4*>(a.pilot_feats)[(j + 1) * N + path] = make_float4(S->date_t[k], x, v, 0.f);
+          }
+          prev = S->date_disc[k] * Sk;
+          if (MODE == 2 && j + 1 < Dc) eval_issue_l1(wg, tid, wc, P, sW1, S->date_t[k], x, v);
         }
-        if (MODE == 1 && valid) {
-          a.pilot_dS[k * N + path] = dsk;
-          if (k + 1 < D)
-            reinterpret_cast<float4*>(a.pilot_feats)[(k + 1) * N + path] = make_float4(S->date_t[k], x, v, 0.f);
-        }
-        prev = S->date_disc[k] * Sk;
-        if (MODE == 2 && k + 1 < D) eval_issue_l1(wg, tid, wc, P, sW1, S->date_t[k], x, v);
       }
     };
     // steps 2 pb and 2 pb + 1 from Philox block pb, in f32x2 pairs
@@ -449,6 +479,7 @@ __global__ void __launch_bounds__(kPathThreads, MODE == 2 ? kCvCtasPerSm : kPlai
     if (MODE == 1) {
       if (valid) a.pilot_Y[path] = Y;
     } else {
+      if (a.path_values != nullptr && valid) reinterpret_cast<float2*>(a.path_values)[path] = make_float2(Y, cv);
       float q[5];
       q[0] = valid ? Y : 0.f;
       q[1] = q[0] * q[0];
@@ -956,6 +987,7 @@ extern "C" int tqf_heston_asian(const tqf_heston_asian_args* a, void* stream) {
     TQF_REQUIRE(a->mlp.w2_bf16 && a->mlp.host, "tqf_heston_asian: network weights required (w2_bf16, host)");
   if (a->mode == 2)
     TQF_REQUIRE((reinterpret_cast<uintptr_t>(a->mlp.w2_bf16) & 15u) == 0, "tqf_heston_asian: w2_bf16 must be 16-byte aligned");
+  TQF_REQUIRE((reinterpret_cast<uintptr_t>(a->path_values) & 7u) == 0, "tqf_heston_asian: path_values must be 8-byte aligned");
   const size_t smem = asian_smem_bytes(a->mode, a->num_steps);
   TQF_REQUIRE(smem <= 227 * 1024, "tqf_heston_asian: step table too large for shared memory");
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -403,6 +403,7 @@ class HestonAsianArgs(ctypes.Structure):
         ("workspace", c_vp),
         ("workspace_bytes", ctypes.c_size_t),
         ("dev_status", c_vp),
+        ("path_values", c_vp),
     ]
 
 

@@ -3,8 +3,10 @@
 Pipeline, all on the GPU through libtqf.so:
 
 1. ``pilot``: full-truncation Euler paths (``tqf_heston_asian`` mode 1) give,
-   per path and monitoring interval k, the start features (t_k, log S_k, v_k),
-   the discounted-spot increment dS~_k and the discounted payoff Y.
+   per path and control interval j, the start features (t_j, log S_j, v_j),
+   the discounted-spot increment dS~_j and the discounted payoff Y.  The
+   control dates are every ``control_every``-th monitoring date counted back
+   from the last; the network's position is held over the dates in between.
 2. ``train``: the MLP g (3 -> 64 -> 64 -> 1, SiLU, BF16 weights, FP32
    accumulation) minimises mean_p (Y_p - c - sum_k g_pk dS~_pk)^2 with Adam
    (``tqf_mlp_train_step`` on tcgen05 tensor cores + ``tqf_mlp_adam``).
@@ -60,23 +62,38 @@ class AsianEstimate:
     se_control: float = 0.0
 
 
-def stage_marks(date_steps) -> np.ndarray:
+def stage_marks(date_steps, busy=()) -> np.ndarray:
     """Steps at which the fused inference advances its network pipeline.
 
-    The evaluation for interval k starts after step date_steps[k-1] (before
-    step 0 for k = 0) and must be complete after step date_steps[k]; its two
-    middle stages run about a third and two thirds of the way between, at
-    steps strictly inside the interval (none when the interval is too short:
-    the kernel then runs them at the date)."""
+    The evaluation for control interval j starts after step date_steps[j-1]
+    (before step 0 for j = 0) and must be complete after step date_steps[j];
+    its two middle stages run at the free steps strictly inside the interval
+    nearest a third and two thirds of the way between.  ``busy`` steps (the
+    other monitoring dates) carry a date slot and are never marked; without a
+    free step the kernel runs the stage at the date."""
+    busy = set(int(b) for b in np.asarray(busy, dtype=np.int64).reshape(-1).tolist())
     marks = []
     prev = -1
     for s in np.asarray(date_steps, dtype=np.int64).tolist():
         gap = s - prev
-        a = prev + max(1, int(round(gap / 3.0)))
-        b = prev + max(a - prev + 1, int(round(2.0 * gap / 3.0)))
-        marks += [m for m in (a, b) if prev < m < s]
+        free = [m for m in range(prev + 1, s) if m not in busy]
+        chosen = []
+        for target in (prev + gap / 3.0, prev + 2.0 * gap / 3.0):
+            cands = [m for m in free if not chosen or m > chosen[-1]]
+            if cands:
+                chosen.append(min(cands, key=lambda m: (abs(m - target), m)))
+        marks += chosen
         prev = s
     return np.asarray(marks, dtype=np.int64)
+
+
+def control_dates(num_dates: int, every: int) -> np.ndarray:
+    """Indices of the monitoring dates that end a control interval: every
+    ``every``-th date counted back from the last (which always ends one)."""
+    if every < 1:
+        raise ValueError("control_every must be >= 1")
+    k = np.arange(num_dates)
+    return k[(num_dates - 1 - k) % every == 0]
 
 
 def _bf16_bits(x: torch.Tensor) -> torch.Tensor:
@@ -89,7 +106,7 @@ class HestonAsianCV:
 
     def __init__(self, *, spot=100.0, variance=0.04, mean_reversion=2.0, theta=0.04, volvol=0.3, rho=-0.7,
                  rate=0.02, expiry=1.0, strike=100.0, num_dates=52, num_time_steps=252, init_seed=0,
-                 pipeline_stages=True):
+                 pipeline_stages=True, control_every=1):
         self.device = _lib.require_cuda()
         d = self.device
         self.spot, self.v0, self.kappa, self.theta, self.xi, self.rho = spot, variance, mean_reversion, theta, volvol, rho
@@ -103,8 +120,11 @@ class HestonAsianCV:
             raise ValueError("monitoring dates must map to distinct grid points after t = 0")
         slots = np.full(self.num_steps, -1, np.int32)
         slots[ti - 1] = np.arange(self.num_dates)  # state after step i is at grid point i + 1
+        self.control_every = int(control_every)
+        self.control_dates = control_dates(self.num_dates, self.control_every)
+        self.num_control = len(self.control_dates)
         if pipeline_stages:
-            slots[stage_marks(ti - 1)] = -2
+            slots[stage_marks(ti[self.control_dates] - 1, busy=ti - 1)] = -2
         dt = (grid[1:] - grid[:-1]).astype(f32)
         coef = HestonFullTruncation(rate, mean_reversion, theta, volvol, rho)
         rows = heston_model.full_truncation_table(coef, grid, dt, np.sqrt(dt).astype(f32), slots, self.num_steps)
@@ -113,6 +133,8 @@ class HestonAsianCV:
         dtab = np.zeros((self.num_dates, 4), np.float32)
         dtab[:, 0] = t_dates
         dtab[:, 1] = np.exp(-rate * t_dates)
+        dtab[:, 2] = 1.0  # hold the network's position over the date ...
+        dtab[self.control_dates, 2] = 0.0  # ... except at the control dates
         self.date_table = torch.as_tensor(dtab).to(d)
         self.dates = t_dates
         self.discount_T = float(np.exp(-rate * float(grid[-1])))
@@ -120,8 +142,8 @@ class HestonAsianCV:
         self.feat_shift = [0.0, math.log(spot), theta]
         self.feat_scale = [1.0 / expiry, 1.0 / math.sqrt(theta * expiry),
                            1.0 / max(volvol * math.sqrt(theta / (2 * mean_reversion)), 1e-6)]
-        # one training CTA holds whole paths in one 128-row tile
-        self.train_paths_per_cta = max(1, 128 // self.num_dates)
+        # one training CTA holds whole paths (all their control intervals) in one 128-row tile
+        self.train_paths_per_cta = max(1, 128 // self.num_control)
         self._init_params(init_seed)
         self.loss_history: list[float] = []
         self.train_seconds = 0.0
@@ -189,7 +211,7 @@ class HestonAsianCV:
     # ---- stages ------------------------------------------------------------------
     def pilot(self, num_paths=1 << 20, seed=(977, 5)):
         d = self.device
-        D = self.num_dates
+        D = self.num_control
         # date-major storage (coalesced stores in the path kernel); the
         # attributes are [N, D, ...] views of it
         self._feats_dm = torch.empty((D, num_paths, 4), dtype=torch.float32, device=d)
@@ -211,7 +233,7 @@ class HestonAsianCV:
 
     def _train_args(self, path_begin, batch_paths, partials):
         t = _lib.MlpTrainArgs()
-        t.num_dates = self.num_dates
+        t.num_dates = self.num_control
         t.batch_paths = int(batch_paths)
         t.paths_per_cta = self.train_paths_per_cta
         t.path_begin = int(path_begin)
@@ -311,7 +333,10 @@ class HestonAsianCV:
         self.loss_history = losses.cpu().tolist()
         return self.loss_history
 
-    def price(self, num_paths, control_variate=True, seed=(31, 41), path_offset=0) -> AsianEstimate:
+    def price(self, num_paths, control_variate=True, seed=(31, 41), path_offset=0, path_values=None) -> AsianEstimate:
+        """Fresh paths: plain MC (control_variate=False) or the fused control
+        variate.  ``path_values`` (optional float32 [num_paths, 2] device
+        tensor) receives each path's (Y, C)."""
         d = self.device
         mode = 2 if control_variate else 0
         out = torch.zeros(5, dtype=torch.float64, device=d)
@@ -321,6 +346,11 @@ class HestonAsianCV:
         if control_variate:
             a.mlp = self._mlp_struct()
         a.out = out.data_ptr()
+        if path_values is not None:
+            if (path_values.dtype != torch.float32 or tuple(path_values.shape) != (int(num_paths), 2)
+                    or not path_values.is_contiguous() or path_values.device != d):
+                raise ValueError("path_values must be a contiguous float32 [num_paths, 2] tensor on the device")
+            a.path_values = path_values.data_ptr()
         a.workspace = ws.data_ptr()
         a.workspace_bytes = ws.numel()
         s = torch.cuda.current_stream()
@@ -354,4 +384,4 @@ def time_to_ci(estimate: AsianEstimate, rel_halfwidth=1e-4, z=1.96) -> dict:
     return {"paths": n_req, "seconds": estimate.seconds * n_req / estimate.num_paths}
 
 
-__all__ = ["HestonAsianCV", "AsianEstimate", "time_to_ci", "stage_marks"]
+__all__ = ["HestonAsianCV", "AsianEstimate", "time_to_ci", "stage_marks", "control_dates"]
