@@ -393,7 +393,7 @@ TQF_API int tqf_hjm_paths(const tqf_hjm_args* args, void* stream);
  * tqf_milstein_affine: the whole loop for structured coefficients
  * a(x) = m + M x, B(x)_kj = (s0_k + s1_k x_k) C_kj (exact dB_kj/dx_i =
  * delta_ik s1_k C_kj), step table [num_steps][4] = (dt, sqrt dt, slot, 0),
- * dim <= 8. */
+ * any dim (above 8, one warp per path). */
 typedef struct tqf_milstein_affine_args {
   int32_t dtype;
   int32_t dim;
@@ -417,7 +417,10 @@ typedef struct tqf_milstein_affine_args {
 TQF_API int tqf_milstein_affine(const tqf_milstein_affine_args* args, void* stream);
 
 /* One Milstein step for coefficients the caller evaluated at t_{i+1}:
- * drift [N][d], vol [N][d][d] = B, grad [N][d(i)][d(k)][d(j)] = dB_kj/dx_i. */
+ * drift [N][d], vol [N][d][d] = B, grad [N][d(i)][d(k)][d(j)] = dB_kj/dx_i.
+ * increments_out (optional, [N][d + d*d] in the dtype) receives the step's
+ * dW and Stratonovich integrals J (row-major J_im; J_00 = dW^2/2 for d = 1),
+ * which a backward pass through the step needs. */
 typedef struct tqf_milstein_update_args {
   int32_t dtype;
   int32_t dim;
@@ -435,6 +438,7 @@ typedef struct tqf_milstein_update_args {
   void* x_next;
   tqf_draws draws;
   void* paths_out;           /* [N][num_slots][d] or NULL */
+  void* increments_out;      /* [N][d + d*d] or NULL */
 } tqf_milstein_update_args;
 
 TQF_API int tqf_milstein_update(const tqf_milstein_update_args* args, void* stream);

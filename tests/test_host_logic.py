@@ -2,6 +2,7 @@
 
 import numpy as np
 import pytest
+import torch
 
 from oracle import grids as ogrids
 
@@ -267,3 +268,30 @@ def test_heston_expected_total_variance():
                      dtype=np.float64)
     with pytest.raises(ValueError):
         pw.expected_total_variance(1.0, 1.0)
+
+
+def test_hull_white_rejects_bad_jump_batches():
+    """hull_white_test.py:388-420: a piecewise parameter's jump locations have
+    batch shape [] or [dim]; batch [1] for dim 2, or batch rank 2, raise
+    ValueError when the model is built."""
+    from tqf.math.piecewise import PiecewiseConstantFunc
+    from tqf.models.hull_white import VectorHullWhiteModel
+
+    def rate(t):
+        return 0.01 * torch.ones(tuple(t.shape) + (2,), dtype=t.dtype)
+
+    bad_size = PiecewiseConstantFunc([[0.1, 2.0]], values=[3 * [0.1]], dtype=np.float64)
+    with pytest.raises(ValueError):
+        VectorHullWhiteModel(2, bad_size, [0.01, 0.02], rate, dtype=np.float64)
+    bad_rank = PiecewiseConstantFunc([[[0.1, 2.0]]], values=[[3 * [[0.1, 0.05]]]], dtype=np.float64)
+    with pytest.raises(ValueError):
+        VectorHullWhiteModel(2, bad_rank, [0.01, 0.02], rate, dtype=np.float64)
+    # per-axis volatility evaluates per axis; the knots of all parameters are merged per axis
+    vol = PiecewiseConstantFunc([[0.1, 2.0], [0.5, 1.0]], [[0.01, 0.02, 0.01], [0.01, 0.015, 0.03]],
+                                dtype=np.float64)
+    m = VectorHullWhiteModel(2, [0.03, 0.02], vol, rate, dtype=np.float64)
+    np.testing.assert_array_equal(m._jumps(), [[0.1, 2.0], [0.5, 1.0]])
+    np.testing.assert_array_equal(m._vol(np.array([0.1, 0.7, 3.0])), [[0.01, 0.01], [0.02, 0.015], [0.01, 0.03]])
+    # a constant curve given as a list answers the same at every time
+    c = VectorHullWhiteModel(2, [0.03, 0.02], vol, lambda *args: [0.01, 0.015], dtype=np.float64)
+    np.testing.assert_allclose(c._forward(np.array([0.0, 0.5, 1.0])), [[0.01, 0.015]] * 3, rtol=1e-15)

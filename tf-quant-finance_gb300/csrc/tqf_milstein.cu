@@ -218,11 +218,26 @@ __global__ void __launch_bounds__(kBlock) milstein_update_kernel(tqf_milstein_up
   T dw[DM], xn[DM];
 #pragma unroll(DM <= 4 ? DM : 1)
   for (int c = 0; c < DM; ++c) dw[c] = c < d ? src.get(a.step, c) * sdt : T(0);
+  T* io = a.increments_out ? static_cast<T*>(a.increments_out) + path * (int64_t)(d + d * d) : nullptr;
   if (DM == 1) {
     xn[0] = x[0] + dt * A[0] + B[0] * dw[0] + (B[0] * G[0]) * (dw[0] * dw[0] - dt) / T(2);
+    if (io) {
+      io[0] = dw[0];
+      io[1] = dw[0] * dw[0] / T(2);
+    }
   } else {
     T J[DM][DM];
     stratonovich_J<T, DM>(d, order, dt, sdt, sqrt((T)rho_c), dw, src, a.step, J);
+    if (io) {
+#pragma unroll(DM <= 4 ? DM : 1)
+      for (int i = 0; i < DM; ++i) {
+        if (i >= d) continue;
+        io[i] = dw[i];
+#pragma unroll(DM <= 4 ? DM : 1)
+        for (int m = 0; m < DM; ++m)
+          if (m < d) io[d + i * d + m] = J[i][m];
+      }
+    }
 #pragma unroll(DM <= 4 ? DM : 1)
     for (int k = 0; k < DM; ++k) {
       if (k >= d) {
@@ -415,6 +430,11 @@ __global__ void milstein_update_wide_kernel(tqf_milstein_update_args a, double r
       b.Rt[(size_t)i * d + j] = r;
     }
   __syncwarp();
+  if (a.increments_out) {
+    T* io = static_cast<T*>(a.increments_out) + path * ((int64_t)d + (int64_t)d * d);
+    for (int c = lane; c < d; c += 32) io[c] = b.dw[c];
+    for (int e = lane; e < d * d; e += 32) io[d + e] = b.Jt[(size_t)(e % d) * d + e / d];  // J_im, row-major
+  }
   T* xo = static_cast<T*>(a.x_next) + path * d;
   T* po = a.paths_out && a.out_slot >= 0 ? static_cast<T*>(a.paths_out) + (path * a.num_slots + a.out_slot) * d
                                           : nullptr;

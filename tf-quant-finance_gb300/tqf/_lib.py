@@ -220,6 +220,7 @@ class MilsteinUpdateArgs(ctypes.Structure):
         ("x_next", c_vp),
         ("draws", Draws),
         ("paths_out", c_vp),
+        ("increments_out", c_vp),
     ]
 
 

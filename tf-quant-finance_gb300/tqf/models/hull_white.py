@@ -14,7 +14,10 @@ Euler sampler on the model's drift and volatility, as in the reference.
 
 Parameters: scalars / [dim] arrays, or ``PiecewiseConstantFunc`` with shared
 (1-D) jump locations and values [n + 1] or [n + 1, dim] ([n + 1, dim, dim] for
-the correlation).
+the correlation), or per-axis jump locations [dim, n] with values
+[dim, n + 1] (mean reversion and volatility; vector_hull_white.py:156-198).
+A piecewise mean reversion with jumps samples with the Euler sampler, as the
+reference does (:1052-1054).
 """
 
 from __future__ import annotations
@@ -31,23 +34,47 @@ from tqf.models.generic_ito_process import GenericItoProcess
 
 
 class _Param:
-    """A parameter as per-axis piecewise-constant functions (jumps, values[:, d])."""
+    """A parameter as per-axis piecewise-constant functions.
+
+    ``jumps`` keeps the jump locations as given ([n] shared by the axes, or
+    [dim, n] per axis, vector_hull_white.py:156-198); ``axis_jumps`` [dim, n]
+    and ``axis_values`` [dim, n + 1] hold them per axis (values[i] on
+    (jumps[i-1], jumps[i]], left-continuous).  The correlation matrix takes
+    shared jumps only, as the reference documents (:176-181)."""
 
     def __init__(self, p, dim, dtype, name, matrix=False):
         self.name = name
+        self.dim = dim
         self.callable = callable(p) and not isinstance(p, PiecewiseConstantFunc)
         self.fn = p if self.callable else None
+        self.matrix = matrix
         if self.callable:
             self.jumps = np.zeros(0, dtype)
+            self.axis_jumps = np.zeros((dim, 0), dtype)
             return
         if isinstance(p, PiecewiseConstantFunc):
             self.jumps = np.asarray(p.jump_locations(), dtype)
-            if self.jumps.ndim != 1:
-                raise NotImplementedError("piecewise parameters with per-axis jump locations are not supported")
             v = np.asarray(p.values(), dtype)
+            if self.jumps.ndim > 2:
+                raise ValueError("Batch rank of `jump_locations` should be `1` for all piecewise constant arguments "
+                                 f"but {self.jumps.ndim - 1} instead")
+            if self.jumps.ndim == 2:
+                if self.jumps.shape[0] != dim:
+                    raise ValueError(f"Batch shape of `jump_locations` should be either empty or `[{dim}]` but "
+                                     f"`[{self.jumps.shape[0]}]` instead")
+                if matrix:
+                    raise ValueError(f"{name}: jump locations must be shared by the axes (shape [num_jumps])")
+                n = self.jumps.shape[1]
+                if v.shape[:2] != (dim, n + 1) or v.size != dim * (n + 1):
+                    raise ValueError(f"{name}: per-axis values must have shape [{dim}, {n + 1}], got {v.shape}")
+                self.axis_jumps = self.jumps
+                self.axis_values = v.reshape(dim, n + 1)
+                return
         else:
             self.jumps = np.zeros(0, dtype)
             v = np.asarray(p, dtype)[None]
+        n = len(self.jumps)
+        self.axis_jumps = np.broadcast_to(self.jumps, (dim, n)).astype(dtype)
         if matrix:
             self.values = np.broadcast_to(v, (v.shape[0], dim, dim)).astype(dtype)
         else:
@@ -55,12 +82,20 @@ class _Param:
                 v = v[:, None]
             if v.shape[-1] not in (1, dim):
                 raise ValueError(f"Length of {name} ({v.shape[-1]}) should be the same as `dims`({dim}).")
-            self.values = np.broadcast_to(v, (v.shape[0], dim)).astype(dtype)
+            self.axis_values = np.ascontiguousarray(np.broadcast_to(v, (v.shape[0], dim)).T).astype(dtype)
 
     def __call__(self, t):
         """Values at times t (left-continuous): [len(t), dim(, dim)]."""
-        t = np.asarray(t, self.values.dtype)
-        return self.values[np.searchsorted(self.jumps, t, side="left")]
+        t = np.asarray(t, self.axis_jumps.dtype)
+        if self.matrix:
+            return self.values[np.searchsorted(self.jumps, t, side="left")]
+        return self.at(np.broadcast_to(t.reshape(-1), (self.dim, t.size))).T
+
+    def at(self, t):
+        """Per-axis values at per-axis times t [dim, m]: [dim, m]."""
+        t = np.asarray(t, self.axis_values.dtype)
+        return np.stack([self.axis_values[d][np.searchsorted(self.axis_jumps[d], t[d], side="left")]
+                         for d in range(self.dim)]).reshape(t.shape)
 
 
 class VectorHullWhiteModel(GenericItoProcess):
@@ -95,11 +130,24 @@ class VectorHullWhiteModel(GenericItoProcess):
 
     # ---- forward curve -----------------------------------------------------------
     def _forward(self, t, derivative=False):
-        """f(0, t) = d/dt (r(t) t) (and its derivative) per axis: [len(t), dim] float64."""
-        tt = torch.as_tensor(np.asarray(t, np.float64), dtype=torch.float64).requires_grad_(True)
+        """f(0, t) = d/dt (r(t) t) (and its derivative) per axis: [len(t), dim] float64.
+
+        The rate function answers input_shape or input_shape + [dim]
+        (vector_hull_white.py:208-236).  One that answers [dim] whatever its
+        input (a constant curve) is evaluated time by time, on scalars, as the
+        reference's sampler does; so is a vector of exactly dim times, where
+        the two readings cannot be told apart."""
+        t64 = np.asarray(t, np.float64)
+        tt = torch.as_tensor(t64, dtype=torch.float64).requires_grad_(True)
         r = torch.as_tensor(self._r_fn(tt), dtype=torch.float64)
         if r.dim() == tt.dim():
             r = r[..., None]
+        if tt.dim() == 1 and (tuple(r.shape[:1]) not in ((tt.shape[0],), (1,)) or (tt.shape[0] == self._dim > 1)):
+            parts = [self._forward(v.reshape(()), derivative) for v in t64]
+            if derivative:
+                return (np.stack([p[0] for p in parts]).reshape(len(t64), self._dim),
+                        np.stack([p[1] for p in parts]).reshape(len(t64), self._dim))
+            return np.stack(parts).reshape(len(t64), self._dim)
         r = torch.broadcast_to(r, tt.shape + (self._dim,))
         f_cols, df_cols = [], []
         for d in range(self._dim):
@@ -120,8 +168,11 @@ class VectorHullWhiteModel(GenericItoProcess):
         return f
 
     def _param_at(self, p, t):
+        """A parameter at time t; a callable is called with a scalar time, as
+        the reference's drift and volatility do (vector_hull_white.py:956-978)."""
         if p.callable:
-            v = p.fn(torch.as_tensor(t))
+            tn = np.asarray(t, np.float64)
+            v = p.fn(torch.as_tensor(tn.reshape(()) if tn.size == 1 else tn))
             return np.asarray(torch.as_tensor(v).detach().cpu().numpy(), np.float64)
         return p(t)
 
@@ -148,24 +199,32 @@ class VectorHullWhiteModel(GenericItoProcess):
 
     # ---- exact transition tables (:816-955) -------------------------------------
     def _jumps(self):
-        parts = [self._vol.jumps, self._mr.jumps] + ([self._corr.jumps] if self._corr is not None else [])
-        return np.sort(np.concatenate(parts)).astype(self._np_dtype)
+        """All parameters' jump locations per axis, sorted: [dim, J] (:816-855)."""
+        parts = [self._vol.axis_jumps, self._mr.axis_jumps]
+        if self._corr is not None:
+            parts.append(np.broadcast_to(self._corr.jumps, (self._dim, len(self._corr.jumps))))
+        return np.sort(np.concatenate(parts, axis=1), axis=1).astype(self._np_dtype)
+
+    @staticmethod
+    def _search(jl, t):
+        """Per-axis searchsorted (left) of t [dim, m] in jl [dim, J]."""
+        return np.stack([np.searchsorted(jl[d], t[d], side="left") for d in range(jl.shape[0])])
 
     def _integrals(self, t):
         """(conditional mean increment, conditional variance) per interval of t: [dim, len(t)-1] each."""
         npd = self._np_dtype
         dim = self._dim
-        jl = np.broadcast_to(self._jumps(), (dim, len(self._jumps())))
+        jl = self._jumps()
         J = jl.shape[1]
         zero = np.zeros((dim, 1), npd)
-        jv_vol = self._vol(jl[0]).T.reshape(dim, J) if J else np.zeros((dim, 0), npd)
-        jv_mr = self._mr(jl[0]).T.reshape(dim, J) if J else np.zeros((dim, 0), npd)
+        jv_vol = self._vol.at(jl) if J else np.zeros((dim, 0), npd)
+        jv_mr = self._mr.at(jl) if J else np.zeros((dim, 0), npd)
         knots = np.concatenate([zero, jl[:, :-1]], 1)[:, :J]
         vn = np.concatenate([zero, jl], 1)
         t = np.broadcast_to(np.asarray(t, npd), (dim, len(t)))
-        mr_t = self._mr(t[0]).T
-        sig_t = self._vol(t[0]).T
-        ti = np.searchsorted(jl[0], t[0], side="left")[None].repeat(dim, 0) if J else np.zeros(t.shape, np.int64)
+        mr_t = self._mr.at(t)
+        sig_t = self._vol.at(t)
+        ti = self._search(jl, t) if J else np.zeros(t.shape, np.int64)
 
         def y_int(t0, t1, vol, k):
             return (vol * vol) / (2 * k) * (np.exp(2 * k * t1) - np.exp(2 * k * t0))
@@ -190,7 +249,8 @@ class VectorHullWhiteModel(GenericItoProcess):
         npd = self._np_dtype
         if times_grid is None:
             extra = [self._vol.jumps, self._mr.jumps] + ([self._corr.jumps] if self._corr is not None else [])
-            all_times = np.sort(np.concatenate([np.zeros(1, npd), times] + [np.asarray(e, npd) for e in extra]))
+            all_times = np.sort(np.concatenate([np.zeros(1, npd), times]
+                                               + [np.asarray(e, npd).reshape(-1) for e in extra]))
             idx = np.searchsorted(all_times, times, side="left")
         else:
             all_times = np.asarray(times_grid, npd)
@@ -295,17 +355,18 @@ class VectorHullWhiteModel(GenericItoProcess):
         # y(t) = exp(-2 a t) int_0^t sigma(u)^2 exp(2 a u) du
         dim = self._dim
         jl = self._jumps()
-        J = len(jl)
+        J = jl.shape[1]
         zero = np.zeros((dim, 1), npd)
-        knots = np.concatenate([zero, np.broadcast_to(jl, (dim, J))[:, :-1]], 1)[:, :J]
-        jv_vol = self._vol(jl).T.reshape(dim, J) if J else np.zeros((dim, 0), npd)
-        jv_mr = self._mr(jl).T.reshape(dim, J) if J else np.zeros((dim, 0), npd)
+        knots = np.concatenate([zero, jl[:, :-1]], 1)[:, :J]
+        jv_vol = self._vol.at(jl) if J else np.zeros((dim, 0), npd)
+        jv_mr = self._mr.at(jl) if J else np.zeros((dim, 0), npd)
         yb = jv_vol * jv_vol / (2 * jv_mr) * (np.exp(2 * jv_mr * jl) - np.exp(2 * jv_mr * knots))
         y_at = np.concatenate([zero, np.cumsum(yb, 1)], 1)
-        vn = np.concatenate([zero, np.broadcast_to(jl, (dim, J))], 1)
-        ti = np.searchsorted(jl, tf_, side="left")[None].repeat(dim, 0)
-        mr_t = self._mr(tf_).T
-        sig_t = self._vol(tf_).T
+        vn = np.concatenate([zero, jl], 1)
+        tb = np.broadcast_to(tf_, (dim, tf_.size))
+        ti = self._search(jl, tb) if J else np.zeros(tb.shape, np.int64)
+        mr_t = self._mr.at(tb)
+        sig_t = self._vol.at(tb)
         t0 = np.take_along_axis(vn, ti, 1)
         y = sig_t * sig_t / (2 * mr_t) * (np.exp(2 * mr_t * tf_) - np.exp(2 * mr_t * t0)) + np.take_along_axis(
             y_at, ti, 1)

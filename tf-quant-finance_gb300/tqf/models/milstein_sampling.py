@@ -8,7 +8,12 @@ arithmetic BM, OU, ...) run the whole loop in one kernel
 (``tqf_milstein_affine``) with the exact volatility gradient; any other
 callables are evaluated once per step by the caller's torch code (the gradient
 by forward-mode AD when ``grad_volatility_fn`` is not given, as the reference
-does) and the step runs in ``tqf_milstein_update``.
+does) and the step runs in ``tqf_milstein_update``.  With ``watch_params``
+(or an initial state that requires grad) each step is an autograd Function
+whose backward uses the step's dW and Stratonovich integrals, which the
+forward kernel writes out: gradients reach the watched parameters through the
+drift, the volatility and its gradient, as the reference's custom for_loop
+gradient does (milstein_sampling.py:212-215, 389-424).
 
 Extension: ``normal_draws`` ([num_samples, steps, dim + 3 dim order]) supplies
 the normals explicitly.
@@ -39,9 +44,6 @@ def sample(*, dim, drift_fn, volatility_fn, times, time_step=None, num_time_step
     del swap_memory, precompute_normal_draws, name
     if stratonovich_order <= 0:
         raise ValueError("`stratonovich_order` must be a positive integer.")
-    if watch_params:  # an empty list watches nothing: the paths are the same as without it
-        raise NotImplementedError("watch_params (the custom for_loop gradient) is provided by "
-                                  "euler_sampling.sample; the Milstein sampler is forward-only here")
     np_dt = utils.np_dtype(dtype) if dtype is not None else utils.infer_dtype(times)
     td = utils.torch_dtype(np_dt)
     times_np = utils.to_numpy(times, np_dt).reshape(-1)
@@ -57,7 +59,11 @@ def sample(*, dim, drift_fn, volatility_fn, times, time_step=None, num_time_step
     device = _lib.require_cuda()
     if initial_state is None:
         initial_state = np.zeros(dim, np_dt)
-    x0 = torch.as_tensor(utils.to_numpy(initial_state, np_dt)).to(device)
+    if isinstance(initial_state, torch.Tensor) and initial_state.requires_grad:
+        x0 = initial_state.to(device=device, dtype=td)
+    else:
+        x0 = torch.as_tensor(utils.to_numpy(initial_state, np_dt)).to(device)
+    differentiable = watch_params is not None or x0.requires_grad
     K = num_normal_draws(dim, stratonovich_order)
     steps_total = len(all_times) - 1
     step_slot, init_slot, steps_exec, unwritten = utils.plan_output_slots(keep, num_requested, int(keep[0]))
@@ -84,6 +90,10 @@ def sample(*, dim, drift_fn, volatility_fn, times, time_step=None, num_time_step
         else:
             draws = mvn.philox_draws(rt, seed, int(num_samples))
     N = int(num_samples)
+    if differentiable:
+        return _differentiable(dim, drift_fn, volatility_fn, grad_volatility_fn, all_times, dt, sqrt_dt, step_slot,
+                               init_slot, steps_exec, x0, N, draws, num_requested, int(stratonovich_order), td,
+                               device)
     alloc = torch.zeros if unwritten else torch.empty
     paths = alloc((N, num_requested, dim), dtype=td, device=device)
     if isinstance(drift_fn, coef.AffineDrift) and isinstance(volatility_fn, coef.ScaledVolatility) \
@@ -145,6 +155,38 @@ def _vol_gradient(volatility_fn, grad_volatility_fn, t, x, dim):
     return torch.stack(cols, 1)
 
 
+def _run_update(x, a_, B, G, step, dt, sqrt_dt, draws, order, device, paths=None, slot=-1, num_slots=0,
+                need_increments=False):
+    """One tqf_milstein_update call: (x_next, [N, d + d*d] dW and J or None)."""
+    N, dim = x.shape
+    x_next = torch.empty_like(x)
+    inc = torch.empty((N, dim + dim * dim), dtype=x.dtype, device=x.device) if need_increments else None
+    u = _lib.MilsteinUpdateArgs()
+    u.dtype = _lib.dtype_code(x.dtype)
+    u.dim = dim
+    u.num_paths = N
+    u.step = step
+    u.out_slot = int(slot)
+    u.order = order
+    u.num_slots = num_slots
+    u.dt = float(dt)
+    u.sqrt_dt = float(sqrt_dt)
+    u.x, u.drift, u.vol, u.grad, u.x_next = x.data_ptr(), a_.data_ptr(), B.data_ptr(), G.data_ptr(), \
+        x_next.data_ptr()
+    u.draws = draws
+    u.paths_out = paths.data_ptr() if paths is not None else None
+    u.increments_out = inc.data_ptr() if inc is not None else None
+    _lib.call("tqf_milstein_update", u, _lib.stream_ptr(device))
+    return x_next, inc
+
+
+def _coefficients(drift_fn, volatility_fn, grad_volatility_fn, t, x, N, dim, td):
+    a_ = torch.broadcast_to(drift_fn(t, x), (N, dim)).to(td).contiguous()
+    B = torch.broadcast_to(volatility_fn(t, x), (N, dim, dim)).to(td).contiguous()
+    G = _vol_gradient(volatility_fn, grad_volatility_fn, t, x, dim).to(td).contiguous()
+    return a_, B, G
+
+
 def _generic(dim, drift_fn, volatility_fn, grad_volatility_fn, all_times, dt, sqrt_dt, step_slot, init_slot,
              steps_exec, x0, N, draws, paths, num_requested, order, td, device):
     """Per-step loop for arbitrary callables (milstein_sampling.py:356-424, 596-671)."""
@@ -153,27 +195,63 @@ def _generic(dim, drift_fn, volatility_fn, grad_volatility_fn, all_times, dt, sq
         paths[:, init_slot] = x
     for i in range(steps_exec):
         t = torch.as_tensor(all_times[i + 1], dtype=td, device=device)
-        a_ = torch.broadcast_to(drift_fn(t, x), (N, dim)).to(td).contiguous()
-        B = torch.broadcast_to(volatility_fn(t, x), (N, dim, dim)).to(td).contiguous()
-        G = _vol_gradient(volatility_fn, grad_volatility_fn, t, x, dim).to(td).contiguous()
-        x_next = torch.empty_like(x)
-        u = _lib.MilsteinUpdateArgs()
-        u.dtype = _lib.dtype_code(td)
-        u.dim = dim
-        u.num_paths = N
-        u.step = i
-        u.out_slot = int(step_slot[i])
-        u.order = order
-        u.num_slots = num_requested
-        u.dt = float(dt[i])
-        u.sqrt_dt = float(sqrt_dt[i])
-        u.x, u.drift, u.vol, u.grad, u.x_next = x.data_ptr(), a_.data_ptr(), B.data_ptr(), G.data_ptr(), \
-            x_next.data_ptr()
-        u.draws = draws
-        u.paths_out = paths.data_ptr()
-        _lib.call("tqf_milstein_update", u, _lib.stream_ptr(device))
-        x = x_next
+        a_, B, G = _coefficients(drift_fn, volatility_fn, grad_volatility_fn, t, x, N, dim, td)
+        x, _ = _run_update(x, a_, B, G, i, dt[i], sqrt_dt[i], draws, order, device, paths, int(step_slot[i]),
+                           num_requested)
     return paths
+
+
+class _MilsteinStep(torch.autograd.Function):
+    """One Milstein step, forward in tqf_milstein_update, backward by the chain
+    rule through the kernel's update (u, h and J as in the kernel):
+      d = 1: x' = x + dt a + b dW + b b' q,  q = (dW^2 - dt) / 2;
+      d > 1: x'_k = x_k + dt (a_k - u_k) + sum_j B_kj dW_j + h_k,
+             u_k = sum_ij G_ikj B_ij,  h_k = sum_im (sum_j G_ikj B_jm) J_im,
+    with G_ikj = dB_kj/dx_i and the step's dW, J saved from the forward call."""
+
+    @staticmethod
+    def forward(ctx, x, a_, B, G, args_tuple):
+        step, dt, sqrt_dt, draws, order, device = args_tuple
+        x_next, inc = _run_update(x, a_, B, G, step, dt, sqrt_dt, draws, order, device, need_increments=True)
+        ctx.save_for_backward(B, G, inc)
+        ctx.dt = float(dt)
+        return x_next
+
+    @staticmethod
+    def backward(ctx, g):
+        B, G, inc = ctx.saved_tensors
+        d = g.shape[-1]
+        dt = ctx.dt
+        dw = inc[:, :d]
+        if d == 1:
+            q = (dw * dw - dt) / 2
+            gB = (g * (dw + G.reshape(-1, 1) * q)).reshape(-1, 1, 1)
+            gG = (g * B.reshape(-1, 1) * q).reshape(-1, 1, 1, 1)
+        else:
+            J = inc[:, d:].reshape(-1, d, d)
+            gB = (torch.einsum("nk,nj->nkj", g, dw) - dt * torch.einsum("nk,nikj->nij", g, G)
+                  + torch.einsum("nk,nikj,nim->njm", g, G, J))
+            R = torch.einsum("nim,njm->nij", J, B) - dt * B  # dx'_k / dG_ikj = g_k R_ij
+            gG = torch.einsum("nk,nij->nikj", g, R)
+        return g, g * dt, gB, gG, None
+
+
+def _differentiable(dim, drift_fn, volatility_fn, grad_volatility_fn, all_times, dt, sqrt_dt, step_slot, init_slot,
+                    steps_exec, x0, N, draws, num_requested, order, td, device):
+    """Per-step loop with the states in the autograd graph (the role of the
+    reference's custom for_loop with watch_params)."""
+    x = torch.broadcast_to(x0, (N, dim)).to(td).contiguous()
+    recorded = [None] * num_requested
+    if init_slot >= 0:
+        recorded[init_slot] = x
+    for i in range(steps_exec):
+        t = torch.as_tensor(all_times[i + 1], dtype=td, device=device)
+        a_, B, G = _coefficients(drift_fn, volatility_fn, grad_volatility_fn, t, x, N, dim, td)
+        x = _MilsteinStep.apply(x.contiguous(), a_, B, G, (i, dt[i], sqrt_dt[i], draws, order, device))
+        if step_slot[i] >= 0:
+            recorded[int(step_slot[i])] = x
+    zero = torch.zeros((N, dim), dtype=td, device=device)
+    return torch.stack([r if r is not None else zero for r in recorded], dim=1)
 
 
 __all__ = ["sample", "num_normal_draws"]
