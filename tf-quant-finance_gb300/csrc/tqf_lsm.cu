@@ -19,6 +19,13 @@
 //                      X'X in FP64 (serial for <= 16 basis functions, parallel
 //                      round-robin rotations above), pinv with tf.linalg.pinv's
 //                      cutoff, beta.
+//   lsm_loop_kernel    the structured single-payoff case (d <= 2, <= 5 basis
+//                      functions) in one cooperative launch: every date's
+//                      masked Gram matrix (which does not depend on the
+//                      coefficients) and its pseudo-inverse first, in
+//                      parallel; then per date one pass (exercise update +
+//                      the G sums of X'y), a fixed-order reduction and
+//                      beta = P X'y, between bounded grid barriers.
 // tqf_lsm_price runs the whole backward loop for the structured basis and
 // payoff without returning to the caller.
 #include <math.h>
@@ -134,7 +141,7 @@ __host__ inline int lsm_gather_grid(const tqf_lsm_args& a) {
 }
 
 struct WsLayout {
-  size_t partials, sums, beta, means, mean_partials, eig_v, xt, sync, total;
+  size_t partials, sums, beta, means, mean_partials, eig_v, xt, sync, gram, pinv, total;
 };
 
 // Grid of the one-launch date loop (0 when the call does not qualify).
@@ -167,6 +174,12 @@ __host__ inline WsLayout lsm_layout(const tqf_lsm_args& a) {
   if (a.degree >= 0) off += up((size_t)a.paths_batch * E * a.num_paths * a.dim * es);
   w.sync = off;
   off += 256;
+  // one-launch loop: per-CTA Gram partials of every date, then each date's
+  // pseudo-inverse (FP64 [G][G])
+  w.gram = off;
+  if (gl >= 1) off += up((size_t)E * gl * (size_t)(G * (G + 1) / 2) * 8);
+  w.pinv = off;
+  if (gl >= 1) off += up((size_t)E * G * G * 8);
   w.total = off;
   return w;
 }
@@ -897,8 +910,6 @@ __device__ bool loop_barrier(LoopSync* sy, unsigned gen, int32_t* status) {
   return ok_s != 0;
 }
 
-__device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
-
 // The rotation (c, s) of the pair (x, xp) of the current round, from the
 // lanes holding A_pp, A_qq and A_pq (Golub & Van Loan, sym.schur2); identity
 // when x has no partner.  Kept out of line: the solver runs in one warp once
@@ -926,29 +937,32 @@ __device__ __noinline__ float2 jacobi_rot_f32(float af, int x, int xp) {
   return make_float2(c, sn);
 }
 
-// Pseudo-inverse solve of a G x G system (G <= 5) by one warp.  FP64 is a
-// narrow pipe on this GPU (a warp-wide FP64 instruction occupies it for ~64
-// cycles, measured, whatever the active lanes), so the eigenvectors come
-// from cyclic Jacobi in FP32 and only a fixed, short FP64 stage follows:
+// The pseudo-inverse of one date's masked Gram matrix A (G x G, G <= 5;
+// packed upper triangle in `gram`, FP64, shared memory) as an explicit FP64
+// matrix P = V_K B_KK^-1 V_K^T, formed by one warp.  FP64 is a narrow pipe on
+// this GPU (a warp-wide FP64 instruction occupies it for ~64 cycles,
+// measured, whatever the active lanes), so the eigenvectors come from cyclic
+// Jacobi in FP32 and only a short FP64 stage follows:
 //   1. lane i*G + j holds A_ij (and V_ij); A scaled by a power of two to
-//      O(1), warm-started by V^T A V from the previous date's V; FP32 Jacobi
-//      sweeps (round-robin pairing over G rounded up to even, partner of x in
-//      round r = 2r - x mod (Pe - 1), the last index with r; the rotation of
-//      Golub & Van Loan's sym.schur2) until the off-diagonal is below 1e-12
-//      of the total or stops shrinking; skipped on a warm start whose
-//      Gershgorin discs keep every direction far above the cutoff;
-//   2. FP64: B = V^T A V and u = V^T X'y with the FP32 V (any invertible V
-//      gives A^-1 = V B^-1 V^T exactly, and B is diagonal to ~1e-7, so its
-//      diagonal holds the eigenvalues to FP64 accuracy);
+//      O(1); FP32 Jacobi sweeps from the identity (round-robin pairing over G
+//      rounded up to even, partner of x in round r = 2r - x mod (Pe - 1), the
+//      last index with r; the rotation of Golub & Van Loan's sym.schur2)
+//      until the off-diagonal is below 1e-12 of the total or stops shrinking;
+//   2. FP64: B = V^T A V with the FP32 V (any invertible V gives
+//      A^-1 = V B^-1 V^T exactly, and B is diagonal to ~1e-7, so its diagonal
+//      holds the eigenvalues to FP64 accuracy);
 //   3. tf.linalg.pinv's cutoff (rcond x max |B_kk|) drops directions; the
-//      kept block B_KK x = u_K is solved by Gaussian elimination in FP64 (one
-//      row per lane, pivots on the diagonal; reciprocals from the FP32
-//      reciprocal refined by two Newton steps), beta = V x.
-// sums: packed upper triangle then X'y (FP64, shared); Vs (shared) keeps V
-// for the next date; Ws, Bs: shared scratch [G*G + G].
+//      kept block B_KK X = I_K is solved by Gaussian elimination in FP64 (one
+//      row per lane, pivots on the diagonal, reciprocals from the FP32
+//      reciprocal refined by two Newton steps; back substitution one column
+//      per lane), and P = V X V^T.
+// The Gram matrices do not depend on the regression coefficients, so the
+// one-launch loop forms every date's P before its date loop, dates spread
+// over CTAs; a date's coefficients are then P X'y.  Vs: [G G] FP32, Ws:
+// [2 G G] and Bs: [G G + G] FP64 shared scratch.
 template <int G>
-__device__ __noinline__ void warp_pinv_solve(const double* sums, double rcond, bool warm, float* Vs, float* Fs,
-                                             double* Ws, double* Bs, double* beta_out) {
+__device__ __noinline__ void warp_pinv_matrix(const double* gram, double rcond, float* Vs, double* Ws, double* Bs,
+                                              double* P_out) {
   const int lane = threadIdx.x & 31;
   const bool in = lane < G * G;
   const int i = in ? lane / G : 0, j = in ? lane % G : 0;
@@ -956,32 +970,15 @@ __device__ __noinline__ void warp_pinv_solve(const double* sums, double rcond, b
     const int p = r < c ? r : c, q = r < c ? c : r;
     return p * G - p * (p - 1) / 2 + (q - p);
   };
-  const double a = in ? sums[packed(i, j)] : 0.0;
+  const double a = in ? gram[packed(i, j)] : 0.0;
   // 1. FP32 Jacobi on A scaled by 2^-e (e from the largest diagonal entry)
   float af = (float)a;
   float dm = in && i == j ? fabsf(af) : 0.f;
   for (int o = 16; o > 0; o >>= 1) dm = fmaxf(dm, __shfl_xor_sync(0xffffffffu, dm, o));
   int e2 = 0;
   frexpf(dm > 0.f ? dm : 1.f, &e2);
-  const float scf = ldexpf(1.f, -e2);
-  af *= scf;
-  float vf = in ? (warm ? Vs[lane] : (i == j ? 1.f : 0.f)) : 0.f;
-  if (warm) {
-    if (in) Fs[lane] = af;
-    __syncwarp();
-    float x = 0.f;
-    if (in)
-      for (int k = 0; k < G; ++k) {
-        float t = 0.f;
-        for (int l = 0; l < G; ++l) t = fmaf(Fs[k * G + l], Vs[l * G + j], t);
-        x = fmaf(Vs[k * G + i], t, x);
-      }
-    __syncwarp();
-    if (in) Fs[lane] = x;
-    __syncwarp();
-    af = in ? 0.5f * (x + Fs[j * G + i]) : 0.f;
-    __syncwarp();
-  }
+  af *= ldexpf(1.f, -e2);
+  float vf = in && i == j ? 1.f : 0.f;
   constexpr int Pe = G + (G & 1);
   auto partner = [](int x, int r) {
     constexpr int m = Pe - 1;
@@ -991,34 +988,9 @@ __device__ __noinline__ void warp_pinv_solve(const double* sums, double rcond, b
     else p = ((2 * r - x) % m + m) % m;
     return p < G ? p : -1;
   };
-  // With the previous date's V, V^T A V is usually close to diagonal.  When
-  // Gershgorin's bound puts every eigenvalue far above the cutoff (64 x
-  // rcond x the largest diagonal entry, plus 1e-5 of it for the FP32
-  // rounding of V^T A V), no direction is dropped and the FP64 stage below
-  // solves with that V exactly (any invertible V), so the sweeps are skipped.
-  bool sweep_needed = !warm;
-  if (warm) {
-    if (in) Fs[lane] = af;
-    __syncwarp();
-    float lo = 3.0e38f, hi = 0.f;
-    if (lane < G) {
-      float rad = 0.f;
-      for (int c = 0; c < G; ++c)
-        if (c != lane) rad += fabsf(Fs[lane * G + c]);
-      const float dg = Fs[lane * G + lane];
-      lo = dg - rad;
-      hi = fabsf(dg);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-      hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-    }
-    sweep_needed = !(lo > (64.f * (float)rcond + 1e-5f) * hi);
-    __syncwarp();
-  }
   float prev = 0.f;
 #pragma unroll 1
-  for (int sweep = 0; sweep < 30 && G > 1 && sweep_needed; ++sweep) {
+  for (int sweep = 0; sweep < 30 && G > 1; ++sweep) {
     float off = in && i != j ? af * af : 0.f, tot = in ? af * af : 0.f;
     for (int o = 16; o > 0; o >>= 1) {
       off += __shfl_xor_sync(0xffffffffu, off, o);
@@ -1050,15 +1022,13 @@ __device__ __noinline__ void warp_pinv_solve(const double* sums, double rcond, b
       vf = in ? vn : 0.f;
     }
   }
-  // 2. FP64: B = V^T A V (W = A V first) and u = V^T X'y, same instruction
-  //    stream for all lanes (per-lane operand pointers)
-  double* As = Ws + G * G;  // [G*G] A, then [G] u
+  // 2. FP64: B = V^T A V (W = A V first)
+  double* As = Ws + G * G;
   if (in) {
     Vs[lane] = vf;
     As[lane] = a;
   }
   __syncwarp();
-  const double* rhs = sums + G * (G + 1) / 2;
   {
     double w = 0.0;
     if (in)
@@ -1066,59 +1036,69 @@ __device__ __noinline__ void warp_pinv_solve(const double* sums, double rcond, b
     __syncwarp();
     if (in) Ws[lane] = w;
     __syncwarp();
-  }
-  const bool ul = lane >= G * G && lane < G * G + G;  // lanes computing u
-  {
-    double bsum = 0.0;
-    if (in || ul) {
-      const int col = in ? i : lane - G * G;
-      for (int k = 0; k < G; ++k)
-        bsum = fma((double)Vs[k * G + col], in ? Ws[k * G + j] : rhs[k], bsum);
-    }
-    if (in) Bs[lane] = bsum;
-    if (ul) Bs[lane] = bsum;  // u at Bs[G*G + k]
+    double b = 0.0;
+    if (in)
+      for (int k = 0; k < G; ++k) b = fma((double)Vs[k * G + i], Ws[k * G + j], b);
+    if (in) Bs[lane] = b;
     __syncwarp();
   }
-  // 3. cutoff on the diagonal, kept block by elimination (row i in lane i)
+  // 3. cutoff on the diagonal; B_KK X = I_K by elimination, row i in lane i
   double lmax = 0.0;
   for (int k = 0; k < G; ++k) lmax = fmax(lmax, fabs(Bs[k * G + k]));
   const double cutoff = rcond * lmax;
   auto kept = [&](int k) { const double l = Bs[k * G + k]; return fabs(l) > cutoff && l != 0.0; };
-  double row[G + 1];
+  double row[2 * G];
   const int ri = lane < G ? lane : 0;
   const bool kr = kept(ri);
 #pragma unroll
-  for (int c = 0; c < G; ++c) row[c] = kr && kept(c) ? Bs[ri * G + c] : (c == ri ? 1.0 : 0.0);
-  row[G] = kr ? Bs[G * G + ri] : 0.0;
+  for (int c = 0; c < G; ++c) {
+    row[c] = kr && kept(c) ? Bs[ri * G + c] : (c == ri ? 1.0 : 0.0);
+    row[G + c] = kr && c == ri ? 1.0 : 0.0;
+  }
+  __syncwarp();
   double rcp[G];
 #pragma unroll
   for (int p = 0; p < G; ++p) {
-    const double d = __shfl_sync(0xffffffffu, row[p], p);
-    double r0 = (double)__frcp_rn((float)d);
-    r0 = r0 * fma(-d, r0, 2.0);
-    r0 = r0 * fma(-d, r0, 2.0);
+    const double dd = __shfl_sync(0xffffffffu, row[p], p);
+    double r0 = (double)__frcp_rn((float)dd);
+    r0 = r0 * fma(-dd, r0, 2.0);
+    r0 = r0 * fma(-dd, r0, 2.0);
     rcp[p] = r0;
     const double f = row[p] * r0;
 #pragma unroll
-    for (int c = p + 1; c <= G; ++c) {
+    for (int c = p + 1; c < 2 * G; ++c) {
       const double pc = __shfl_sync(0xffffffffu, row[c], p);
       if (lane > p) row[c] = fma(-f, pc, row[c]);
     }
   }
-  // back substitution: x_i = (rhs_i - sum_{c > i} U_ic x_c) / U_ii
+  // U | Y rows to shared memory; lane m solves column m of X
+  if (lane < G)
+#pragma unroll
+    for (int c = 0; c < 2 * G; ++c) Ws[lane * 2 * G + c] = row[c];
+  __syncwarp();
   double x[G];
+  const int m = lane < G ? lane : 0;
 #pragma unroll
   for (int p = G - 1; p >= 0; --p) {
-    double t = __shfl_sync(0xffffffffu, row[G], p);
+    double t = Ws[p * 2 * G + G + m];
 #pragma unroll
-    for (int c = p + 1; c < G; ++c) t = fma(-__shfl_sync(0xffffffffu, row[c], p), x[c], t);
+    for (int c = p + 1; c < G; ++c) t = fma(-Ws[p * 2 * G + c], x[c], t);
     x[p] = t * rcp[p];
   }
-  if (lane < G) {
-    double bt = 0.0;
+  __syncwarp();
+  if (lane < G)
 #pragma unroll
-    for (int k = 0; k < G; ++k) bt = fma((double)Vs[lane * G + k], x[k], bt);
-    __stcg(beta_out + lane, bt);
+    for (int p = 0; p < G; ++p) Bs[p * G + m] = x[p];  // X[p][m]
+  __syncwarp();
+  // 4. P = V X V^T, lane (j, k) = (i, j)
+  if (in) {
+    double pv = 0.0;
+    for (int r = 0; r < G; ++r) {
+      double w = 0.0;
+      for (int c = 0; c < G; ++c) w = fma(Bs[r * G + c], (double)Vs[j * G + c], w);
+      pv = fma((double)Vs[i * G + r], w, pv);
+    }
+    __stcg(P_out + lane, pv);
   }
   __syncwarp();
 }
@@ -1133,13 +1113,17 @@ __host__ __device__ inline size_t lsm_loop_smem(int K) {
   return (size_t)K * kLoopThreads * (2 + DM) * sizeof(T);
 }
 
+// Two CTAs per SM (three, with 85 registers, measured 1.44 against 1.29 ms
+// per call for 2^20 float paths x 50 dates: more CTAs at every barrier and
+// more partial rows per reduction).
 template <typename T, int DM, int GN>
 __global__ void __launch_bounds__(kLoopThreads, 2)
     lsm_loop_kernel(tqf_lsm_args a, const T* __restrict__ xt, typename Acc<T>::S* __restrict__ partials,
-                    double* __restrict__ beta, const double* __restrict__ means, LoopSync* sy, int K) {
+                    double* __restrict__ beta, const double* __restrict__ means, LoopSync* sy, int K,
+                    double* __restrict__ gram, double* __restrict__ pinv) {
   using A = Acc<T>;
   using S = typename A::S;
-  constexpr int EN = GN * (GN + 1) / 2 + GN;
+  constexpr int EA = GN * (GN + 1) / 2;  // Gram entries (packed upper triangle)
   constexpr int C = kLoopThreads;
   constexpr int KB = 8;  // paths per batch of loads
   extern __shared__ __align__(16) unsigned char dsm[];
@@ -1148,9 +1132,9 @@ __global__ void __launch_bounds__(kLoopThreads, 2)
   T* xs_ = vs_ + (size_t)K * C;        // [K][DM][C] states at the last accumulated date
   __shared__ T beta_s[GN];
   __shared__ T mu_s[2][kMaxDimLsm];
-  __shared__ S red[C / 32][EN];
+  __shared__ S red[C / 32][EA];
   __shared__ double sums_s[kLoopMaxEn];
-  __shared__ float Vs[kLoopMaxG * kLoopMaxG], Fs[kLoopMaxG * kLoopMaxG];
+  __shared__ float Vs[kLoopMaxG * kLoopMaxG];
   __shared__ double Ws[2 * kLoopMaxG * kLoopMaxG], Bs[kLoopMaxG * kLoopMaxG + kLoopMaxG];
   __shared__ S rsum[16][16];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1190,15 +1174,128 @@ __global__ void __launch_bounds__(kLoopThreads, 2)
     }
   };
   (void)deg;
+  // Block reduction of per-thread accumulators (the register mode of
+  // lsm_pass_kernel) into this CTA's row of `dst` ([rows][width], 8-byte S).
+  auto block_store = [&](const S* accv, const T* partv, int width, double* dst) {
+    for (int q = 0; q < width; ++q) {
+      T t = (T)A::value(A::add(accv[q], partv[q]));
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      if (lane == 0) red[warp][q] = A::add(A::zero(), t);
+    }
+    __syncthreads();
+    for (int q = tid; q < width; q += C) {
+      S t = A::zero();
+      for (int w = 0; w < C / 32; ++w) t = A::sum(t, red[w][q]);
+      __stcg(dst + (size_t)blockIdx.x * width + q, *reinterpret_cast<double*>(&t));
+    }
+    __syncthreads();
+  };
+  // Fixed-order reduction of rows [gridDim.x][width] of `src` into sums_s:
+  // thread (r, e), r < 16, sums rows r, r + 16, ... of entry e (eight loads
+  // in flight), then the 16 groups in order.
+  auto grid_reduce = [&](const double* src, int width) {
+    const int e = tid & 15, r = tid >> 4;
+    S t = A::zero();
+    if (e < width) {
+      const int rows = (int)gridDim.x;
+      for (int row0 = r; row0 < rows; row0 += 128) {
+        double raw[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int row = row0 + 16 * q;
+          raw[q] = row < rows ? __ldcg(src + (size_t)row * width + e) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (row0 + 16 * q < rows) t = A::sum(t, *reinterpret_cast<const S*>(&raw[q]));
+      }
+    }
+    rsum[r][e] = t;
+    __syncthreads();
+    if (tid < width) {
+      S u = A::zero();
+      for (int q = 0; q < 16; ++q) u = A::sum(u, rsum[q][tid]);
+      sums_s[tid] = A::value(u);
+    }
+    __syncthreads();
+  };
   unsigned gen = 0;
+  // Phase 1: the masked Gram matrix of every regression date (lsm.py:355-372)
+  // depends only on that date's states, not on the coefficients of later
+  // dates, so all of them are summed here, before the date loop, and each
+  // date's pseudo-inverse is formed once (dates spread over CTAs).
+  for (int acc = 1; acc <= E - 1; ++acc) {
+    __syncthreads();
+    for (int c = tid; c < DM; c += C) mu_s[1][c] = (T)means[(size_t)(acc - 1) * kMaxDimLsm + c];
+    __syncthreads();
+    T part[EA];
+    S acc2[EA];
+    int cnt = 0;
+#pragma unroll
+    for (int e = 0; e < EA; ++e) {
+      part[e] = T(0);
+      acc2[e] = A::zero();
+    }
+    for (int kb = 0; kb < K; kb += KB) {
+      T xa[KB][DM];
+#pragma unroll
+      for (int q = 0; q < KB; ++q) {
+        const int64_t n = ((int64_t)blockIdx.x + (int64_t)(kb + q) * gridDim.x) * C + tid;
+#pragma unroll
+        for (int c = 0; c < DM; ++c) xa[q][c] = T(0);
+        if (kb + q < K && n < n_cal) load_x(acc - 1, n, xa[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < KB; ++q) {
+        const int64_t n = ((int64_t)blockIdx.x + (int64_t)(kb + q) * gridDim.x) * C + tid;
+        if (kb + q >= K || n >= n_cal) continue;
+        T xc[DM], phi[GN];
+#pragma unroll
+        for (int cc = 0; cc < DM; ++cc) xc[cc] = xa[q][cc] - mu_s[1][cc];
+        basis(xc, phi);
+        const bool use = pay(xa[q]) > T(0);
+#pragma unroll
+        for (int g = 0; g < GN; ++g) phi[g] = use ? phi[g] : T(0);
+        int e = 0;
+#pragma unroll
+        for (int jj = 0; jj < GN; ++jj)
+#pragma unroll
+          for (int kk = jj; kk < GN; ++kk) part[e++] += phi[jj] * phi[kk];
+        if (++cnt == kSubSum) {
+#pragma unroll
+          for (int qq = 0; qq < EA; ++qq) {
+            acc2[qq] = A::add(acc2[qq], part[qq]);
+            part[qq] = T(0);
+          }
+          cnt = 0;
+        }
+      }
+    }
+    block_store(acc2, part, EA, gram + (size_t)acc * gridDim.x * EA);
+  }
+  if (!loop_barrier(sy, ++gen, a.dev_status)) return;
+  for (int acc = 1 + (int)blockIdx.x; acc <= E - 1; acc += (int)gridDim.x) {
+    grid_reduce(gram + (size_t)acc * gridDim.x * EA, EA);
+    if (warp == 0) warp_pinv_matrix<GN>(sums_s, rcond, Vs, Ws, Bs, pinv + (size_t)acc * GN * GN);
+    __syncthreads();
+  }
+  if (!loop_barrier(sy, ++gen, a.dev_status)) return;
+  // Phase 2: the backward date loop.  Per date one pass (the exercise update
+  // of the previous date with its coefficients, fused with this date's
+  // masked right-hand side X'y), one grid barrier, then every CTA reduces the
+  // GN sums in the same fixed order and forms beta = P X'y in FP64 itself
+  // (identical in every CTA), so no second barrier broadcasts it.  The
+  // partial rows alternate between two buffers by date: a CTA can run at
+  // most one date ahead of the slowest reader (it cannot pass the next
+  // barrier before every CTA has reduced), so it never overwrites rows that
+  // are still being read.
   for (int step = 0;; ++step) {
+    double* pout = reinterpret_cast<double*>(partials) + (size_t)(step & 1) * gridDim.x * GN;
     const int init = step == 0;
     const int upd = step == 0 ? 0 : E - step;
     const int acc = E - 1 - step;
     const int fin = acc < 1;
     __syncthreads();
-    if (upd >= 1)
-      for (int g = tid; g < GN; g += C) beta_s[g] = (T)__ldcg(beta + g);
     for (int i = tid; i < 2 * kMaxDimLsm; i += C) {
       const int which = i / kMaxDimLsm, c = i % kMaxDimLsm;
       const int idx = which == 0 ? upd : acc;
@@ -1208,11 +1305,11 @@ __global__ void __launch_bounds__(kLoopThreads, 2)
     const T r_upd = upd >= 1 && a.disc_stride_n == 0 ? ctx.ratio(upd, 0) : T(0);
     const T r_acc = acc >= 1 && a.disc_stride_n == 0 ? ctx.ratio(acc, 0) : T(0);
     const T r_fin = fin && a.disc_stride_n == 0 ? ctx.ratio(0, 0) : T(0);
-    T part[EN];
-    S acc2[EN];
+    T part[GN];
+    S acc2[GN];
     int cnt = 0;
 #pragma unroll
-    for (int e = 0; e < EN; ++e) {
+    for (int e = 0; e < GN; ++e) {
       part[e] = T(0);
       acc2[e] = A::zero();
     }
@@ -1272,26 +1369,20 @@ __global__ void __launch_bounds__(kLoopThreads, 2)
 #pragma unroll
         for (int cc = 0; cc < DM; ++cc) xs_[((size_t)k * DM + cc) * C + tid] = xa[q][cc];
         if (n < n_cal) {
-          // masked normal equations of exercise index acc (lsm.py:355-379)
-          const T cv = ctx.ratio_at(acc, n, r_acc) * (v + c);
+          // masked right-hand side of exercise index acc (lsm.py:373-379)
           const T eva = pay(xa[q]);
-          T xc[DM], phi[GN];
+          if (eva > T(0)) {
+            const T cv = ctx.ratio_at(acc, n, r_acc) * (v + c);
+            T xc[DM], phi[GN];
 #pragma unroll
-          for (int cc = 0; cc < DM; ++cc) xc[cc] = xa[q][cc] - mu_s[1][cc];
-          basis(xc, phi);
-          const bool use = eva > T(0);
+            for (int cc = 0; cc < DM; ++cc) xc[cc] = xa[q][cc] - mu_s[1][cc];
+            basis(xc, phi);
 #pragma unroll
-          for (int g = 0; g < GN; ++g) phi[g] = use ? phi[g] : T(0);
-          int e = 0;
-#pragma unroll
-          for (int jj = 0; jj < GN; ++jj)
-#pragma unroll
-            for (int kk = jj; kk < GN; ++kk) part[e++] += phi[jj] * phi[kk];
-#pragma unroll
-          for (int jj = 0; jj < GN; ++jj) part[e++] += phi[jj] * cv;
+            for (int jj = 0; jj < GN; ++jj) part[jj] += phi[jj] * cv;
+          }
           if (++cnt == kSubSum) {
 #pragma unroll
-            for (int qq = 0; qq < EN; ++qq) {
+            for (int qq = 0; qq < GN; ++qq) {
               acc2[qq] = A::add(acc2[qq], part[qq]);
               part[qq] = T(0);
             }
@@ -1300,22 +1391,9 @@ __global__ void __launch_bounds__(kLoopThreads, 2)
         }
       }
     }
-    const int width = fin ? 1 : EN;
-    double* pout = reinterpret_cast<double*>(partials);
+    const int width = fin ? 1 : GN;
     if (!fin) {
-      // the block reduction of lsm_pass_kernel's register mode
-#pragma unroll
-      for (int q = 0; q < EN; ++q) {
-        T t = (T)A::value(A::add(acc2[q], part[q]));
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-        if (lane == 0) red[warp][q] = A::add(A::zero(), t);
-      }
-      __syncthreads();
-      for (int q = tid; q < EN; q += C) {
-        S t = A::zero();
-        for (int w = 0; w < C / 32; ++w) t = A::sum(t, red[w][q]);
-        __stcg(pout + (size_t)blockIdx.x * EN + q, *reinterpret_cast<double*>(&t));
-      }
+      block_store(acc2, part, GN, pout);
     } else {
       for (int o = 16; o > 0; o >>= 1) final_acc = A::sum(final_acc, A::shfl_down(final_acc, o));
       if (lane == 0) red[warp][0] = final_acc;
@@ -1327,44 +1405,25 @@ __global__ void __launch_bounds__(kLoopThreads, 2)
       }
     }
     if (!loop_barrier(sy, ++gen, a.dev_status)) return;
-    if (blockIdx.x == 0) {
-      // fixed-order reduction: thread (r, e), r < 16, sums rows r, r + 16, ...
-      // of entry e (eight loads in flight), then the 16 groups in order
-      const int e = tid & 15, r = tid >> 4;
-      S t = A::zero();
-      if (e < width) {
-        const int rows = (int)gridDim.x;
-        for (int row0 = r; row0 < rows; row0 += 128) {
-          double raw[8];
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const int row = row0 + 16 * q;
-            raw[q] = row < rows ? __ldcg(pout + (size_t)row * width + e) : 0.0;
-          }
-#pragma unroll
-          for (int q = 0; q < 8; ++q)
-            if (row0 + 16 * q < rows) t = A::sum(t, *reinterpret_cast<const S*>(&raw[q]));
-        }
-      }
-      rsum[r][e] = t;
-      __syncthreads();
-      if (tid < width) {
-        S u = A::zero();
-        for (int q = 0; q < 16; ++q) u = A::sum(u, rsum[q][tid]);
-        sums_s[tid] = A::value(u);
-      }
-      __syncthreads();
-      if (fin) {
+    if (fin) {
+      if (blockIdx.x == 0) {
+        grid_reduce(pout, width);
         if (tid == 0) {
           const int64_t count = a.num_calibration > 0 ? N - a.num_calibration : N;
           a.out[0] = sums_s[0] * (1.0 / (double)count);
         }
-      } else if (warp == 0) {
-        warp_pinv_solve<GN>(sums_s, rcond, acc < E - 1, Vs, Fs, Ws, Bs, beta);
       }
+      return;
     }
-    if (fin) return;
-    if (!loop_barrier(sy, ++gen, a.dev_status)) return;
+    grid_reduce(pout, width);
+    if (tid < GN) {
+      // beta = P X'y (FP64), P this date's pseudo-inverse from phase 1
+      const double* P = pinv + (size_t)acc * GN * GN + (size_t)tid * GN;
+      double b = 0.0;
+#pragma unroll
+      for (int k = 0; k < GN; ++k) b = fma(__ldcg(P + k), sums_s[k], b);
+      beta_s[tid] = (T)b;
+    }
   }
 }
 
@@ -1450,7 +1509,10 @@ int launch_loop(const tqf_lsm_args& a, cudaStream_t s) {
   void* partials = ws + L.partials;
   double* beta = reinterpret_cast<double*>(ws + L.beta);
   const double* means = reinterpret_cast<const double*>(ws + L.means);
-  void* params[] = {&args, const_cast<void**>(&xt), &partials, &beta, const_cast<double**>(&means), &sy, &K};
+  double* gram = reinterpret_cast<double*>(ws + L.gram);
+  double* pinv = reinterpret_cast<double*>(ws + L.pinv);
+  void* params[] = {&args, const_cast<void**>(&xt), &partials, &beta, const_cast<double**>(&means), &sy, &K,
+                    &gram, &pinv};
   rc = check_cuda(cudaLaunchCooperativeKernel(k, dim3((unsigned)grid), dim3(kLoopThreads), params, smem, s),
                   "lsm_loop_kernel cooperative launch");
   if (rc) return rc;
