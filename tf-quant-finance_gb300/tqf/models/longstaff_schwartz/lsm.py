@@ -125,9 +125,9 @@ def least_square_mc(sample_paths, exercise_times, payoff_fn, basis_fn, discount_
         B = max(len(strikes), paths_batch)
         if len(strikes) not in (1, B) or paths_batch not in (1, B):
             raise ValueError("strikes and the batch of sample_paths must broadcast")
-        strikes_t = torch.as_tensor(np.broadcast_to(basis_strikes, (B,)).copy()).to(device)
+        strikes_t = utils.upload(np.broadcast_to(basis_strikes, (B,)), td, device)
         G = (basis_fn.degree + 1) ** dim
-        exps_t = torch.as_tensor(polynomial_exponents(basis_fn.degree, dim)).to(device)
+        exps_t = utils.upload(polynomial_exponents(basis_fn.degree, dim), torch.int32, device)
         design_batch = paths_batch
     else:
         ev0, des0 = explicit(ex[E - 1])
@@ -146,9 +146,9 @@ def least_square_mc(sample_paths, exercise_times, payoff_fn, basis_fn, discount_
     Nd, Bd = D.shape[1], D.shape[2]
     if Nd not in (1, N) or Bd not in (1, B):
         raise ValueError("discount_factors must broadcast to [num_samples, batch_size, num_exercise_times]")
-    D_t = torch.as_tensor(D).to(device)
-    ex_t = torch.as_tensor(np.asarray(ex, np.int32)).to(device)
-    state = torch.zeros((2, B, N), dtype=td, device=device)
+    D_t = utils.upload(D, td, device)
+    ex_t = utils.upload(np.asarray(ex, np.int32), torch.int32, device)
+    state = torch.empty((2, B, N), dtype=td, device=device)  # written by the first pass before any read
     out = torch.zeros(B, dtype=torch.float64, device=device)
 
     a = _lib.LsmArgs()

@@ -9,6 +9,9 @@ ceil((b - a)/d) points a + i*d and tf.linspace(a, b, n) is
 
 from __future__ import annotations
 
+import collections
+import threading
+
 import numpy as np
 import torch
 
@@ -184,9 +187,44 @@ def generate_mc_normal_draws(num_normal_draws, num_time_steps, num_sample_paths,
     return draws.reshape(shape)
 
 
+_UPLOADS: "collections.OrderedDict[tuple, torch.Tensor]" = collections.OrderedDict()
+_UPLOADS_LOCK = threading.Lock()
+_UPLOADS_MAX = 256            # arrays kept
+_UPLOADS_MAX_BYTES = 1 << 18  # largest array kept
+
+
+def upload(array, dtype: torch.dtype, device) -> torch.Tensor:
+    """Device copy of a small host array that kernels only read (step tables,
+    exercise schedules, discount tables, strikes).  Copies are kept by
+    content (device, dtype, shape, bytes; at most 256 arrays of at most
+    256 KiB, least recently used dropped), so repeated calls with the same
+    schedules upload nothing: a pageable host-to-device copy would make the
+    host wait for all earlier GPU work before it could prepare the launch.
+    Callers must not write to the returned tensor."""
+    a = np.ascontiguousarray(array)
+    dev = torch.device(device)
+    if dev.type != "cuda":
+        return torch.tensor(a, dtype=dtype)
+    if a.nbytes > _UPLOADS_MAX_BYTES:
+        return torch.tensor(a, dtype=dtype).to(dev)
+    index = dev.index if dev.index is not None else torch.cuda.current_device()
+    key = (index, str(dtype), a.dtype.str, a.shape, a.tobytes())
+    with _UPLOADS_LOCK:
+        hit = _UPLOADS.get(key)
+        if hit is not None:
+            _UPLOADS.move_to_end(key)
+            return hit
+    t = torch.tensor(a, dtype=dtype).to(dev)
+    with _UPLOADS_LOCK:
+        _UPLOADS[key] = t
+        while len(_UPLOADS) > _UPLOADS_MAX:
+            _UPLOADS.popitem(last=False)
+    return t
+
+
 def step_table(rows: np.ndarray, dtype: torch.dtype, device) -> torch.Tensor:
     """Uploads a [steps, cols] host table (16-byte aligned device copy)."""
-    return torch.as_tensor(np.ascontiguousarray(rows), dtype=dtype).to(device, non_blocking=False)
+    return upload(rows, dtype, device)
 
 
-__all__ = ["prepare_grid", "generate_mc_normal_draws", "plan_output_slots", "tf_range", "tf_linspace"]
+__all__ = ["prepare_grid", "generate_mc_normal_draws", "plan_output_slots", "tf_range", "tf_linspace", "upload"]
