@@ -92,8 +92,8 @@ typedef struct tqf_draws {
  * i records slot base + i for every step (base = 1 after an initial state at
  * slot 0, else 0) and num_slots = base + num_steps: path rows then fill front
  * to back, and the Euler (tqf_euler_affine) and GBM (tqf_mvgbm_paths) kernels
- * write rows that are a multiple of 16 bytes with bulk shared -> global
- * copies (4, 8 or 16 bytes per slot).  Such a kernel that finds the
+ * gather 32 words of 32 paths' rows per warp in shared memory and write each
+ * path's 128 bytes with one store instruction.  Such a kernel that finds the
  * declaration false writes no states and sets *dev_status to TQF_E_INVALID;
  * the other kernels ignore the field. */
 typedef struct tqf_path_output {

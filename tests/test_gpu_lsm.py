@@ -134,3 +134,33 @@ def test_lsm_american_put_bounds(cuda):
     euro = closed_form.black_scholes(1.0, 1.1, 0.06, 0.2, 1.0, is_call=False)
     assert p1[0] > euro and p1[0] > 0.1
     assert p1[0] < euro + 0.03
+
+
+@pytest.mark.parametrize("dim,degree,calib", [(1, 3, None), (1, 4, 15000), (2, 1, None), (2, 1, 12000)])
+def test_lsm_one_launch_loop_matches_oracle(cuda, dim, degree, calib):
+    """The one-launch loop (one payoff, d <= 2, <= 5 basis functions: Gram
+    pseudo-inverses of every date before the date loop, one barrier per date)
+    against the restatement in FP64 to 1e-9, with and without a calibration
+    split, and against the float32 restatement in float32 to 2.5e-4: the
+    two float32 regressions round differently (sums, the pseudo-inverse's
+    cutoff directions), which flips exercise decisions at near-ties;
+    measured up to 1.1e-4 on these cases."""
+    from tqf import _lib
+    from tqf.models import longstaff_schwartz as L
+    S = _gbm_paths(40000, 10, dim=dim, seed=11 + dim)
+    ex = list(range(1, 11))
+    df = np.exp(-0.05 * np.arange(1, 11) / 10)
+    pay, basis = L.make_basket_put_payoff([1.05]), L.make_polynomial_basis(degree)
+    c0 = _lib.launch_count()
+    got = L.least_square_mc(S, ex, pay, basis, discount_factors=df, num_calibration_samples=calib,
+                            dtype=np.float64).cpu().numpy()
+    assert _lib.launch_count() - c0 == 4  # gather, reduce, scale, loop
+    want = olsm.least_square_mc(S, ex, [1.05], degree, discount_factors=df, num_calibration_samples=calib,
+                                dtype=np.float64)
+    np.testing.assert_allclose(got, want, rtol=1e-9)
+    S32 = S.astype(np.float32)
+    got32 = L.least_square_mc(S32, ex, L.make_basket_put_payoff([1.05], dtype=np.float32), basis,
+                              discount_factors=df, num_calibration_samples=calib, dtype=np.float32).cpu().numpy()
+    want32 = olsm.least_square_mc(S32, ex, [1.05], degree, discount_factors=df, num_calibration_samples=calib,
+                                  dtype=np.float32)
+    np.testing.assert_allclose(got32, want32, rtol=2.5e-4)

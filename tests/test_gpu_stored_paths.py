@@ -190,12 +190,13 @@ def test_gaussian_hjm_every_time_recorded(cuda, dtype, rtol, dim):
 
 @pytest.mark.parametrize("dtype,rtol", DTYPES)
 @pytest.mark.parametrize("d", [1, 2, 4])
-def test_euler_bulk_rows_every_step(cuda, dtype, rtol, d):
-    """Every grid time recorded (times = times_grid, t = 0 included): rows of
-    72 slots x d values are a multiple of 16 bytes, so the kernel writes them
-    with bulk shared -> global copies in 128-byte pieces (2 full pieces and a
-    partial one per path for d = 1); 1000 paths leave the last CTA round
-    partly empty.  d = 4 in float64 (32 bytes per slot) takes the RowStager."""
+def test_euler_warp_rows_every_step(cuda, dtype, rtol, d):
+    """Every grid time recorded (times = times_grid, t = 0 included): the
+    kernel gathers 32-word pieces of 32 paths' rows per warp and writes each
+    path's piece with one store instruction (72 words per path for d = 1 in
+    float32: 2 full pieces and a partial one; pieces end inside a step for
+    d = 4 in float32 and every float64 case); 1000 paths leave the last warp
+    with 8 paths."""
     from tqf.models import coefficients, euler_sampling
     N, steps = 1000, 71
     rng = np.random.default_rng(20 + d)
@@ -248,7 +249,7 @@ def test_heston_every_step_of_times_grid(cuda):
 
 
 def test_every_step_declaration_is_checked(cuda):
-    """A path kernel told that every step is recorded in order (the bulk-row
+    """A path kernel told that every step is recorded in order (the warp-row
     layout) verifies it on its step table: here one date records nothing, so
     the kernel writes no state and reports TQF_E_INVALID in the status word."""
     import tqf._lib as L

@@ -32,8 +32,9 @@ __host__ __device__ inline size_t affine_stage_offset(int steps, bool staged) {
 // STAGE: 0 = each thread stores its own recorded states; 1 = through the
 // coalescing RowStager (chosen when a path's output row is long enough for
 // scattered stores to cost more than the stager's registers and shared
-// memory); 2 = BulkRowStager (every step declared recorded in order, dim ==
-// DM, DM * sizeof(T) in {4, 8, 16}, 16-byte rows and alignment).
+// memory); 2 = WarpRowStager (every step declared recorded in order: no
+// per-step slot lookup, 128-byte row pieces per store instruction, no CTA
+// barrier).
 template <typename T, int DM, int SRC, int STAGE>
 __global__ void __launch_bounds__(kBlock)
     euler_affine_kernel(tqf_euler_affine_args a, int staged) {
@@ -80,26 +81,29 @@ __global__ void __launch_bounds__(kBlock)
       return;
     }
   }
-  // with the RowStager every thread runs every round (a thread past the last
-  // path simulates that path again and its output is dropped)
+  // with the RowStager every thread runs every round, with the warp stager
+  // every lane of a warp that has a path (a thread past the last path
+  // simulates that path again and its output is dropped)
   const bool stage_out = STAGE == 1 && out != nullptr;
   RowStager<T, DM, kBlock> stg(smem + affine_stage_offset<T, DM>(steps, staged != 0), dim);
-  BulkRowStager bst(smem + affine_stage_offset<T, DM>(steps, staged != 0));
-  unsigned char* out_bytes = reinterpret_cast<unsigned char*>(out);
-  const int64_t row_bytes = (int64_t)ns * DM * (int64_t)sizeof(T);
+  WarpRowStager wst(smem + affine_stage_offset<T, DM>(steps, staged != 0));
+  uint32_t* out_words = reinterpret_cast<uint32_t*>(out);
+  const int64_t row_words = (int64_t)ns * dim * (int64_t)(sizeof(T) / 4);
   const int64_t per_round = (int64_t)gridDim.x * kBlock;
   for (int64_t base = 0; base < N; base += per_round) {
     const int64_t row0 = base + (int64_t)blockIdx.x * kBlock;
     const int64_t path = row0 + threadIdx.x;
-    if (path >= N && !stage_out) break;
+    const int64_t warp0 = row0 + (threadIdx.x & ~31);
+    if (STAGE == 2 ? warp0 >= N : (path >= N && !stage_out)) break;
     const int64_t pc = path < N ? path : N - 1;
     T x[DM];
     const T* x0 = static_cast<const T*>(a.x0) + (a.x0_per_path ? pc * dim : 0);
 #pragma unroll
     for (int j = 0; j < DM; ++j) x[j] = j < dim ? x0[j] : T(0);
+    if constexpr (STAGE == 2) wst.begin();
     if (out && a.output.init_slot >= 0) {
       if constexpr (STAGE == 2) {
-        bst.put<T, DM>(out_bytes, row_bytes, path, a.output.init_slot, x);
+        wst.put<T, DM>(x, dim, out_words, row_words, warp0, N);
       } else if (stage_out) {
         stg.put(out, ns, row0, N, a.output.init_slot, x);
       } else {
@@ -131,24 +135,25 @@ __global__ void __launch_bounds__(kBlock)
       }
 #pragma unroll
       for (int r = 0; r < DM; ++r) x[r] = xn[r];
-      const int slot = (int)row[2];
-      if (out && slot >= 0) {
-        if constexpr (STAGE == 2) {
-          bst.put<T, DM>(out_bytes, row_bytes, path, slot, x);
-        } else if (stage_out) {
-          stg.put(out, ns, row0, N, slot, x);
-        } else {
-          T* o = out + (path * ns + slot) * dim;
+      if constexpr (STAGE == 2) {
+        wst.put<T, DM>(x, dim, out_words, row_words, warp0, N);  // every step, in order
+      } else {
+        const int slot = (int)row[2];
+        if (out && slot >= 0) {
+          if (stage_out) {
+            stg.put(out, ns, row0, N, slot, x);
+          } else {
+            T* o = out + (path * ns + slot) * dim;
 #pragma unroll
-          for (int j = 0; j < DM; ++j)
-            if (j < dim) o[j] = x[j];
+            for (int j = 0; j < DM; ++j)
+              if (j < dim) o[j] = x[j];
+          }
         }
       }
     }
     if (stage_out && stg.cnt > 0) stg.flush(out, ns, row0, N);
-    if (STAGE == 2) bst.flush(out_bytes);
+    if (STAGE == 2 && wst.nw > 0) wst.flush(out_words, row_words, warp0, N);
   }
-  if (STAGE == 2) bst.finish(out_bytes);
 }
 
 template <typename T, int DM>
@@ -348,26 +353,23 @@ int launch_affine(const tqf_euler_affine_args& a, cudaStream_t s) {
   const size_t tab_bytes = (size_t)a.num_steps * kCols * sizeof(T);
   const bool staged = tab_bytes > 0 && tab_bytes <= 96 * 1024 &&
                       (reinterpret_cast<uintptr_t>(a.step_table) & 15u) == 0;
-  // bulk rows for every-step outputs of 4, 8 or 16 bytes per slot; else
-  // stage the output when a path's row is at least 64 bytes
-  constexpr bool kBulkable = DM * sizeof(T) == 4 || DM * sizeof(T) == 8 || DM * sizeof(T) == 16;
+  // the warp stager for every-step outputs; else stage the output when a
+  // path's row is at least 64 bytes
   const size_t row = (size_t)a.output.num_slots * a.dim * sizeof(T);
-  const bool bulk = kBulkable && a.output.ptr != nullptr && a.output.every_step && a.dim == DM &&
-                    (reinterpret_cast<uintptr_t>(a.output.ptr) & 15u) == 0 && row % 16 == 0;
-  const bool stage_out = !bulk && a.output.ptr != nullptr && row >= 64;
+  const bool warp_rows = a.output.ptr != nullptr && a.output.every_step &&
+                         (reinterpret_cast<uintptr_t>(a.output.ptr) & (sizeof(T) - 1)) == 0;
+  const bool stage_out = !warp_rows && a.output.ptr != nullptr && row >= 64;
   const size_t smem = affine_stage_offset<T, DM>(a.num_steps, staged) +
-                      (bulk ? (size_t)kBlock * BulkRowStager::kRowBytes
-                            : (stage_out ? RowStager<T, DM, kBlock>::kBytes : 0));
+                      (warp_rows ? WarpRowStager::bytes(kBlock / 32)
+                                 : (stage_out ? RowStager<T, DM, kBlock>::kBytes : 0));
   const bool philox = a.draws.source == TQF_DRAWS_PHILOX;
   void (*k)(tqf_euler_affine_args, int) =
       stage_out ? (philox ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX, 1>
                           : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY, 1>)
                 : (philox ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX, 0>
                           : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY, 0>);
-  if constexpr (kBulkable) {
-    if (bulk)
-      k = philox ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX, 2> : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY, 2>;
-  }
+  if (warp_rows)
+    k = philox ? euler_affine_kernel<T, DM, TQF_DRAWS_PHILOX, 2> : euler_affine_kernel<T, DM, TQF_DRAWS_MEMORY, 2>;
   if (smem > 48 * 1024) set_smem_config(k, smem);
   int occ = 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem) != cudaSuccess || occ < 1)

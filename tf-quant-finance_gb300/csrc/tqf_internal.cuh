@@ -598,93 +598,70 @@ __device__ __forceinline__ bool stage_to_smem(void* dst, const void* src, uint32
   return true;
 }
 
-// ---- every-step output by bulk stores --------------------------------------------
-// When every output slot is recorded once, in increasing order from slot 0,
-// and a path's output row is a multiple of 16 bytes long (and the output
-// 16-byte aligned), a path's recorded values fill its row front to back.
-// Then each thread gathers its own row in 128-byte pieces in a private
-// shared-memory row (16-byte vector stores of packed values) and writes each
-// full piece with one cp.async.bulk shared -> global copy: no CTA barrier, no
-// per-value global store, and threads past the last path simply stop.  The
-// row stride of 144 bytes (an odd multiple of 16 modulo 128) keeps the
-// quarter-warp phases of the 16-byte shared stores conflict-free.  Before a
-// row is refilled the thread waits (cp.async.bulk.wait_group.read 0) for its
-// previous copy to have read it; finish() waits for every copy to complete.
-// Values per slot (W) times sizeof(T) must be 4, 8 or 16 bytes.
-struct BulkRowStager {
-  static constexpr int kPiece = 128;
-  static constexpr int kRowBytes = kPiece + 16;
-  uint32_t row;         // shared-memory address of this thread's row
-  uint32_t h0, h1, h2;  // pending words of the next 16-byte store
-  int pk, nb;           // pending words, bytes gathered in the row
-  int64_t gofs;
-  __device__ explicit BulkRowStager(void* smem)
-      : row(smem_addr(smem) + threadIdx.x * (uint32_t)kRowBytes), h0(0), h1(0), h2(0), pk(0), nb(0), gofs(0) {}
-  __device__ __forceinline__ void store16(uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
-    asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(row + (uint32_t)nb), "r"(a), "r"(b), "r"(c),
-                 "r"(d)
-                 : "memory");
-    nb += 16;
+// ---- every-step output rows ------------------------------------------------------
+// Every-step output rows through a per-warp transposition buffer.  Each step
+// a lane appends its path's values (as 32-bit words) to its own row of the
+// warp's [32][33] word buffer in shared memory; when 32 words per path have
+// gathered, the warp writes them path by path: one store instruction puts 32
+// consecutive words (128 bytes) of one path's output row.  Only __syncwarp,
+// no CTA barrier, no per-step slot lookup: the launch has checked that every
+// step is recorded in order (tqf_path_output.every_step), so each path's row
+// fills front to back.  Every lane of the warp takes part in every put and
+// flush (a lane past the last path works on a duplicate path and its stores
+// are dropped).  Row padding of 33 words keeps both the appends and the
+// column reads free of bank conflicts.
+struct WarpRowStager {
+  static constexpr int kStride = 33;
+  static constexpr int kWarpWords = 32 * kStride;
+  static constexpr size_t bytes(int warps) { return (size_t)warps * kWarpWords * 4; }
+  uint32_t* wbuf;  // this warp's buffer
+  int nw;          // words per lane gathered in the current piece (warp-uniform)
+  int64_t w0;      // row word offset of the current piece
+  __device__ explicit WarpRowStager(void* smem)
+      : wbuf(static_cast<uint32_t*>(smem) + (threadIdx.x >> 5) * kWarpWords), nw(0), w0(0) {}
+  __device__ __forceinline__ void begin() {
+    nw = 0;
+    w0 = 0;
   }
-  // Appends the W values x[0..W) of `slot` of path `path` (row_bytes = the
-  // output row length in bytes); W * sizeof(T) is 4, 8 or 16.
-  template <typename T, int W>
-  __device__ __forceinline__ void put(unsigned char* out, int64_t row_bytes, int64_t path, int slot, const T* x) {
-    constexpr int B = W * (int)sizeof(T);
-    static_assert(B == 4 || B == 8 || B == 16, "bulk rows take 4, 8 or 16 bytes per slot");
-    if (nb == 0 && pk == 0) {
-      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-      gofs = path * row_bytes + (int64_t)slot * B;
+  // Writes the gathered words of the warp's 32 paths path0 .. path0 + 31
+  // (rows of row_words words) and starts the next piece.
+  __device__ __forceinline__ void flush(uint32_t* out, int64_t row_words, int64_t path0, int64_t N) {
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    const int rmax = N - path0 < 32 ? (int)(N - path0) : 32;
+    const bool on = lane < nw;
+    const uint32_t* src = wbuf + lane;
+    uint32_t* dst = out + path0 * row_words + w0 + lane;
+#pragma unroll 8
+    for (int r = 0; r < 32; ++r) {
+      const uint32_t v = src[r * kStride];
+      if (on && r < rmax) *dst = v;
+      dst += row_words;
     }
-    uint32_t w[B / 4];
-    if constexpr (sizeof(T) == 4) {
+    __syncwarp();
+    w0 += nw;
+    nw = 0;
+  }
+  __device__ __forceinline__ void push(uint32_t w, uint32_t* out, int64_t row_words, int64_t path0, int64_t N) {
+    wbuf[(threadIdx.x & 31) * kStride + nw] = w;
+    if (++nw == 32) flush(out, row_words, path0, N);
+  }
+  // Appends the first `dim` of the DM values of this step.
+  template <typename T, int DM>
+  __device__ __forceinline__ void put(const T* x, int dim, uint32_t* out, int64_t row_words, int64_t path0,
+                                      int64_t N) {
 #pragma unroll
-      for (int c = 0; c < W; ++c) w[c] = __float_as_uint(x[c]);
-    } else {
-#pragma unroll
-      for (int c = 0; c < W; ++c) {
-        const unsigned long long u = __double_as_longlong(x[c]);
-        w[2 * c] = (uint32_t)u;
-        w[2 * c + 1] = (uint32_t)(u >> 32);
+    for (int c = 0; c < DM; ++c) {
+      if (c < dim) {
+        if constexpr (sizeof(T) == 4) {
+          push(__float_as_uint(x[c]), out, row_words, path0, N);
+        } else {
+          const unsigned long long u = __double_as_longlong(x[c]);
+          push((uint32_t)u, out, row_words, path0, N);
+          push((uint32_t)(u >> 32), out, row_words, path0, N);
+        }
       }
     }
-    if constexpr (B == 16) {
-      store16(w[0], w[1], w[2], w[3]);
-    } else if constexpr (B == 8) {
-      if (pk == 0) {
-        h0 = w[0];
-        h1 = w[1];
-        pk = 2;
-      } else {
-        store16(h0, h1, w[0], w[1]);
-        pk = 0;
-      }
-    } else {
-      if (pk == 0) h0 = w[0];
-      else if (pk == 1) h1 = w[0];
-      else if (pk == 2) h2 = w[0];
-      if (pk == 3) {
-        store16(h0, h1, h2, w[0]);
-        pk = 0;
-      } else {
-        ++pk;
-      }
-    }
-    if (nb == kPiece) flush(out);
-  }
-  // Writes the gathered bytes (whole 16-byte groups under the layout contract).
-  __device__ __forceinline__ void flush(unsigned char* out) {
-    if (nb == 0) return;
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(out + gofs), "r"(row),
-                 "r"(nb)
-                 : "memory");
-    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-    nb = 0;
-  }
-  __device__ __forceinline__ void finish(unsigned char* out) {
-    flush(out);
-    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
   }
 };
 

@@ -52,9 +52,9 @@ __device__ __forceinline__ void load_coef(GbmCoef<T, DM>* c, int dim, const void
 // STAGE: 1 = recorded states go through the coalescing RowStager (dynamic
 // shared memory), chosen when a path's output row is at least 64 bytes; then
 // every thread runs every round and a thread past the last path simulates
-// that path again with its output dropped.  2 = BulkRowStager (every date
-// declared recorded in order, dim == DM, DM * sizeof(T) in {4, 8, 16},
-// 16-byte rows and alignment).  0 = direct stores.
+// that path again with its output dropped.  2 = WarpRowStager (every date
+// declared recorded in order; every lane of a warp that has a path runs every
+// round).  0 = direct stores.
 template <typename T, int DM, int STAGE>
 __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
   __shared__ GbmCoef<T, DM> coef;
@@ -77,14 +77,15 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
     }
   }
   RowStager<T, DM, kBlock> stg(stage_smem, dim);
-  BulkRowStager bst(stage_smem);
-  unsigned char* out_bytes = reinterpret_cast<unsigned char*>(out);
-  const int64_t row_bytes = (int64_t)ns * DM * (int64_t)sizeof(T);
+  WarpRowStager wst(stage_smem);
+  uint32_t* out_words = reinterpret_cast<uint32_t*>(out);
+  const int64_t row_words = (int64_t)ns * dim * (int64_t)(sizeof(T) / 4);
   const int64_t per_round = (int64_t)gridDim.x * kBlock;
   for (int64_t base = 0; base < N; base += per_round) {
     const int64_t row0 = base + (int64_t)blockIdx.x * kBlock;
     const int64_t path = row0 + threadIdx.x;
-    if (STAGE != 1 && path >= N) break;
+    const int64_t warp0 = row0 + (threadIdx.x & ~31);
+    if (STAGE == 2 ? warp0 >= N : (STAGE == 0 && path >= N)) break;
     const int64_t pc = path < N ? path : N - 1;
     const T* x0p = static_cast<const T*>(a.x0) + (a.x0_per_path ? pc * dim : 0);
     T x0[DM], cs[DM];
@@ -93,9 +94,10 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
       x0[j] = j < dim ? x0p[j] : T(0);
       cs[j] = T(0);
     }
+    if constexpr (STAGE == 2) wst.begin();
     if (a.output.init_slot >= 0) {
       if constexpr (STAGE == 2) {
-        bst.put<T, DM>(out_bytes, row_bytes, path, a.output.init_slot, x0);
+        wst.put<T, DM>(x0, dim, out_words, row_words, warp0, N);
       } else if constexpr (STAGE == 1) {
         stg.put(out, ns, row0, N, a.output.init_slot, x0);
       } else {
@@ -119,12 +121,12 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
         for (int c = 0; c <= r; ++c) y += coef.L[r * DM + c] * z[c];
         cs[r] += coef.drift[r] * dt + sdt * coef.sigma[r] * y;
       }
-      if (slot >= 0) {
+      if (STAGE == 2 || slot >= 0) {  // STAGE 2: every date, in order
         if constexpr (STAGE == 2) {
           T xs[DM];
 #pragma unroll
           for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
-          bst.put<T, DM>(out_bytes, row_bytes, path, slot, xs);
+          wst.put<T, DM>(xs, dim, out_words, row_words, warp0, N);
         } else if constexpr (STAGE == 1) {
           T xs[DM];
 #pragma unroll
@@ -139,9 +141,8 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
       }
     }
     if (STAGE == 1 && stg.cnt > 0) stg.flush(out, ns, row0, N);
-    if (STAGE == 2) bst.flush(out_bytes);
+    if (STAGE == 2 && wst.nw > 0) wst.flush(out_words, row_words, warp0, N);
   }
-  if (STAGE == 2) bst.finish(out_bytes);
 }
 
 // ---- tensor-core L z (split BF16, three products) ------------------------------
@@ -661,19 +662,15 @@ __global__ void __launch_bounds__(256) cholesky_f64_global_kernel(const double* 
 
 template <typename T, int DM>
 int launch_paths(const tqf_mvgbm_args& a, cudaStream_t s) {
-  // bulk rows for every-date outputs of 4, 8 or 16 bytes per date; else
-  // stage the output when a path's row is at least 64 bytes
-  constexpr bool kBulkable = DM * sizeof(T) == 4 || DM * sizeof(T) == 8 || DM * sizeof(T) == 16;
+  // the warp stager for every-date outputs; else stage the output when a
+  // path's row is at least 64 bytes
   const size_t row = (size_t)a.output.num_slots * a.dim * sizeof(T);
-  const bool bulk = kBulkable && a.output.every_step && a.dim == DM &&
-                    (reinterpret_cast<uintptr_t>(a.output.ptr) & 15u) == 0 && row % 16 == 0;
-  const bool stage = !bulk && row >= 64;
+  const bool warp_rows = a.output.every_step && (reinterpret_cast<uintptr_t>(a.output.ptr) & (sizeof(T) - 1)) == 0;
+  const bool stage = !warp_rows && row >= 64;
   auto k = stage ? mvgbm_paths_kernel<T, DM, 1> : mvgbm_paths_kernel<T, DM, 0>;
-  if constexpr (kBulkable) {
-    if (bulk) k = mvgbm_paths_kernel<T, DM, 2>;
-  }
+  if (warp_rows) k = mvgbm_paths_kernel<T, DM, 2>;
   const size_t smem =
-      bulk ? (size_t)kBlock * BulkRowStager::kRowBytes : (stage ? RowStager<T, DM, kBlock>::kBytes : 0);
+      warp_rows ? WarpRowStager::bytes(kBlock / 32) : (stage ? RowStager<T, DM, kBlock>::kBytes : 0);
   if (smem > 48 * 1024) set_smem_config(k, smem);
   int occ = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBlock, smem);
