@@ -11,6 +11,7 @@
 // cross-path accumulation in a fixed order (deterministic).  The CTA loop is
 // persistent: grid = SMs x resident CTAs, each CTA walks path tiles.
 #include <mutex>
+#include <vector>
 
 #include "tqf_internal.cuh"
 
@@ -680,12 +681,52 @@ KernelFn<T, SCHEME> pick_kernel(int src, bool store, bool price, bool anti = fal
               : pick<T, SCHEME, TQF_DRAWS_PHILOX, false>(store, price);
 }
 
+// cuCtxGetId through the runtime's driver entry-point query, so the library
+// needs no link against libcuda.  nullptr when the driver lacks it.
+using CtxGetIdFn = int (*)(void* ctx, unsigned long long* id);
+CtxGetIdFn ctx_get_id_fn() {
+  static CtxGetIdFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    cudaGetLastError();
+    return reinterpret_cast<CtxGetIdFn>(p);
+  }();
+  return fn;
+}
+
 template <typename T, int SCHEME>
 int grid_for(int64_t N, int ns, int steps, bool staged, int src, bool store, bool price,
              SmemLayout* out_layout, bool anti = false) {
   const int cols = SCHEME == 0 ? kFtCols : kQeCols;
   SmemLayout L = smem_layout<T>(steps, cols, price ? ns : 0, staged, store, src == TQF_DRAWS_SOBOL);
   if (out_layout) *out_layout = L;
+  // The kernel attributes and the occupancy query are driver calls that a
+  // pricing call would otherwise repeat (twice: workspace size, launch); the
+  // result is kept per context (a reset context needs the attributes again).
+  struct Key {
+    unsigned long long ctx;
+    int64_t N;
+    int ns, steps, src;
+    bool staged, store, price, anti;
+  };
+  static std::mutex mu;
+  static std::vector<std::pair<Key, int>> cache;
+  unsigned long long ctx = 0;
+  const CtxGetIdFn get_id = ctx_get_id_fn();
+  const bool have_ctx = get_id != nullptr && get_id(nullptr, &ctx) == 0;
+  const Key key{ctx, N, ns, steps, src, staged, store, price, anti};
+  auto same = [&](const Key& k) {
+    return k.ctx == key.ctx && k.N == key.N && k.ns == key.ns && k.steps == key.steps && k.src == key.src &&
+           k.staged == key.staged && k.store == key.store && k.price == key.price && k.anti == key.anti;
+  };
+  if (have_ctx) {
+    std::lock_guard<std::mutex> lock(mu);
+    for (const auto& e : cache)
+      if (same(e.first)) return e.second;
+  }
   auto k = pick_kernel<T, SCHEME>(src, store, price, anti);
   set_smem_config(k, L.total);
   int occ = 0;
@@ -696,6 +737,11 @@ int grid_for(int64_t N, int ns, int steps, bool staged, int src, bool store, boo
   const int64_t cap = (int64_t)num_sms() * occ;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
+  if (have_ctx) {
+    std::lock_guard<std::mutex> lock(mu);
+    if (cache.size() >= 256) cache.erase(cache.begin());
+    cache.push_back({key, (int)blocks});
+  }
   return (int)blocks;
 }
 
@@ -777,21 +823,6 @@ struct NoAllocSlot {
 };
 NoAllocSlot g_noalloc_slot[kNoAllocMaxDevices] = {};
 
-// cuCtxGetId through the runtime's driver entry-point query, so the library
-// needs no link against libcuda.  nullptr when the driver lacks it.
-using CtxGetIdFn = int (*)(void* ctx, unsigned long long* id);
-CtxGetIdFn ctx_get_id_fn() {
-  static CtxGetIdFn fn = [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      p = nullptr;
-    cudaGetLastError();
-    return reinterpret_cast<CtxGetIdFn>(p);
-  }();
-  return fn;
-}
 
 // Device address of g_noalloc_partials in the current device's context (the
 // host-side symbol is only a stand-in, never a device pointer).  The address

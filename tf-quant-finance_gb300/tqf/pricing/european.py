@@ -33,6 +33,14 @@ class MonteCarloResult:
     sums: torch.Tensor  # [n_strikes, 2] raw (sum, sum of squares) of undiscounted payoffs
     num_paths: int
     discount: float
+    stats: "torch.Tensor | None" = None  # [2, n_strikes]: price and standard_error are its rows
+
+    def to_host(self):
+        """(price, standard_error) as host arrays, read with one device-to-host copy."""
+        if self.stats is not None:
+            both = self.stats.cpu().numpy()
+            return both[0], both[1]
+        return self.price.cpu().numpy(), self.standard_error.cpu().numpy()
 
 
 def stats_from_sums(sums: torch.Tensor, n: int, discount: float) -> MonteCarloResult:
@@ -43,7 +51,7 @@ def stats_from_sums(sums: torch.Tensor, n: int, discount: float) -> MonteCarloRe
     _lib.call("tqf_mc_price_stats", sums.data_ptr(), ns, int(n), float(discount), price_se.data_ptr(),
               _lib.stream_ptr(sums.device))
     return MonteCarloResult(price=price_se[0], standard_error=price_se[1], sums=sums,
-                            num_paths=n, discount=discount)
+                            num_paths=n, discount=discount, stats=price_se)
 
 
 def make_payoff(strikes, is_call, dtype, device, num_paths, ws_bytes_fn, tag):
@@ -51,8 +59,9 @@ def make_payoff(strikes, is_call, dtype, device, num_paths, ws_bytes_fn, tag):
         # host tensor in the compute dtype: one copy, asynchronous on the
         # current stream when the tensor is pinned (the caller keeps it
         # unchanged until the stream has passed the call, as for any
-        # non-blocking copy), synchronous otherwise
-        k = strikes.reshape(-1).to(device, non_blocking=strikes.is_pinned())
+        # non-blocking copy), synchronous otherwise (non_blocking has no
+        # effect on pageable memory, so no pinned-memory query is needed)
+        k = strikes.reshape(-1).to(device, non_blocking=True)
     else:
         k = torch.as_tensor(utils.to_numpy(strikes, np.float64).reshape(-1), dtype=dtype).to(device)
     ns = int(k.numel())
