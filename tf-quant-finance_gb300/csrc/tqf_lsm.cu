@@ -912,9 +912,9 @@ __device__ bool loop_barrier(LoopSync* sy, unsigned gen, int32_t* status) {
 
 // The rotation (c, s) of the pair (x, xp) of the current round, from the
 // lanes holding A_pp, A_qq and A_pq (Golub & Van Loan, sym.schur2); identity
-// when x has no partner.  Kept out of line: the solver runs in one warp once
-// per date, so its code is cold in the instruction cache and small code is
-// what makes it fast.
+// when x has no partner.  Kept out of line: the pseudo-inverse runs in one
+// warp per date, so its code is cold in the instruction cache and small code
+// is what makes it fast.
 template <int G>
 __device__ __noinline__ float2 jacobi_rot_f32(float af, int x, int xp) {
   const int p = xp < 0 ? x : (x < xp ? x : xp), q = xp < 0 ? x : (x < xp ? xp : x);

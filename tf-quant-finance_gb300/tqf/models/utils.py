@@ -109,8 +109,8 @@ def prepare_grid(*, times, time_step, dtype, tolerance=None, num_time_steps=None
 def every_step_layout(step_slot, init_slot: int, steps_exec: int, num_slots: int) -> int:
     """1 if step i records slot base + i for every executed step (base = 1
     after an initial state at slot 0) and the slots end at num_slots: the
-    tqf_path_output.every_step declaration that lets the path kernels write
-    whole rows with bulk copies."""
+    tqf_path_output.every_step declaration that lets the Euler and GBM path
+    kernels write rows front to back through their per-warp stager."""
     base = 1 if init_slot >= 0 else 0
     if init_slot not in (-1, 0) or base + int(steps_exec) != int(num_slots):
         return 0
