@@ -168,7 +168,12 @@ struct LzShape {
   static constexpr int kBTile = KP * KP * 2;
   // TMEM columns: two buffers of KP, rounded up to a power of two >= 32
   static constexpr uint32_t kTmemCols = KB == 1 ? 32u : (KB == 2 ? 64u : 128u);
-  static constexpr size_t kSmem = 1024 + 4 * (size_t)kATile + 2 * (size_t)kBTile;
+  // From 48 factors on, one A buffer: the next step's normals are staged
+  // once this step's MMAs have read the tile (its TMEM result stays double
+  // buffered), which halves the A tiles and lets more CTAs share an SM.
+  static constexpr bool kSingleA = KB >= 3;
+  static constexpr int kATiles = kSingleA ? 2 : 4;
+  static constexpr size_t kSmem = 1024 + kATiles * (size_t)kATile + 2 * (size_t)kBTile;
 };
 
 __device__ __forceinline__ uint32_t pack2_bf16(float a, float b) {
@@ -197,8 +202,8 @@ __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_ar
   constexpr int KP = Sh::KP;
   extern __shared__ __align__(1024) unsigned char smem[];
   LzSmem* S = reinterpret_cast<LzSmem*>(smem);
-  unsigned char* sA = smem + 1024;          // [2 buffers][hi, lo] x kATile
-  unsigned char* sB = sA + 4 * Sh::kATile;  // L_hi, L_lo
+  unsigned char* sA = smem + 1024;                 // [1 or 2 buffers][hi, lo] x kATile
+  unsigned char* sB = sA + Sh::kATiles * Sh::kATile;  // L_hi, L_lo
   const int tid = threadIdx.x, warp = tid >> 5;
   const int dim = FULL ? KP : a.dim;
   // split L (row-major [dim][dim], lower; zero-padded to KP) into BF16 hi/lo
@@ -270,7 +275,7 @@ __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_ar
     if (valid && a.output.init_slot >= 0) record(a.output.init_slot, true);
     // write the split normals of `step` into buffer b
     auto stage = [&](int step, int b) {
-      unsigned char* th = sA + (2 * b) * Sh::kATile;
+      unsigned char* th = sA + (Sh::kSingleA ? 0 : 2 * b) * Sh::kATile;
       unsigned char* tl = th + Sh::kATile;
 #pragma unroll
       for (int kb = 0; kb < KB; ++kb) {
@@ -298,7 +303,7 @@ __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_ar
       __syncthreads();
       tc::fence_after_sync();
       if (tid == 0) {
-        const uint32_t ah = smem_addr(sA + (2 * b) * Sh::kATile), al = ah + Sh::kATile;
+        const uint32_t ah = smem_addr(sA + (Sh::kSingleA ? 0 : 2 * b) * Sh::kATile), al = ah + Sh::kATile;
         const uint32_t bh = smem_addr(sB), bl = bh + Sh::kBTile;
         const uint32_t d = tmem + (uint32_t)(KP * b);
 #pragma unroll
@@ -325,7 +330,7 @@ __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_ar
     }
     for (int i = 0; i < steps; ++i) {
       const int b = i & 1;
-      if (i + 1 < steps) {
+      if (!Sh::kSingleA && i + 1 < steps) {
         stage(i + 1, b ^ 1);
         issue(b ^ 1);
       }
@@ -336,6 +341,12 @@ __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_ar
       }
       phase[b] ^= 1u;
       tc::fence_after_sync();
+      if (Sh::kSingleA && i + 1 < steps) {
+        // step i's MMAs have read the single A tile: stage and issue step
+        // i + 1 (into the other TMEM buffer) before consuming step i
+        stage(i + 1, b ^ 1);
+        issue(b ^ 1);
+      }
 #pragma unroll
       for (int kb = 0; kb < KB; ++kb) {
         float y[16];
