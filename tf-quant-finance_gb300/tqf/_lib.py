@@ -551,10 +551,16 @@ def launch_count() -> int:
     return int(load().tqf_launch_count())
 
 
+_cuda_checked = False
+
+
 def require_cuda() -> torch.device:
-    if not torch.cuda.is_available():
-        raise RuntimeError("tqf runs on a CUDA device (sm_103a); none is available")
-    load()
+    global _cuda_checked
+    if not _cuda_checked:
+        if not torch.cuda.is_available():
+            raise RuntimeError("tqf runs on a CUDA device (sm_103a); none is available")
+        load()
+        _cuda_checked = True
     return torch.device("cuda", torch.cuda.current_device())
 
 

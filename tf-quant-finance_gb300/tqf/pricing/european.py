@@ -11,6 +11,7 @@ from tqf import _lib
 from tqf.models import utils
 
 _workspaces: dict[tuple[int, str], torch.Tensor] = {}
+_ws_bytes: dict[tuple, int] = {}  # workspace sizes per (tag, device, strikes, paths, dtype)
 
 
 def workspace(nbytes: int, device: torch.device, tag: str) -> torch.Tensor:
@@ -43,13 +44,14 @@ class MonteCarloResult:
         return self.price.cpu().numpy(), self.standard_error.cpu().numpy()
 
 
-def stats_from_sums(sums: torch.Tensor, n: int, discount: float) -> MonteCarloResult:
+def stats_from_sums(sums: torch.Tensor, n: int, discount: float, stream: int | None = None) -> MonteCarloResult:
     """Discounted means and standard errors (unbiased variance) of the
-    [n_strikes, 2] payoff sums, in one kernel (tqf_mc_price_stats)."""
+    [n_strikes, 2] payoff sums, in one kernel (tqf_mc_price_stats) on
+    `stream` (default: the current stream of the sums' device)."""
     ns = int(sums.shape[0])
     price_se = torch.empty((2, ns), dtype=torch.float64, device=sums.device)
     _lib.call("tqf_mc_price_stats", sums.data_ptr(), ns, int(n), float(discount), price_se.data_ptr(),
-              _lib.stream_ptr(sums.device))
+              _lib.stream_ptr(sums.device) if stream is None else stream)
     return MonteCarloResult(price=price_se[0], standard_error=price_se[1], sums=sums,
                             num_paths=n, discount=discount, stats=price_se)
 
@@ -69,7 +71,14 @@ def make_payoff(strikes, is_call, dtype, device, num_paths, ws_bytes_fn, tag):
     if is_call is not None:
         calls = torch.as_tensor(np.broadcast_to(np.asarray(is_call, dtype=np.uint8), (ns,)).copy()).to(device)
     out = torch.empty((ns, 2), dtype=torch.float64, device=device)  # written whole by the sum reduction
-    nbytes = int(ws_bytes_fn(ns))
+    # the size depends only on these (ws_bytes_fn is the same function of ns
+    # for a given tag, device, path count and dtype)
+    idx = device.index if device.index is not None else torch.cuda.current_device()
+    wkey = (tag, idx, ns, num_paths, dtype)
+    nbytes = _ws_bytes.get(wkey)
+    if nbytes is None:
+        nbytes = int(ws_bytes_fn(ns))
+        _ws_bytes[wkey] = nbytes
     ws = workspace(nbytes, device, tag)
     p = _lib.Payoff()
     p.num_strikes = ns

@@ -99,7 +99,7 @@ def heston_european_mc(*, strikes, expiry, spot, variance, mean_reversion, theta
     qe_flag = 1 if qe else 0
     p, out, keep = make_payoff(strikes, is_call_options, td, device, N,
                                lambda ns: _lib.load().tqf_heston_workspace_bytes(_lib.dtype_code(td), qe_flag, N, ns),
-                               "heston")
+                               "heston_qe" if qe else "heston_ft")
     p.spot_scale = scale
     args = _lib.HestonArgs()
     args.dtype = _lib.dtype_code(td)
@@ -110,9 +110,10 @@ def heston_european_mc(*, strikes, expiry, spot, variance, mean_reversion, theta
     args.draws = draws
     args.payoff = p
     args.dev_status = _lib.status_buffer(device).data_ptr()
-    _lib.call("tqf_heston_qe" if qe else "tqf_heston_euler", args, _lib.stream_ptr(device))
+    stream = _lib.stream_ptr(device)
+    _lib.call("tqf_heston_qe" if qe else "tqf_heston_euler", args, stream)
     del keep, draws_keep
-    return stats_from_sums(out, N, float(np.exp(-r * T)))
+    return stats_from_sums(out, N, float(np.exp(-r * T)), stream)
 
 
 def heston_european_vjp(grad_prices, *, strikes, expiry, spot, variance, mean_reversion, theta, volvol, rho,
