@@ -1,0 +1,85 @@
+"""In-kernel Philox draws taken a whole block at a time (GPU).
+
+When a step takes exactly 1, 2, 4, 8 or 16 normals of the canonical stream
+(draw k = step dim + c of path n, four float32 or two float64 normals per
+Philox block), the Euler and exact-GBM path kernels walk whole Philox blocks
+per group of steps instead of testing every draw against the current block.
+The paths must equal, bit for bit, the same kernels reading the stream's
+materialised normals (`generate_mc_normal_draws`, which fills element
+(step, n, c) from draw step dim + c of path n): with every step recorded
+(warp stager) and with the last time only, with a step count that leaves a
+partial last group, with antithetic pairs (the sign carried by sqrt(dt)),
+and for dimensions that keep the per-draw reader (3, 5) as controls.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _draws(d, steps, n, antithetic, seed, dtype):
+    from tqf.math.random import RandomType
+    from tqf.models import utils
+    rt = RandomType.STATELESS_ANTITHETIC if antithetic else RandomType.STATELESS
+    z = utils.generate_mc_normal_draws(d, steps, n, rt, seed=seed, dtype=dtype)
+    return rt, z.permute(1, 0, 2)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("d", [1, 2, 3, 4, 5, 8])
+@pytest.mark.parametrize("steps", [37, 64])
+@pytest.mark.parametrize("every", [True, False])
+def test_euler_whole_blocks_equal_materialised(cuda, dtype, d, steps, every):
+    from tqf.models import coefficients, euler_sampling
+    np_dt = np.float32 if dtype == torch.float32 else np.float64
+    rng = np.random.default_rng(100 + d + steps)
+    drift, vol = coefficients.gbm(rng.uniform(-0.05, 0.05, d), rng.uniform(0.1, 0.3, d),
+                                  0.5 * np.eye(d) + 0.5)
+    grid = np.linspace(0.0, 1.0, steps + 1).astype(np_dt)
+    times = grid if every else grid[-1:]
+    x0 = np.linspace(1.0, 2.0, d).astype(np_dt)
+    N = 1000
+    for antithetic in (False, True):
+        rt, z = _draws(d, steps, N, antithetic, [5, 6], dtype)
+        kw = dict(times_grid=grid, initial_state=x0, dtype=dtype)
+        fused = euler_sampling.sample(d, drift, vol, times, num_samples=N, random_type=rt, seed=[5, 6], **kw)
+        mat = euler_sampling.sample(d, drift, vol, times, normal_draws=z, **kw)
+        assert fused.shape == (N, len(times), d)
+        torch.testing.assert_close(fused, mat, rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("d", [1, 2, 3, 4, 8])
+@pytest.mark.parametrize("k", [1, 37, 64])
+def test_exact_gbm_whole_blocks_equal_materialised(cuda, dtype, d, k):
+    from tqf.models import MultivariateGeometricBrownianMotion
+    np_dt = np.float32 if dtype == torch.float32 else np.float64
+    rng = np.random.default_rng(200 + d + k)
+    q, _ = np.linalg.qr(rng.standard_normal((d, d)))
+    corr = q @ np.diag(rng.uniform(0.5, 1.5, d)) @ q.T
+    s = np.sqrt(np.diag(corr))
+    corr = corr / s[:, None] / s[None, :]
+    proc = MultivariateGeometricBrownianMotion(d, means=rng.uniform(0.0, 0.05, d), volatilities=rng.uniform(0.1, 0.4, d),
+                                               corr_matrix=corr, dtype=np_dt)
+    times = np.linspace(0.0, 1.0, k + 1)[1:].astype(np_dt)
+    N = 1000
+    for antithetic in (False, True):
+        rt, z = _draws(d, k, N, antithetic, [7, 8], dtype)
+        fused = proc.sample_paths(times, initial_state=np.full(d, 100.0, np_dt), num_samples=N, random_type=rt,
+                                  seed=[7, 8])
+        mat = proc.sample_paths(times, initial_state=np.full(d, 100.0, np_dt), normal_draws=z)
+        assert fused.shape == (N, k, d)
+        torch.testing.assert_close(fused, mat, rtol=0, atol=0)
+
+
+def test_univariate_gbm_whole_blocks_equal_materialised(cuda):
+    from tqf.models import GeometricBrownianMotion
+    proc = GeometricBrownianMotion(0.05, 0.2, dtype=np.float32)
+    times = (np.arange(1, 253) / 252).astype(np.float32)
+    N = 4100
+    rt, z = _draws(1, 252, N, False, [1, 2], torch.float32)
+    fused = proc.sample_paths(times, initial_state=100.0, num_samples=N, random_type=rt, seed=[1, 2])
+    mat = proc.sample_paths(times, initial_state=100.0, normal_draws=z)
+    torch.testing.assert_close(fused, mat, rtol=0, atol=0)

@@ -29,6 +29,27 @@ __host__ __device__ inline size_t affine_stage_offset(int steps, bool staged) {
   return (head + (staged ? (size_t)steps * kCols * sizeof(T) : 0) + 15) & ~(size_t)15;
 }
 
+// x <- x + dt (m + M x) + (s0 + s1 x) (C dw): rows in order, columns summed
+// in order (padding rows and columns are zero).
+template <typename T, int DM>
+__device__ __forceinline__ void affine_advance(const AffineCoef<T, DM>& cf, T (&x)[DM], const T (&dw)[DM], T dt) {
+  T xn[DM];
+#pragma unroll
+  for (int r = 0; r < DM; ++r) {
+    T drift = cf.m[r];
+    T y = T(0);
+#pragma unroll
+    for (int c = 0; c < DM; ++c) {
+      drift += cf.M[r * DM + c] * x[c];
+      y += cf.C[r * DM + c] * dw[c];
+    }
+    const T vol = cf.s0[r] + cf.s1[r] * x[r];
+    xn[r] = x[r] + dt * drift + vol * y;
+  }
+#pragma unroll
+  for (int r = 0; r < DM; ++r) x[r] = xn[r];
+}
+
 // STAGE: 0 = each thread stores its own recorded states; 1 = through the
 // coalescing RowStager (chosen when a path's output row is long enough for
 // scattered stores to cost more than the stager's registers and shared
@@ -81,6 +102,14 @@ __global__ void __launch_bounds__(kBlock)
       return;
     }
   }
+  // In-kernel Philox draws of exactly DM components per step with the table
+  // in shared memory: the loop walks whole Philox blocks (PhiloxGroup).
+  using PG = PhiloxGroup<T, DM>;
+  const bool whole_blocks = SRC == TQF_DRAWS_PHILOX && PG::kAligned && dim == DM && staged;
+  // one-factor coefficients live in registers
+  AffineCoef<T, DM> creg;
+  if constexpr (DM == 1) creg = *coef;
+  const AffineCoef<T, DM>* cf = DM == 1 ? &creg : coef;
   // with the RowStager every thread runs every round, with the warp stager
   // every lane of a warp that has a path (a thread past the last path
   // simulates that path again and its output is dropped)
@@ -113,32 +142,12 @@ __global__ void __launch_bounds__(kBlock)
           if (j < dim) o[j] = x[j];
       }
     }
-    DrawSource<T> src(a.draws, pc, dim);
-    for (int i = 0; i < steps; ++i) {
-      const T* row = table + (size_t)i * kCols;
-      const T dt = row[0], sdt = row[1];
-      T dw[DM];
-#pragma unroll
-      for (int c = 0; c < DM; ++c) dw[c] = c < dim ? src.get(i, c) * sdt : T(0);
-      T xn[DM];
-#pragma unroll
-      for (int r = 0; r < DM; ++r) {
-        T drift = coef->m[r];
-        T y = T(0);
-#pragma unroll
-        for (int c = 0; c < DM; ++c) {
-          drift += coef->M[r * DM + c] * x[c];
-          y += coef->C[r * DM + c] * dw[c];
-        }
-        const T vol = coef->s0[r] + coef->s1[r] * x[r];
-        xn[r] = x[r] + dt * drift + vol * y;
-      }
-#pragma unroll
-      for (int r = 0; r < DM; ++r) x[r] = xn[r];
+    // records the state after step i at its slot (STAGE 2: every step, in order)
+    auto record = [&](int i) {
       if constexpr (STAGE == 2) {
-        wst.put<T, DM>(x, dim, out_words, row_words, warp0, N);  // every step, in order
+        wst.put<T, DM>(x, dim, out_words, row_words, warp0, N);
       } else {
-        const int slot = (int)row[2];
+        const int slot = (int)table[(size_t)i * kCols + 2];
         if (out && slot >= 0) {
           if (stage_out) {
             stg.put(out, ns, row0, N, slot, x);
@@ -149,6 +158,44 @@ __global__ void __launch_bounds__(kBlock)
               if (j < dim) o[j] = x[j];
           }
         }
+      }
+    };
+    DrawSource<T> src(a.draws, pc, dim);
+    if (whole_blocks) {
+      // dw = z (sign sqrt dt) equals (sign z) sqrt dt exactly (sign = +-1);
+      // the warp stager makes room for a whole group's words at once
+      constexpr int kGroupWords = PG::kNormals * (int)(sizeof(T) / 4);
+      static_assert(kGroupWords <= 32, "a group's words fit one piece");
+      for (int i = 0; i < steps; i += PG::kSteps) {
+        if constexpr (STAGE == 2) wst.make_room(kGroupWords, out_words, row_words, warp0, N);
+        T z[PG::kNormals];
+        PG::get(i / PG::kSteps, src.rng.path, src.rng.k0, src.rng.k1, z);
+#pragma unroll
+        for (int s = 0; s < PG::kSteps; ++s) {
+          if (PG::kSteps > 1 && i + s >= steps) break;
+          T dt, sdt;
+          step_pair<false>(table + (size_t)(i + s) * kCols, dt, sdt);
+          sdt *= src.sign;
+          T dw[DM];
+#pragma unroll
+          for (int c = 0; c < DM; ++c) dw[c] = z[s * DM + c] * sdt;
+          affine_advance<T, DM>(*cf, x, dw, dt);
+          if constexpr (STAGE == 2) {
+            wst.append<T, DM>(x);
+          } else {
+            record(i + s);
+          }
+        }
+      }
+    } else {
+      for (int i = 0; i < steps; ++i) {
+        const T* row = table + (size_t)i * kCols;
+        const T dt = row[0], sdt = row[1];
+        T dw[DM];
+#pragma unroll
+        for (int c = 0; c < DM; ++c) dw[c] = c < dim ? src.get(i, c) * sdt : T(0);
+        affine_advance<T, DM>(*cf, x, dw, dt);
+        record(i);
       }
     }
     if (stage_out && stg.cnt > 0) stg.flush(out, ns, row0, N);

@@ -400,6 +400,50 @@ struct PhiloxReader<double> {
   }
 };
 
+__device__ __forceinline__ void philox_normals(int64_t block, int64_t path, uint32_t k0, uint32_t k1, float* z) {
+  philox_normals4_f32(block, path, k0, k1, z);
+}
+__device__ __forceinline__ void philox_normals(int64_t block, int64_t path, uint32_t k0, uint32_t k1, double* z) {
+  philox_normals2_f64(block, path, k0, k1, z);
+}
+
+// Whole-block walk of the canonical stream for steps of exactly DM draws
+// each (draw k = step DM + c): when DM divides the normals per block, or the
+// normals per block divide DM, Philox blocks fall on step boundaries, so a
+// loop over groups of kSteps steps (= kBlocks blocks) needs no per-draw
+// block test or lane select.  Group g holds steps g kSteps .. g kSteps +
+// kSteps - 1, i.e. blocks g kBlocks .. g kBlocks + kBlocks - 1; a last
+// partial group is generated whole and its tail dropped, as the stream is
+// the same either way.
+template <typename T, int DM>
+struct PhiloxGroup {
+  static constexpr int kNpb = NormalsPerBlock<T>::value;
+  static constexpr bool kAligned = (kNpb % DM == 0) || (DM % kNpb == 0);
+  static constexpr int kSteps = DM < kNpb ? kNpb / DM : 1;
+  static constexpr int kBlocks = DM < kNpb ? 1 : DM / kNpb;
+  static constexpr int kNormals = kSteps * DM;
+  __device__ __forceinline__ static void get(int64_t group, int64_t path, uint32_t k0, uint32_t k1, T* z) {
+#pragma unroll
+    for (int b = 0; b < kBlocks; ++b) philox_normals(group * kBlocks + b, path, k0, k1, z + b * kNpb);
+  }
+};
+
+// dt and sqrt(dt) of a step-table row [dt, sqrt dt, slot, -] with one
+// vector load (the row aligned to two values); GLOBAL reads through the
+// read-only path.
+template <bool GLOBAL>
+__device__ __forceinline__ void step_pair(const float* row, float& dt, float& sdt) {
+  const float2 v = GLOBAL ? __ldg(reinterpret_cast<const float2*>(row)) : *reinterpret_cast<const float2*>(row);
+  dt = v.x;
+  sdt = v.y;
+}
+template <bool GLOBAL>
+__device__ __forceinline__ void step_pair(const double* row, double& dt, double& sdt) {
+  const double2 v = GLOBAL ? __ldg(reinterpret_cast<const double2*>(row)) : *reinterpret_cast<const double2*>(row);
+  dt = v.x;
+  sdt = v.y;
+}
+
 // ---- Sobol normals ------------------------------------------------------------
 // Inverse-normal conversion of a Sobol integer x at nd digits:
 // u = float(x) 2^-nd, z = sqrt(2) erfinv((u - 1/2) 2)
@@ -645,6 +689,26 @@ struct WarpRowStager {
   __device__ __forceinline__ void push(uint32_t w, uint32_t* out, int64_t row_words, int64_t path0, int64_t N) {
     wbuf[(threadIdx.x & 31) * kStride + nw] = w;
     if (++nw == 32) flush(out, row_words, path0, N);
+  }
+  // Appends all DM values of this step without the full-piece test: the
+  // caller runs make_room before the piece could pass 32 words.
+  template <typename T, int DM>
+  __device__ __forceinline__ void append(const T* x) {
+    uint32_t* row = wbuf + (threadIdx.x & 31) * kStride;
+#pragma unroll
+    for (int c = 0; c < DM; ++c) {
+      if constexpr (sizeof(T) == 4) {
+        row[nw++] = __float_as_uint(x[c]);
+      } else {
+        const unsigned long long u = __double_as_longlong(x[c]);
+        row[nw++] = (uint32_t)u;
+        row[nw++] = (uint32_t)(u >> 32);
+      }
+    }
+  }
+  // Flushes the piece unless `words` more still fit in it.
+  __device__ __forceinline__ void make_room(int words, uint32_t* out, int64_t row_words, int64_t path0, int64_t N) {
+    if (nw > 32 - words) flush(out, row_words, path0, N);
   }
   // Appends the first `dim` of the DM values of this step.
   template <typename T, int DM>

@@ -49,6 +49,18 @@ __device__ __forceinline__ void load_coef(GbmCoef<T, DM>* c, int dim, const void
   }
 }
 
+// cs += (mu - sigma^2/2) dt + sqrt(dt) sigma (L z), L lower triangular.
+template <typename T, int DM>
+__device__ __forceinline__ void gbm_advance(const GbmCoef<T, DM>& cf, T (&cs)[DM], const T* z, T dt, T sdt) {
+#pragma unroll
+  for (int r = 0; r < DM; ++r) {
+    T y = T(0);
+#pragma unroll
+    for (int c = 0; c <= r; ++c) y += cf.L[r * DM + c] * z[c];
+    cs[r] += cf.drift[r] * dt + sdt * cf.sigma[r] * y;
+  }
+}
+
 // STAGE: 1 = recorded states go through the coalescing RowStager (dynamic
 // shared memory), chosen when a path's output row is at least 64 bytes; then
 // every thread runs every round and a thread past the last path simulates
@@ -76,6 +88,15 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
       return;
     }
   }
+  // In-kernel Philox draws of exactly DM components per step (table rows
+  // aligned for pair loads): the loop walks whole Philox blocks.
+  using PG = PhiloxGroup<T, DM>;
+  const bool whole_blocks = PG::kAligned && dim == DM && a.draws.source == TQF_DRAWS_PHILOX &&
+                            (reinterpret_cast<uintptr_t>(table) & (2 * sizeof(T) - 1)) == 0;
+  // one-factor coefficients live in registers
+  GbmCoef<T, DM> creg;
+  if constexpr (DM == 1) creg = coef;
+  const GbmCoef<T, DM>* cf = DM == 1 ? &creg : &coef;
   RowStager<T, DM, kBlock> stg(stage_smem, dim);
   WarpRowStager wst(stage_smem);
   uint32_t* out_words = reinterpret_cast<uint32_t*>(out);
@@ -107,37 +128,64 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
           if (j < dim) o[j] = x0[j];
       }
     }
-    DrawSource<T> src(a.draws, pc, dim);
-    for (int i = 0; i < a.num_steps; ++i) {
-      const T dt = table[i * 4], sdt = table[i * 4 + 1];
-      const int slot = (int)table[i * 4 + 2];
-      T z[DM];
+    // records x0 exp(cs) after step i at its slot (STAGE 2: every date, in order)
+    auto record = [&](int i) {
+      if constexpr (STAGE == 2) {
+        T xs[DM];
 #pragma unroll
-      for (int c = 0; c < DM; ++c) z[c] = c < dim ? src.get(i, c) : T(0);
+        for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
+        wst.put<T, DM>(xs, dim, out_words, row_words, warp0, N);
+      } else {
+        const int slot = (int)table[i * 4 + 2];
+        if (slot >= 0) {
+          if constexpr (STAGE == 1) {
+            T xs[DM];
 #pragma unroll
-      for (int r = 0; r < DM; ++r) {
-        T y = T(0);
+            for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
+            stg.put(out, ns, row0, N, slot, xs);
+          } else {
+            T* o = out + (path * ns + slot) * dim;
 #pragma unroll
-        for (int c = 0; c <= r; ++c) y += coef.L[r * DM + c] * z[c];
-        cs[r] += coef.drift[r] * dt + sdt * coef.sigma[r] * y;
-      }
-      if (STAGE == 2 || slot >= 0) {  // STAGE 2: every date, in order
-        if constexpr (STAGE == 2) {
-          T xs[DM];
-#pragma unroll
-          for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
-          wst.put<T, DM>(xs, dim, out_words, row_words, warp0, N);
-        } else if constexpr (STAGE == 1) {
-          T xs[DM];
-#pragma unroll
-          for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
-          stg.put(out, ns, row0, N, slot, xs);
-        } else {
-          T* o = out + (path * ns + slot) * dim;
-#pragma unroll
-          for (int j = 0; j < DM; ++j)
-            if (j < dim) o[j] = x0[j] * exp(cs[j]);
+            for (int j = 0; j < DM; ++j)
+              if (j < dim) o[j] = x0[j] * exp(cs[j]);
+          }
         }
+      }
+    };
+    DrawSource<T> src(a.draws, pc, dim);
+    if (whole_blocks) {
+      // sqrt(dt) carries the antithetic sign: L (sign z) = sign (L z) exactly;
+      // the warp stager makes room for a whole group's words at once
+      constexpr int kGroupWords = PG::kNormals * (int)(sizeof(T) / 4);
+      static_assert(kGroupWords <= 32, "a group's words fit one piece");
+      for (int i = 0; i < a.num_steps; i += PG::kSteps) {
+        if constexpr (STAGE == 2) wst.make_room(kGroupWords, out_words, row_words, warp0, N);
+        T z[PG::kNormals];
+        PG::get(i / PG::kSteps, src.rng.path, src.rng.k0, src.rng.k1, z);
+#pragma unroll
+        for (int s = 0; s < PG::kSteps; ++s) {
+          if (PG::kSteps > 1 && i + s >= a.num_steps) break;
+          T dt, sdt;
+          step_pair<true>(table + (size_t)(i + s) * 4, dt, sdt);
+          gbm_advance<T, DM>(*cf, cs, z + s * DM, dt, sdt * src.sign);
+          if constexpr (STAGE == 2) {
+            T xs[DM];
+#pragma unroll
+            for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
+            wst.append<T, DM>(xs);
+          } else {
+            record(i + s);
+          }
+        }
+      }
+    } else {
+      for (int i = 0; i < a.num_steps; ++i) {
+        const T dt = table[i * 4], sdt = table[i * 4 + 1];
+        T z[DM];
+#pragma unroll
+        for (int c = 0; c < DM; ++c) z[c] = c < dim ? src.get(i, c) : T(0);
+        gbm_advance<T, DM>(*cf, cs, z, dt, sdt);
+        record(i);
       }
     }
     if (STAGE == 1 && stg.cnt > 0) stg.flush(out, ns, row0, N);
