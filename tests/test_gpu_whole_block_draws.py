@@ -1,15 +1,16 @@
 """In-kernel Philox draws taken a whole block at a time (GPU).
 
-When a step takes exactly 1, 2, 4, 8 or 16 normals of the canonical stream
+When a step takes exactly 1, 2, 3 or 4 normals of the canonical stream
 (draw k = step dim + c of path n, four float32 or two float64 normals per
-Philox block), the Euler and exact-GBM path kernels walk whole Philox blocks
-per group of steps instead of testing every draw against the current block.
-The paths must equal, bit for bit, the same kernels reading the stream's
-materialised normals (`generate_mc_normal_draws`, which fills element
-(step, n, c) from draw step dim + c of path n): with every step recorded
-(warp stager) and with the last time only, with a step count that leaves a
-partial last group, with antithetic pairs (the sign carried by sqrt(dt)),
-and for dimensions that keep the per-draw reader (3, 5) as controls.
+Philox block), the Euler and exact-GBM path kernels walk groups of steps
+that use lcm(dim, normals per block) draws, i.e. whole Philox blocks,
+instead of testing every draw against the current block.  The paths must
+equal, bit for bit, the same kernels reading the stream's materialised
+normals (`generate_mc_normal_draws`, which fills element (step, n, c) from
+draw step dim + c of path n): with every step recorded (warp stager) and
+with the last time only, with step counts that leave a partial last group,
+with antithetic pairs (the sign carried by sqrt(dt)), and for dimensions
+that keep the per-draw reader (5, 8) as controls.
 """
 
 import numpy as np

@@ -102,10 +102,13 @@ __global__ void __launch_bounds__(kBlock)
       return;
     }
   }
-  // In-kernel Philox draws of exactly DM components per step with the table
-  // in shared memory: the loop walks whole Philox blocks (PhiloxGroup).
+  // In-kernel Philox draws of exactly DM <= 4 components per step with the
+  // table in shared memory: the loop walks whole Philox blocks (PhiloxGroup).
+  // (From 8 factors on the step's matrix products outweigh the per-draw
+  // block test, and the unrolled group would cost registers.)
   using PG = PhiloxGroup<T, DM>;
-  const bool whole_blocks = SRC == TQF_DRAWS_PHILOX && PG::kAligned && dim == DM && staged;
+  constexpr bool kWhole = SRC == TQF_DRAWS_PHILOX && DM <= 4;
+  const bool whole_blocks = kWhole && dim == DM && staged;
   // one-factor coefficients live in registers
   AffineCoef<T, DM> creg;
   if constexpr (DM == 1) creg = *coef;
@@ -161,7 +164,7 @@ __global__ void __launch_bounds__(kBlock)
       }
     };
     DrawSource<T> src(a.draws, pc, dim);
-    if (whole_blocks) {
+    if (kWhole && whole_blocks) {
       // dw = z (sign sqrt dt) equals (sign z) sqrt dt exactly (sign = +-1);
       // the warp stager makes room for a whole group's words at once
       constexpr int kGroupWords = PG::kNormals * (int)(sizeof(T) / 4);
@@ -169,10 +172,10 @@ __global__ void __launch_bounds__(kBlock)
       for (int i = 0; i < steps; i += PG::kSteps) {
         if constexpr (STAGE == 2) wst.make_room(kGroupWords, out_words, row_words, warp0, N);
         T z[PG::kNormals];
-        PG::get(i / PG::kSteps, src.rng.path, src.rng.k0, src.rng.k1, z);
 #pragma unroll
         for (int s = 0; s < PG::kSteps; ++s) {
           if (PG::kSteps > 1 && i + s >= steps) break;
+          PG::fill_step(i / PG::kSteps, s, src.rng.path, src.rng.k0, src.rng.k1, z);
           T dt, sdt;
           step_pair<false>(table + (size_t)(i + s) * kCols, dt, sdt);
           sdt *= src.sign;
@@ -432,6 +435,7 @@ template <typename T>
 int dispatch_affine(const tqf_euler_affine_args& a, cudaStream_t s) {
   if (a.dim <= 1) return launch_affine<T, 1>(a, s);
   if (a.dim <= 2) return launch_affine<T, 2>(a, s);
+  if (a.dim == 3) return launch_affine<T, 3>(a, s);
   if (a.dim <= 4) return launch_affine<T, 4>(a, s);
   if (a.dim <= 8) return launch_affine<T, 8>(a, s);
   if (a.dim <= 16) return launch_affine<T, 16>(a, s);

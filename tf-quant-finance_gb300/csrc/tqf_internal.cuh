@@ -407,24 +407,31 @@ __device__ __forceinline__ void philox_normals(int64_t block, int64_t path, uint
   philox_normals2_f64(block, path, k0, k1, z);
 }
 
+constexpr int gcd_int(int a, int b) { return b == 0 ? a : gcd_int(b, a % b); }
+
 // Whole-block walk of the canonical stream for steps of exactly DM draws
-// each (draw k = step DM + c): when DM divides the normals per block, or the
-// normals per block divide DM, Philox blocks fall on step boundaries, so a
-// loop over groups of kSteps steps (= kBlocks blocks) needs no per-draw
-// block test or lane select.  Group g holds steps g kSteps .. g kSteps +
-// kSteps - 1, i.e. blocks g kBlocks .. g kBlocks + kBlocks - 1; a last
-// partial group is generated whole and its tail dropped, as the stream is
-// the same either way.
+// each (draw k = step DM + c): a group of kSteps steps takes kNormals =
+// lcm(DM, normals per block) draws, i.e. exactly kBlocks whole Philox
+// blocks, so a loop over groups needs no per-draw block test or lane select.
+// Group g holds steps g kSteps .. g kSteps + kSteps - 1 and blocks g kBlocks
+// .. g kBlocks + kBlocks - 1; a last partial group is generated whole and
+// its tail dropped, as the stream is the same either way.
 template <typename T, int DM>
 struct PhiloxGroup {
   static constexpr int kNpb = NormalsPerBlock<T>::value;
-  static constexpr bool kAligned = (kNpb % DM == 0) || (DM % kNpb == 0);
-  static constexpr int kSteps = DM < kNpb ? kNpb / DM : 1;
-  static constexpr int kBlocks = DM < kNpb ? 1 : DM / kNpb;
-  static constexpr int kNormals = kSteps * DM;
-  __device__ __forceinline__ static void get(int64_t group, int64_t path, uint32_t k0, uint32_t k1, T* z) {
+  static constexpr int kNormals = DM / gcd_int(DM, kNpb) * kNpb;
+  static constexpr int kSteps = kNormals / DM;
+  static constexpr int kBlocks = kNormals / kNpb;
+  // Generates the blocks that begin within step s of the group (z holds the
+  // group's kNormals draws), so that each block is made just before its
+  // first use.
+  __device__ __forceinline__ static void fill_step(int64_t group, int s, int64_t path, uint32_t k0, uint32_t k1,
+                                                   T* z) {
 #pragma unroll
-    for (int b = 0; b < kBlocks; ++b) philox_normals(group * kBlocks + b, path, k0, k1, z + b * kNpb);
+    for (int c = 0; c < DM; ++c) {
+      const int q = s * DM + c;
+      if (q % kNpb == 0) philox_normals(group * kBlocks + q / kNpb, path, k0, k1, z + q);
+    }
   }
 };
 

@@ -88,10 +88,11 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
       return;
     }
   }
-  // In-kernel Philox draws of exactly DM components per step (table rows
-  // aligned for pair loads): the loop walks whole Philox blocks.
+  // In-kernel Philox draws of exactly DM <= 4 components per step (table
+  // rows aligned for pair loads): the loop walks whole Philox blocks.
   using PG = PhiloxGroup<T, DM>;
-  const bool whole_blocks = PG::kAligned && dim == DM && a.draws.source == TQF_DRAWS_PHILOX &&
+  constexpr bool kWhole = DM <= 4;
+  const bool whole_blocks = kWhole && dim == DM && a.draws.source == TQF_DRAWS_PHILOX &&
                             (reinterpret_cast<uintptr_t>(table) & (2 * sizeof(T) - 1)) == 0;
   // one-factor coefficients live in registers
   GbmCoef<T, DM> creg;
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
       }
     };
     DrawSource<T> src(a.draws, pc, dim);
-    if (whole_blocks) {
+    if (kWhole && whole_blocks) {
       // sqrt(dt) carries the antithetic sign: L (sign z) = sign (L z) exactly;
       // the warp stager makes room for a whole group's words at once
       constexpr int kGroupWords = PG::kNormals * (int)(sizeof(T) / 4);
@@ -161,10 +162,10 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
       for (int i = 0; i < a.num_steps; i += PG::kSteps) {
         if constexpr (STAGE == 2) wst.make_room(kGroupWords, out_words, row_words, warp0, N);
         T z[PG::kNormals];
-        PG::get(i / PG::kSteps, src.rng.path, src.rng.k0, src.rng.k1, z);
 #pragma unroll
         for (int s = 0; s < PG::kSteps; ++s) {
           if (PG::kSteps > 1 && i + s >= a.num_steps) break;
+          PG::fill_step(i / PG::kSteps, s, src.rng.path, src.rng.k0, src.rng.k1, z);
           T dt, sdt;
           step_pair<true>(table + (size_t)(i + s) * 4, dt, sdt);
           gbm_advance<T, DM>(*cf, cs, z + s * DM, dt, sdt * src.sign);
@@ -876,6 +877,7 @@ int dispatch_paths(const tqf_mvgbm_args& a, cudaStream_t s) {
     return launch_paths_tc(a, s);
   if (a.dim <= 1) return launch_paths<T, 1>(a, s);
   if (a.dim <= 2) return launch_paths<T, 2>(a, s);
+  if (a.dim == 3) return launch_paths<T, 3>(a, s);
   if (a.dim <= 4) return launch_paths<T, 4>(a, s);
   if (a.dim <= 8) return launch_paths<T, 8>(a, s);
   if (a.dim <= 16) return launch_paths<T, 16>(a, s);
