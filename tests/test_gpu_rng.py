@@ -68,6 +68,27 @@ def test_sobol_normals_close_to_erfinv(cuda):
     np.testing.assert_allclose(got64, want64, rtol=1e-13, atol=1e-13)
 
 
+def test_sobol_normal_f32_every_input_at_20_digits(cuda):
+    """Dimension 0 at 2^20 - 1 points (nd = 20) takes every integer 1 ..
+    2^20 - 1 once (van der Corput), so the float32 inverse normal is checked
+    on every input of that conversion, tails (|x| up to 1 - 2^-19) included:
+    within 6e-7 relative of float64 erfinv (erfinvf's documented 2 ulp, the
+    rounding of the product by sqrt(2) and of the float32 result), and
+    exactly 0 at u = 1/2."""
+    from scipy.special import erfinv
+    from tqf.math.random import sobol
+    n = 2 ** 20 - 1
+    got = sobol.sample_normal(1, n).cpu().numpy()[:, 0].astype(np.float64)
+    ints = osobol.sample_int(1, n, 0)[:, 0].astype(np.int64)
+    assert np.array_equal(np.sort(ints), np.arange(1, n + 1))
+    want = erfinv(ints * 2.0 ** -19 - 1.0) * np.sqrt(2.0)
+    zero = want == 0
+    assert zero.sum() == 1 and got[zero][0] == 0.0
+    rel = np.abs(got[~zero] - want[~zero]) / np.abs(want[~zero])
+    assert rel.max() < 6e-7, rel.max()
+    assert np.array_equal(np.sign(got), np.sign(want))
+
+
 @pytest.mark.parametrize("dim,n,skip", [(1024, 3000, 7), (1030, 1000, 0)])
 def test_sobol_wide_outputs_match_oracle(cuda, dim, n, skip):
     """float32, float32-normal and float64 outputs of wide requests (whole-row

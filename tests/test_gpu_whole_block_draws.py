@@ -84,3 +84,49 @@ def test_univariate_gbm_whole_blocks_equal_materialised(cuda):
     fused = proc.sample_paths(times, initial_state=100.0, num_samples=N, random_type=rt, seed=[1, 2])
     mat = proc.sample_paths(times, initial_state=100.0, normal_draws=z)
     torch.testing.assert_close(fused, mat, rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("d", [16, 17, 32, 64])
+def test_tensor_core_gbm_whole_blocks_equal_materialised(cuda, d):
+    """The tensor-core L z kernel (float32, 16 to 64 factors) takes each
+    16-factor column block's draws as 4 whole Philox blocks when the factor
+    count is a multiple of 16 (17 keeps the per-draw reader)."""
+    from tqf.models import MultivariateGeometricBrownianMotion
+    rng = np.random.default_rng(300 + d)
+    q, _ = np.linalg.qr(rng.standard_normal((d, d)))
+    corr = q @ np.diag(rng.uniform(0.5, 1.5, d)) @ q.T
+    s = np.sqrt(np.diag(corr))
+    corr = corr / s[:, None] / s[None, :]
+    proc = MultivariateGeometricBrownianMotion(d, means=0.03, volatilities=rng.uniform(0.1, 0.4, d), corr_matrix=corr,
+                                               dtype=np.float32)
+    times = np.linspace(0.0, 1.0, 10)[1:].astype(np.float32)
+    N = 1000
+    for antithetic in (False, True):
+        rt, z = _draws(d, len(times), N, antithetic, [3, 4], torch.float32)
+        fused = proc.sample_paths(times, initial_state=np.full(d, 100.0, np.float32), num_samples=N, random_type=rt,
+                                  seed=[3, 4], lz_mode=0)
+        mat = proc.sample_paths(times, initial_state=np.full(d, 100.0, np.float32), normal_draws=z, lz_mode=0)
+        torch.testing.assert_close(fused, mat, rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("d", [3, 4, 8, 16])
+def test_basket_pricing_whole_blocks_equal_materialised(cuda, dtype, d):
+    """The fused basket pricer (terminal log-spots from w = sum sqrt(dt) z)
+    walks whole Philox blocks when the asset count fills its register tile
+    (4, 8, 16; 3 keeps the per-draw reader): prices and pathwise Greeks equal
+    those from the materialised draws."""
+    from tqf.math.random import RandomType
+    from tqf.models import utils
+    from tqf.pricing import basket_european_mc
+    N, steps = 1 << 13, 7
+    corr = 0.5 * np.eye(d) + 0.5
+    kw = dict(spots=np.full(d, 100.0), vols=np.linspace(0.1, 0.4, d), rate=0.02, corr=corr, strike=100.0,
+              expiry=1.0, num_time_steps=steps, num_samples=N, dtype=dtype)
+    for rt in (RandomType.STATELESS, RandomType.STATELESS_ANTITHETIC):
+        q = basket_european_mc(random_type=rt, seed=(5, 9), **kw)
+        draws = utils.generate_mc_normal_draws(d, steps, N, rt, seed=(5, 9), dtype=dtype)
+        ref = basket_european_mc(normal_draws=draws.permute(1, 0, 2), **kw)
+        assert q.price == ref.price
+        np.testing.assert_array_equal(np.asarray(q.delta.cpu()), np.asarray(ref.delta.cpu()))
+        np.testing.assert_array_equal(np.asarray(q.vega.cpu()), np.asarray(ref.vega.cpu()))

@@ -291,6 +291,7 @@ __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_ar
   // whole float4 rows: dim a multiple of 4 (the dispatcher checks the base
   // pointer's 16-byte alignment)
   const bool vec = FULL || (dim & 3) == 0;
+  const bool philox = a.draws.source == TQF_DRAWS_PHILOX;
   uint32_t phase[2] = {0u, 0u};
   const int64_t per_round = (int64_t)gridDim.x * kLzThreads;
   for (int64_t base = 0; base < a.num_paths; base += per_round) {
@@ -329,8 +330,17 @@ __global__ void __launch_bounds__(kLzThreads) mvgbm_paths_tc_kernel(tqf_mvgbm_ar
 #pragma unroll
       for (int kb = 0; kb < KB; ++kb) {
         float z[16];
+        if (FULL && philox) {
+          // the 16 draws of this column block are 4 whole Philox blocks
+          const int64_t b0 = ((int64_t)step * KP + 16 * kb) >> 2;
 #pragma unroll
-        for (int c = 0; c < 16; ++c) z[c] = (FULL || 16 * kb + c < dim) ? src.get(step, 16 * kb + c) : 0.f;
+          for (int q = 0; q < 4; ++q) philox_normals(b0 + q, src.rng.path, src.rng.k0, src.rng.k1, z + 4 * q);
+#pragma unroll
+          for (int c = 0; c < 16; ++c) z[c] *= src.sign;
+        } else {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) z[c] = (FULL || 16 * kb + c < dim) ? src.get(step, 16 * kb + c) : 0.f;
+        }
         uint32_t hi[8], lo[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
@@ -602,11 +612,28 @@ __global__ void __launch_bounds__(kBlock) basket_price_kernel(tqf_basket_args a)
 #pragma unroll
       for (int j = 0; j < DM; ++j) w[j] = T(0);
       DrawSource<T> src(a.draws, path, dim);
-      for (int i = 0; i < a.num_steps; ++i) {
-        const T sdt = sdt_tab[i];
+      using PG = PhiloxGroup<T, DM>;
+      if (dim == DM && a.draws.source == TQF_DRAWS_PHILOX) {
+        // whole Philox blocks per group of steps; sqrt(dt) carries the
+        // antithetic sign (sdt (sign z) = (sign sdt) z exactly)
+        for (int i = 0; i < a.num_steps; i += PG::kSteps) {
+          T z[PG::kNormals];
 #pragma unroll
-        for (int c = 0; c < DM; ++c)
-          if (c < dim) w[c] += sdt * src.get(i, c);
+          for (int s = 0; s < PG::kSteps; ++s) {
+            if (PG::kSteps > 1 && i + s >= a.num_steps) break;
+            PG::fill_step(i / PG::kSteps, s, src.rng.path, src.rng.k0, src.rng.k1, z);
+            const T sdt = sdt_tab[i + s] * src.sign;
+#pragma unroll
+            for (int c = 0; c < DM; ++c) w[c] += sdt * z[s * DM + c];
+          }
+        }
+      } else {
+        for (int i = 0; i < a.num_steps; ++i) {
+          const T sdt = sdt_tab[i];
+#pragma unroll
+          for (int c = 0; c < DM; ++c)
+            if (c < dim) w[c] += sdt * src.get(i, c);
+        }
       }
       T S[DM], y[DM];
       T B = T(0);
