@@ -30,17 +30,22 @@ def test_prepare_grid_matches_oracle(case, dtype):
         np.testing.assert_array_equal(x, y)
 
 
-@pytest.mark.parametrize("seed", range(20))
+@pytest.mark.parametrize("seed", range(60))
 def test_output_slot_plan_matches_oracle(seed):
+    """The vectorised slot plan against the oracle's replay of the
+    reference's written_count loop: short and long grids, sparse to dense
+    kept times, requests that end the loop early or leave slots unwritten."""
     from tqf.models import utils
     rng = np.random.default_rng(seed)
-    n = int(rng.integers(2, 30))
-    keep = rng.random(n) < 0.3
-    k = max(int(keep.sum()), 1) + int(rng.integers(0, 2))
+    n = int(rng.integers(1, 30)) if seed < 30 else int(rng.integers(30, 700))
+    keep = rng.random(n) < rng.choice([0.05, 0.3, 0.5, 1.0])
+    k = max(int(keep.sum()), 1) + int(rng.integers(-1, 3))
+    k = max(k, 1)
     init = int(rng.integers(0, 2))
     a = utils.plan_output_slots(keep, k, init)
     b = ogrids.write_slots(keep, k, init)
     np.testing.assert_array_equal(a[0], b[0])
+    assert a[0].dtype == np.int32
     assert a[1:] == b[1:]
 
 

@@ -141,7 +141,7 @@ def sample(dim, drift_fn, volatility_fn, times, time_step=None, num_time_steps=N
         rows[:, 2] = step_slot
         table = utils.step_table(rows, td, device)
         d = drift_fn.m.shape[0]
-        t = lambda a: torch.as_tensor(np.asarray(a, np.float64), dtype=td).to(device)  # noqa: E731
+        t = lambda a: utils.upload(np.asarray(a, np.float64), td, device)  # noqa: E731  (read-only)
         m, Mx, s0, s1, C = t(drift_fn.m), t(drift_fn.M), t(volatility_fn.s0), t(volatility_fn.s1), t(volatility_fn.C)
         if d != dim:
             raise ValueError(f"structured coefficients have dimension {d}, sample() got dim={dim}")

@@ -191,22 +191,22 @@ class HestonModel(GenericItoProcess):
     def _qe_table(self, all_times, tolerance, step_slot, steps_exec):
         np_dt = self._np_dtype
         dt, (K, TH, XI, RHO) = self._params_on_grid(all_times)
-        rows = np.zeros((steps_exec, QE_COLS), dtype=np.float64)
-        for i in range(steps_exec):
-            h = float(dt[i])
-            k, th, xi, rho = K[i], TH[i], XI[i], RHO[i]
-            E = float(np_dt.type(np.exp(-k * h)))
-            rows[i, 0] = 0.0 if np_dt.type(dt[i]) > np_dt.type(tolerance) else 1.0
-            rows[i, 1] = th
-            rows[i, 2] = E
-            rows[i, 3] = xi * xi * E * (1.0 - E) / k
-            rows[i, 4] = th * xi * xi * (1.0 - E) ** 2 / (2.0 * k)
-            rows[i, 5] = -rho * k * th / xi * h
-            rows[i, 6] = 0.5 * h * (k * rho / xi - 0.5) - rho / xi
-            rows[i, 7] = 0.5 * h * (k * rho / xi - 0.5) + rho / xi
-            rows[i, 8] = 0.5 * h * (1.0 - rho * rho)
-            rows[i, 9] = 0.5 * h * (1.0 - rho * rho)
-            rows[i, 11] = step_slot[i]
+        n = int(steps_exec)
+        h = dt[:n].astype(np.float64)
+        k, th, xi, rho = K[:n], TH[:n], XI[:n], RHO[:n]
+        E = np.exp(-k * h).astype(np_dt).astype(np.float64)  # e^{-kappa dt} in the model's precision
+        rows = np.zeros((n, QE_COLS), dtype=np.float64)
+        rows[:, 0] = np.where(dt[:n].astype(np_dt) > np_dt.type(tolerance), 0.0, 1.0)  # 1: state kept
+        rows[:, 1] = th
+        rows[:, 2] = E
+        rows[:, 3] = xi * xi * E * (1.0 - E) / k
+        rows[:, 4] = th * xi * xi * ((1.0 - E) * (1.0 - E)) / (2.0 * k)
+        rows[:, 5] = -rho * k * th / xi * h
+        rows[:, 6] = 0.5 * h * (k * rho / xi - 0.5) - rho / xi
+        rows[:, 7] = 0.5 * h * (k * rho / xi - 0.5) + rho / xi
+        rows[:, 8] = 0.5 * h * (1.0 - rho * rho)
+        rows[:, 9] = 0.5 * h * (1.0 - rho * rho)
+        rows[:, 11] = step_slot[:n]
         return rows
 
     def expected_total_variance(self, future_times, initial_var, name=None):

@@ -129,21 +129,25 @@ def plan_output_slots(keep_mask, num_requested: int, initial_written_count: int)
     written_count reaches num_requested, and `unwritten` the slots no write
     reaches (left as zeros).
     """
-    steps = len(keep_mask) - 1
-    wc = int(initial_written_count)
-    owner = {0: -1}
-    i = 0
-    while i < steps and wc < num_requested:
-        owner[wc] = i
-        wc += int(keep_mask[i + 1])
-        i += 1
-    step_slot = np.full(i, -1, dtype=np.int32)
-    for slot, step in owner.items():
-        if step >= 0:
-            step_slot[step] = slot
-    init_slot = 0 if owner[0] == -1 else -1
-    unwritten = [s for s in range(num_requested) if s not in owner]
-    return step_slot, init_slot, i, unwritten
+    keep = np.asarray(keep_mask, dtype=bool).reshape(-1)
+    steps = len(keep) - 1
+    k = int(num_requested)
+    # written_count before step i: the start value plus the kept times so far
+    wc = int(initial_written_count) + np.concatenate(
+        [np.zeros(1, np.int64), np.cumsum(keep[1:steps], dtype=np.int64)])[:max(steps, 0)]
+    over = np.flatnonzero(wc >= k)
+    n = int(over[0]) if over.size else steps
+    wc = wc[:n]
+    # a slot is finally held by the last step that writes it
+    last = np.ones(n, dtype=bool)
+    last[:-1] = wc[1:] != wc[:-1]
+    step_slot = np.where(last, wc, -1).astype(np.int32)
+    init_slot = -1 if n > 0 and wc[0] == 0 else 0
+    written = np.zeros(max(k, 1), dtype=bool)
+    written[0] = True
+    written[wc[wc < k]] = True
+    unwritten = np.flatnonzero(~written[:k]).tolist()
+    return step_slot, init_slot, n, unwritten
 
 
 def generate_mc_normal_draws(num_normal_draws, num_time_steps, num_sample_paths, random_type,
