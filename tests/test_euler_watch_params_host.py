@@ -22,7 +22,7 @@ def _z():
     return torch.from_numpy(np.random.default_rng(3).standard_normal((STEPS, M, 2)))
 
 
-def _fake_run_update(x, a, B, step, dt, sqrt_dt, draws, paths, slot, num_slots, device, need_dw):
+def _fake_run_update(x, a, B, step, dt, sqrt_dt, draws, paths, slot, num_slots, device, need_dw, aux=None):
     # x_next = x + dt a + B (z sqrt dt), the update tqf_euler_update computes
     dw = _z()[step, :, : x.shape[1]].to(x.dtype) * sqrt_dt
     x_next = x + dt * a + torch.einsum("mrc,mc->mr", B, dw)

@@ -205,7 +205,7 @@ class _EulerStep(torch.autograd.Function):
         return gx, ga, gB, None, None
 
 
-def _run_update(x, a, B, step, dt, sqrt_dt, draws, paths, slot, num_slots, device, need_dw):
+def _run_update(x, a, B, step, dt, sqrt_dt, draws, paths, slot, num_slots, device, need_dw, aux=None):
     M, d = x.shape
     x_next = torch.empty_like(x)
     args = _lib.EulerUpdateArgs()
@@ -225,8 +225,12 @@ def _run_update(x, a, B, step, dt, sqrt_dt, draws, paths, slot, num_slots, devic
     if need_dw:
         # dw = (x_next - x - dt a) solved through B is ill-posed; instead run the
         # same kernel with a = 0, B = I, x = 0: it returns z sqrt(dt) exactly.
-        eye = torch.eye(d, dtype=x.dtype, device=x.device).expand(M, d, d).contiguous()
-        zero = torch.zeros_like(x)
+        # (`aux` keeps I and 0 across the steps of one call.)
+        aux = {} if aux is None else aux
+        if "eye" not in aux:
+            aux["eye"] = torch.eye(d, dtype=x.dtype, device=x.device).expand(M, d, d).contiguous()
+            aux["zero"] = torch.zeros_like(x)
+        eye, zero = aux["eye"], aux["zero"]
         dw = torch.empty_like(x)
         a2 = _lib.EulerUpdateArgs()
         ctypes_copy(args, a2)
@@ -247,13 +251,16 @@ def _generic(dim, drift_fn, volatility_fn, all_times, dt, sqrt_dt, step_slot, in
              device, differentiable):
     """Per-step loop for arbitrary callables (euler_sampling.py:405-464)."""
     x = torch.broadcast_to(initial_state, batch_shape + (num_samples, dim)).reshape(M, dim)
+    # the step times on the device in one copy (t_{i+1} as a 0-d view per
+    # step): a per-step host scalar copy would wait for the GPU every step
+    t_dev = utils.step_times(all_times, steps_exec, td, device)
     if not differentiable:
         x = x.detach().contiguous()
         paths = (torch.zeros if init_slot < 0 else torch.empty)((M, num_requested, dim), dtype=td, device=device)
         if init_slot >= 0:
             paths[:, init_slot] = x
         for i in range(steps_exec):
-            t = torch.as_tensor(all_times[i + 1], dtype=td, device=device)
+            t = t_dev[i]
             xs = x.reshape(batch_shape + (num_samples, dim))
             a = torch.broadcast_to(drift_fn(t, xs), xs.shape).reshape(M, dim).to(td).contiguous()
             B = torch.broadcast_to(volatility_fn(t, xs), xs.shape + (dim,)).reshape(M, dim, dim).to(td).contiguous()
@@ -265,13 +272,14 @@ def _generic(dim, drift_fn, volatility_fn, all_times, dt, sqrt_dt, step_slot, in
     recorded = [None] * num_requested
     if init_slot >= 0:
         recorded[init_slot] = x
+    aux = {}
     for i in range(steps_exec):
-        t = torch.as_tensor(all_times[i + 1], dtype=td, device=device)
+        t = t_dev[i]
         xs = x.reshape(batch_shape + (num_samples, dim))
         a = torch.broadcast_to(drift_fn(t, xs), xs.shape).reshape(M, dim).to(td).contiguous()
         B = torch.broadcast_to(volatility_fn(t, xs), xs.shape + (dim,)).reshape(M, dim, dim).to(td).contiguous()
         x = _EulerStep.apply(x.contiguous(), a, B, None,
-                             (i, dt[i], sqrt_dt[i], draws, None, -1, num_requested, device, True))
+                             (i, dt[i], sqrt_dt[i], draws, None, -1, num_requested, device, True, aux))
         if step_slot[i] >= 0:
             recorded[int(step_slot[i])] = x
     zero = torch.zeros((M, dim), dtype=td, device=device)

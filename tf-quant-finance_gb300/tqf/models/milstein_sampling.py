@@ -191,10 +191,11 @@ def _generic(dim, drift_fn, volatility_fn, grad_volatility_fn, all_times, dt, sq
              steps_exec, x0, N, draws, paths, num_requested, order, td, device):
     """Per-step loop for arbitrary callables (milstein_sampling.py:356-424, 596-671)."""
     x = torch.broadcast_to(x0, (N, dim)).to(td).contiguous()
+    t_dev = utils.step_times(all_times, steps_exec, td, device)  # one copy, a 0-d view per step
     if init_slot >= 0:
         paths[:, init_slot] = x
     for i in range(steps_exec):
-        t = torch.as_tensor(all_times[i + 1], dtype=td, device=device)
+        t = t_dev[i]
         a_, B, G = _coefficients(drift_fn, volatility_fn, grad_volatility_fn, t, x, N, dim, td)
         x, _ = _run_update(x, a_, B, G, i, dt[i], sqrt_dt[i], draws, order, device, paths, int(step_slot[i]),
                            num_requested)
@@ -241,11 +242,12 @@ def _differentiable(dim, drift_fn, volatility_fn, grad_volatility_fn, all_times,
     """Per-step loop with the states in the autograd graph (the role of the
     reference's custom for_loop with watch_params)."""
     x = torch.broadcast_to(x0, (N, dim)).to(td).contiguous()
+    t_dev = utils.step_times(all_times, steps_exec, td, device)
     recorded = [None] * num_requested
     if init_slot >= 0:
         recorded[init_slot] = x
     for i in range(steps_exec):
-        t = torch.as_tensor(all_times[i + 1], dtype=td, device=device)
+        t = t_dev[i]
         a_, B, G = _coefficients(drift_fn, volatility_fn, grad_volatility_fn, t, x, N, dim, td)
         x = _MilsteinStep.apply(x.contiguous(), a_, B, G, (i, dt[i], sqrt_dt[i], draws, order, device))
         if step_slot[i] >= 0:

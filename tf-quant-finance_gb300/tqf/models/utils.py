@@ -226,6 +226,13 @@ def upload(array, dtype: torch.dtype, device) -> torch.Tensor:
     return t
 
 
+def step_times(all_times, steps_exec: int, dtype: torch.dtype, device) -> torch.Tensor:
+    """t_1 .. t_steps_exec of a grid as one device tensor, for per-step loops
+    that hand each step's time to user callables as a 0-d view (a host
+    scalar copied per step would make the host wait for the GPU every step)."""
+    return torch.as_tensor(np.asarray(all_times[1:int(steps_exec) + 1]), device=device).to(dtype)
+
+
 def step_table(rows: np.ndarray, dtype: torch.dtype, device) -> torch.Tensor:
     """Uploads a [steps, cols] host table (16-byte aligned device copy)."""
     return upload(rows, dtype, device)
