@@ -130,11 +130,11 @@ def plan_output_slots(keep_mask, num_requested: int, initial_written_count: int)
     reaches (left as zeros).
     """
     keep = np.asarray(keep_mask, dtype=bool).reshape(-1)
-    steps = len(keep) - 1
+    steps = max(len(keep) - 1, 0)
     k = int(num_requested)
     # written_count before step i: the start value plus the kept times so far
     wc = int(initial_written_count) + np.concatenate(
-        [np.zeros(1, np.int64), np.cumsum(keep[1:steps], dtype=np.int64)])[:max(steps, 0)]
+        [np.zeros(1, np.int64), np.cumsum(keep[1:steps], dtype=np.int64)])[:steps]
     over = np.flatnonzero(wc >= k)
     n = int(over[0]) if over.size else steps
     wc = wc[:n]
