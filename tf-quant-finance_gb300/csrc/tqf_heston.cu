@@ -143,8 +143,24 @@ __device__ __forceinline__ double qe_sqrt(double a) { return sqrt(a); }
 
 template <typename T>
 __device__ __forceinline__ void qe_step(const T* __restrict__ row, T zv, T zx, T& x, T& v) {
-  if (row[0] != T(0)) return;  // dt <= tolerance: state kept, draws consumed
-  const T theta = row[1], E = row[2], A = row[3], B = row[4];
+  // float rows [skip, theta, E, A | B, k0, k1, k2 | k3, k4, -, slot] are
+  // 16-byte aligned (the table base is, and a row is 48 bytes): three vector
+  // loads; double rows are read value by value, the log-spot constants after
+  // the variance update (loading them up front costs the double kernels up
+  // to 15 registers)
+  T theta, E, A, B, k0, k1, k2, k3, k4;
+  if constexpr (sizeof(T) == 4) {
+    const float4 q0 = reinterpret_cast<const float4*>(row)[0];
+    if (q0.x != 0.f) return;  // dt <= tolerance: state kept, draws consumed
+    const float4 q1 = reinterpret_cast<const float4*>(row)[1];
+    const float4 q2 = reinterpret_cast<const float4*>(row)[2];
+    theta = q0.y; E = q0.z; A = q0.w;
+    B = q1.x; k0 = q1.y; k1 = q1.z; k2 = q1.w;
+    k3 = q2.x; k4 = q2.y;
+  } else {
+    if (row[0] != T(0)) return;
+    theta = row[1]; E = row[2]; A = row[3]; B = row[4];
+  }
   const T m = theta + (v - theta) * E;
   const T s2 = v * A + B;
   const T psi = qe_div(s2, m * m);
@@ -161,7 +177,9 @@ __device__ __forceinline__ void qe_step(const T* __restrict__ row, T zv, T zx, T
     const T u = T(0.5) * (T(1) + qe_erf<T>(qe_div(zv, T(1.41421356237309504880))));
     v_next = u > p ? qe_div(log(T(1) - p) - log(T(1) - u), beta) : T(0);
   }
-  const T k0 = row[5], k1 = row[6], k2 = row[7], k3 = row[8], k4 = row[9];
+  if constexpr (sizeof(T) == 8) {
+    k0 = row[5]; k1 = row[6]; k2 = row[7]; k3 = row[8]; k4 = row[9];
+  }
   x = x + k0 + k1 * v + k2 * v_next + qe_sqrt(k3 * v + k4 * v_next) * zx;
   v = v_next;
 }
