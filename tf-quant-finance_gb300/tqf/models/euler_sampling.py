@@ -259,13 +259,28 @@ def _generic(dim, drift_fn, volatility_fn, all_times, dt, sqrt_dt, step_slot, in
         paths = (torch.zeros if init_slot < 0 else torch.empty)((M, num_requested, dim), dtype=td, device=device)
         if init_slot >= 0:
             paths[:, init_slot] = x
+        # one argument block and one stream lookup for the whole loop: per
+        # step only the pointers, the step index and its dt change
+        args = _lib.EulerUpdateArgs()
+        args.dtype = _lib.dtype_code(td)
+        args.dim = dim
+        args.num_paths = M
+        args.draws = draws
+        args.paths_out = paths.data_ptr()
+        args.num_slots = num_requested
+        stream = _lib.stream_ptr(device)
+        update = _lib.load().tqf_euler_update
+        dts, sdts, slots = [float(v) for v in dt], [float(v) for v in sqrt_dt], [int(v) for v in step_slot]
         for i in range(steps_exec):
             t = t_dev[i]
             xs = x.reshape(batch_shape + (num_samples, dim))
             a = torch.broadcast_to(drift_fn(t, xs), xs.shape).reshape(M, dim).to(td).contiguous()
             B = torch.broadcast_to(volatility_fn(t, xs), xs.shape + (dim,)).reshape(M, dim, dim).to(td).contiguous()
-            x, _ = _run_update(x, a, B, i, dt[i], sqrt_dt[i], draws, paths, int(step_slot[i]),
-                               num_requested, device, False)
+            x_next = torch.empty_like(x)
+            args.step, args.out_slot, args.dt, args.sqrt_dt = i, slots[i], dts[i], sdts[i]
+            args.x, args.drift, args.vol, args.x_next = x.data_ptr(), a.data_ptr(), B.data_ptr(), x_next.data_ptr()
+            _lib.check(update(args, stream), "tqf_euler_update")
+            x = x_next
         return paths.reshape(out_shape)
     # Differentiable route: states kept in the autograd graph.
     x = x.contiguous() if not x.requires_grad else x
