@@ -6,7 +6,8 @@
 // mvgbm_paths_kernel: one thread per path, log-state (the running cumsum of
 //   (mu - sigma^2/2) dt + sqrt(dt) sigma (L z)) in registers; L staged in
 //   shared memory; states x0 * exp(cumsum) stored at their slots as
-//   contiguous [dim] rows (16-byte vector stores).
+//   contiguous [dim] rows (float: the cumsum kept in base 2, one ex2 per
+//   state).
 // basket_price_kernel: the terminal log-state is linear in the draws,
 //   log S_T,i = log S0_i + (mu_i - sigma_i^2/2) T + sigma_i (L w)_i with
 //   w = sum_k sqrt(dt_k) z_k, so the kernel accumulates w (dim FMAs per
@@ -49,6 +50,18 @@ __device__ __forceinline__ void load_coef(GbmCoef<T, DM>* c, int dim, const void
   }
 }
 
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// A recorded state from its log-state: float log-states are kept in base 2
+// (drift and volatility scaled by log2(e) when the coefficients are loaded),
+// so a state is x0 2^cs, one SFU ex2; double ones in base e.
+__device__ __forceinline__ float gbm_level(float x0, float cs) { return x0 * ex2_approx(cs); }
+__device__ __forceinline__ double gbm_level(double x0, double cs) { return x0 * exp(cs); }
+
 // cs += (mu - sigma^2/2) dt + sqrt(dt) sigma (L z), L lower triangular.
 template <typename T, int DM>
 __device__ __forceinline__ void gbm_advance(const GbmCoef<T, DM>& cf, T (&cs)[DM], const T* z, T dt, T sdt) {
@@ -73,6 +86,13 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
   extern __shared__ __align__(16) unsigned char stage_smem[];
   const int dim = a.dim;
   load_coef<T, DM>(&coef, dim, a.chol, a.drift, a.vol);
+  if constexpr (sizeof(T) == 4) {
+    // base-2 log-states (gbm_level); the threads that loaded the values scale them
+    for (int i = threadIdx.x; i < DM; i += blockDim.x) {
+      coef.drift[i] *= 1.4426950408889634f;
+      coef.sigma[i] *= 1.4426950408889634f;
+    }
+  }
   __syncthreads();
   const T* table = static_cast<const T*>(a.step_table);
   T* out = static_cast<T*>(a.output.ptr);
@@ -129,12 +149,12 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
           if (j < dim) o[j] = x0[j];
       }
     }
-    // records x0 exp(cs) after step i at its slot (STAGE 2: every date, in order)
+    // records x0 e^cs (float: 2^cs) after step i at its slot (STAGE 2: every date, in order)
     auto record = [&](int i) {
       if constexpr (STAGE == 2) {
         T xs[DM];
 #pragma unroll
-        for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
+        for (int j = 0; j < DM; ++j) xs[j] = gbm_level(x0[j], cs[j]);
         wst.put<T, DM>(xs, dim, out_words, row_words, warp0, N);
       } else {
         const int slot = (int)table[i * 4 + 2];
@@ -142,13 +162,13 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
           if constexpr (STAGE == 1) {
             T xs[DM];
 #pragma unroll
-            for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
+            for (int j = 0; j < DM; ++j) xs[j] = gbm_level(x0[j], cs[j]);
             stg.put(out, ns, row0, N, slot, xs);
           } else {
             T* o = out + (path * ns + slot) * dim;
 #pragma unroll
             for (int j = 0; j < DM; ++j)
-              if (j < dim) o[j] = x0[j] * exp(cs[j]);
+              if (j < dim) o[j] = gbm_level(x0[j], cs[j]);
           }
         }
       }
@@ -172,7 +192,7 @@ __global__ void __launch_bounds__(kBlock) mvgbm_paths_kernel(tqf_mvgbm_args a) {
           if constexpr (STAGE == 2) {
             T xs[DM];
 #pragma unroll
-            for (int j = 0; j < DM; ++j) xs[j] = x0[j] * exp(cs[j]);
+            for (int j = 0; j < DM; ++j) xs[j] = gbm_level(x0[j], cs[j]);
             wst.append<T, DM>(xs);
           } else {
             record(i + s);
@@ -236,12 +256,6 @@ struct LzSmem {
   uint32_t pad;
   float drift[16 * kLzMaxKB], sigma[16 * kLzMaxKB], x0[16 * kLzMaxKB];  // drift, sigma pre-scaled by log2(e)
 };
-
-__device__ __forceinline__ float ex2_approx(float x) {
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
 
 // FULL: dim == KP (no padded factors), so every normal is drawn and every
 // row is whole float4 stores without per-factor checks.
