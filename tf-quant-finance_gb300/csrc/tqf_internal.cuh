@@ -85,7 +85,9 @@ __host__ __device__ __forceinline__ void mulhilo32(uint32_t a, uint32_t b,
 
 __host__ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0,
                                                         uint32_t k1) {
+#ifdef __CUDA_ARCH__
 #pragma unroll
+#endif
   for (int r = 0; r < 10; ++r) {
     uint32_t hi0, lo0, hi1, lo1;
     mulhilo32(kPhiloxM0, c.x, hi0, lo0);
