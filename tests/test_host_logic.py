@@ -67,6 +67,34 @@ def test_heston_grid_matches_oracle():
     assert len(a[0]) == 253
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_qe_step_table_rows(dtype):
+    """The vectorised QE step table against the row formulas evaluated one
+    step at a time (heston_model.py:522-572 constants; the skip flag for
+    zero-length steps), on a Heston grid with duplicate times and
+    piecewise-constant kappa and rho."""
+    from tqf.math.piecewise import PiecewiseConstantFunc
+    from tqf.models import utils
+    from tqf.models.heston_model import HestonModel
+    kappa = PiecewiseConstantFunc([0.3, 0.6], [1.5, 2.0, 2.5], dtype=dtype)
+    rho = PiecewiseConstantFunc([0.5], [-0.7, -0.4], dtype=dtype)
+    m = HestonModel(kappa, 0.04, 0.3, rho, dtype=dtype)
+    times = np.array([0.25, 0.5, 1.0], dtype)
+    all_times, keep = m._prepare_grid(times, dtype(1.0) / dtype(40), 40, None)
+    step_slot, _, steps_exec, _ = utils.plan_output_slots(keep, len(times), 0)
+    rows = m._qe_table(all_times, 1e-6, step_slot, steps_exec)
+    dt, (K, TH, XI, RHO) = m._params_on_grid(all_times)
+    assert rows.shape == (steps_exec, 12) and (rows[:, 0] == 1.0).sum() >= 2  # duplicate times skipped
+    for i in range(steps_exec):
+        h, k, th, xi, r = float(dt[i]), float(K[i]), float(TH[i]), float(XI[i]), float(RHO[i])
+        E = float(dtype(np.exp(-k * h)))
+        want = [0.0 if dtype(dt[i]) > dtype(1e-6) else 1.0, th, E, xi * xi * E * (1.0 - E) / k,
+                th * xi * xi * (1.0 - E) ** 2 / (2.0 * k), -r * k * th / xi * h,
+                0.5 * h * (k * r / xi - 0.5) - r / xi, 0.5 * h * (k * r / xi - 0.5) + r / xi,
+                0.5 * h * (1.0 - r * r), 0.5 * h * (1.0 - r * r), 0.0, step_slot[i]]
+        np.testing.assert_allclose(rows[i], want, rtol=1e-15, atol=0)
+
+
 def test_argument_errors_follow_the_reference():
     from tqf import InvalidArgumentError
     from tqf.math.random import sobol
