@@ -271,11 +271,19 @@ def _generic(dim, drift_fn, volatility_fn, all_times, dt, sqrt_dt, step_slot, in
         stream = _lib.stream_ptr(device)
         update = _lib.load().tqf_euler_update
         dts, sdts, slots = [float(v) for v in dt], [float(v) for v in sqrt_dt], [int(v) for v in step_slot]
+        ts = t_dev.unbind(0)  # the steps' 0-d time views, made at once
+        plain = not batch_shape  # the state is already [num_samples, dim]
         for i in range(steps_exec):
-            t = t_dev[i]
-            xs = x.reshape(batch_shape + (num_samples, dim))
-            a = torch.broadcast_to(drift_fn(t, xs), xs.shape).reshape(M, dim).to(td).contiguous()
-            B = torch.broadcast_to(volatility_fn(t, xs), xs.shape + (dim,)).reshape(M, dim, dim).to(td).contiguous()
+            t = ts[i]
+            xs = x if plain else x.reshape(batch_shape + (num_samples, dim))
+            a = drift_fn(t, xs)
+            if a.shape != (M, dim) or a.dtype != td or not a.is_contiguous():
+                a = torch.broadcast_to(a, xs.shape).reshape(M, dim).to(td).contiguous()
+            B = volatility_fn(t, xs)
+            if B.shape != (M, dim, dim) or B.dtype != td or not B.is_contiguous():
+                B = torch.broadcast_to(B, xs.shape + (dim,)).reshape(M, dim, dim).to(td).contiguous()
+            if a.device != x.device or B.device != x.device:
+                raise ValueError(f"drift_fn and volatility_fn must return tensors on {x.device}")
             x_next = torch.empty_like(x)
             args.step, args.out_slot, args.dt, args.sqrt_dt = i, slots[i], dts[i], sdts[i]
             args.x, args.drift, args.vol, args.x_next = x.data_ptr(), a.data_ptr(), B.data_ptr(), x_next.data_ptr()
@@ -293,6 +301,8 @@ def _generic(dim, drift_fn, volatility_fn, all_times, dt, sqrt_dt, step_slot, in
         xs = x.reshape(batch_shape + (num_samples, dim))
         a = torch.broadcast_to(drift_fn(t, xs), xs.shape).reshape(M, dim).to(td).contiguous()
         B = torch.broadcast_to(volatility_fn(t, xs), xs.shape + (dim,)).reshape(M, dim, dim).to(td).contiguous()
+        if a.device != x.device or B.device != x.device:
+            raise ValueError(f"drift_fn and volatility_fn must return tensors on {x.device}")
         x = _EulerStep.apply(x.contiguous(), a, B, None,
                              (i, dt[i], sqrt_dt[i], draws, None, -1, num_requested, device, True, aux))
         if step_slot[i] >= 0:

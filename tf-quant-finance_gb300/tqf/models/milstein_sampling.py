@@ -184,6 +184,8 @@ def _coefficients(drift_fn, volatility_fn, grad_volatility_fn, t, x, N, dim, td)
     a_ = torch.broadcast_to(drift_fn(t, x), (N, dim)).to(td).contiguous()
     B = torch.broadcast_to(volatility_fn(t, x), (N, dim, dim)).to(td).contiguous()
     G = _vol_gradient(volatility_fn, grad_volatility_fn, t, x, dim).to(td).contiguous()
+    if a_.device != x.device or B.device != x.device or G.device != x.device:
+        raise ValueError(f"drift_fn, volatility_fn and grad_volatility_fn must return tensors on {x.device}")
     return a_, B, G
 
 
