@@ -15,7 +15,6 @@ import threading
 import numpy as np
 import torch
 
-from tqf import _lib
 from tqf.errors import InvalidArgumentError
 from tqf.math.random import multivariate_normal as mvn
 from tqf.math.random.multivariate_normal import RandomType
