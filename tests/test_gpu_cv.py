@@ -1,6 +1,5 @@
 """Neural control variate kernels against the oracle (GPU)."""
 
-import math
 
 import numpy as np
 import pytest

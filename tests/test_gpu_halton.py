@@ -3,7 +3,6 @@ and the reference's property tests (halton_test.py)."""
 
 import numpy as np
 import pytest
-import torch
 
 from oracle import halton as ohalton
 

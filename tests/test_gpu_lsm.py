@@ -6,7 +6,6 @@ import os
 
 import numpy as np
 import pytest
-import torch
 
 from oracle import lsm as olsm
 

@@ -11,7 +11,6 @@ the reference's bounds; batched means follow the reference's point layout.
 
 import numpy as np
 import pytest
-import torch
 
 pytestmark = pytest.mark.gpu
 

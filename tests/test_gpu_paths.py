@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 import torch
 
-from oracle import closed_form, euler as oeuler, grids as ogrids, heston as oheston, philox as ophilox
+from oracle import closed_form, euler as oeuler, grids as ogrids, heston as oheston
 
 pytestmark = pytest.mark.gpu
 
